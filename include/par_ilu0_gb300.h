@@ -1,0 +1,94 @@
+/*
+ * GB300 extensions of the ILU/GMRES C ABI.  Everything here is additive: the entry
+ * points of ilu_solver_c.h / gmres_c.h keep the reference's behaviour, and these add
+ * what the reference does not expose (a C-level substitution, precision modes, the
+ * learned diagonal shift, the batched solver, analysis results and timings).
+ * Return codes: 0 success, -1 failure (message via LLJBASH_Gb300LastError), -2 a row
+ * without diagonal entry.
+ */
+#pragma once
+
+#include "gmres_c.h"
+#include "ilu_solver_c.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Message of the last failure reported by an entry point of this library in the
+ * calling thread ("" when none). */
+const char* LLJBASH_Gb300LastError(void);
+
+/* x = U^{-1} L^{-1} b with the factors of the last IluSolverFactorize (host arrays of
+ * length n, b == x allowed).  No counterpart in the reference's C ABI: it replaces the
+ * C++-only lljbash::IluSolver::Substitute (include/ilu_solver.hpp:20,
+ * src/ilu_solver.cpp:736-831). */
+int LLJBASH_IluSolverSubstitute(IluSolverHdl hdl, const double* b, double* x);
+
+/* ILU solver options. */
+enum {
+    /* 1 (default): copy the factors into GetMatrix()->value after Factorize, as the
+     * reference's in-place factorisation leaves them; 0: keep them on the device only. */
+    LLJBASH_ILU_OPT_COPY_BACK = 1
+};
+int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
+
+/* Per-row diagonal shift added to a_ii before the next factorisations (host array of
+ * length n; NULL removes it).  The learned-shift path sets it from the MLP. */
+int LLJBASH_IluSolverSetShift(IluSolverHdl hdl, const double* shift);
+
+typedef struct LLJBASH_IluInfo {
+    int n;
+    int nnz;
+    int levels_lower;     /* level sets of the lower dependency DAG */
+    int levels_upper;     /* level sets of the reversed upper DAG */
+    int breakdowns;       /* zero / non-finite pivots in the last Factorize */
+    int first_breakdown;  /* smallest such row, -1 if none */
+    double factor_ms;     /* device time of the last Factorize (factorisation + packing) */
+} LLJBASH_IluInfo;
+int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
+
+/* Integer results of SetupMatrix's analysis (each array of length n, any may be NULL):
+ * diagonal positions, Liu elimination-tree parents of the lower DAG and of the
+ * reversed upper DAG (roots = n), and level depths of both DAGs.  Identical to the
+ * reference's (src/ilu_solver.cpp:276-289, src/subtree.hpp:35-68, :524-551). */
+int LLJBASH_IluSolverGetAnalysis(IluSolverHdl hdl, int* diag, int* etree_lower, int* etree_upper, int* depth_lower,
+                                 int* depth_upper);
+
+/* Host-only form of SetupMatrix's analysis for a CSR pattern (rows column-sorted):
+ * the same five arrays as LLJBASH_IluSolverGetAnalysis plus the level counts.  Touches
+ * no device.  Returns -2 when a row has no diagonal entry. */
+int LLJBASH_Gb300AnalyzePattern(int n, const int* row_ptr, const int* col_idx, int* diag, int* etree_lower,
+                                int* etree_upper, int* depth_lower, int* depth_upper, int* nlevels /* [2] */);
+
+/* GMRES options. */
+enum {
+    LLJBASH_GMRES_OPT_MODE = 1,        /* 0 plain FP64 (default), 1 FP32 cycles in FP64 refinement */
+    LLJBASH_GMRES_OPT_TAU = 2,         /* mixed mode: residual reduction per FP32 cycle (default 1e-6) */
+    LLJBASH_GMRES_OPT_USE_GRAPH = 3,   /* 1 (default): replay each restart cycle as a CUDA graph */
+    LLJBASH_GMRES_OPT_PROFILE = 4,     /* 1: time every kernel with CUDA events (no graph) */
+    LLJBASH_GMRES_OPT_KEEP_MATRIX = 5, /* 1: reuse the device copy of A from the previous Solve */
+    LLJBASH_GMRES_OPT_VERIFY = 6       /* 1 (default): compute the FP64 true residual at exit */
+};
+int LLJBASH_GmresSetOption(GmresHdl hdl, int option, double value);
+
+typedef struct LLJBASH_GmresReport {
+    int mode;
+    int iterations;
+    int cycles;
+    int converged;    /* FP64 true residual <= tolerance at exit */
+    double residual;  /* ||b - A x||_2 at exit, FP64 (-1 if not computed) */
+    double solve_ms;  /* device time of the cycles */
+} LLJBASH_GmresReport;
+int LLJBASH_GmresGetReport(GmresHdl hdl, LLJBASH_GmresReport* report);
+
+/* Kernel categories: 0 residual, 1 forward substitution, 2 backward substitution,
+ * 3 SpMV, 4 CGS dot, 5 CGS axpy+dot, 6 CGS axpy+norm, 7 solution update.  Filled in
+ * profiling mode; accumulated until reset. */
+#define LLJBASH_GMRES_KERNEL_KINDS 8
+int LLJBASH_GmresGetKernelTimes(GmresHdl hdl, double* ms, long long* launches, int nkinds);
+int LLJBASH_GmresResetKernelTimes(GmresHdl hdl);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,212 @@
+/*
+ * Oracle test infrastructure only: never linked into, or called by, the product
+ * library.  Compiled together with the reference's own, unmodified sources
+ * (src/csr_matrix.cpp, src/iluk.cpp, src/ilu_solver.cpp, src/gmres.cpp,
+ * src_c/ilu_solver_c.cpp, src_c/gmres_c.cpp) into oracle/_ref/libref.so by
+ * oracle/build_ref.sh, so that tests and the fixture generator can run the
+ * reference itself through ctypes.
+ *
+ * Everything here is a thin plain-pointer wrapper around reference entry points:
+ *   IlukSymbolic                 src/iluk.cpp:5-54
+ *   IluSolver::SetupMatrix       src/ilu_solver.cpp:225-373
+ *   IluSolver::Factorize         src/ilu_solver.cpp:616-671
+ *   IluSolver::Substitute        src/ilu_solver.cpp:736-831
+ *   PreconditionedGmres::Solve   src/gmres.cpp:138-288
+ *   build_etree_parent           src/subtree.hpp:35-68
+ *   Levelization::levelize       src/subtree.hpp:524-551
+ * The one restated piece is the diagonal-pointer scan (src/ilu_solver.cpp:276-289),
+ * which lives in the private IluSolver::Ext and is three lines long.
+ */
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "csr_matrix.h"
+#include "gmres.hpp"
+#include "ilu_solver.hpp"
+#include "iluk.h"
+#include "subtree.hpp"
+
+using namespace lljbash;
+
+namespace {
+CsrMatrix g_last_f;  // result of the last ref_iluk_symbolic call
+std::vector<int> g_last_nzmap;
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void load_matrix(CsrMatrix* m, int n, const int* rp, const int* ci, const double* val) {
+    const int nnz = rp[n];
+    SetupCsrMatrix(m, n, nnz);
+    std::copy_n(rp, n + 1, m->row_ptr);
+    std::copy_n(ci, nnz, m->col_idx);
+    if (val) {
+        std::copy_n(val, nnz, m->value);
+    } else {
+        std::fill_n(m->value, nnz, 0.0);
+    }
+}
+}  // namespace
+
+extern "C" {
+
+/* IlukSymbolic on A; keeps F and nzmap for ref_iluk_fetch; returns nnz(F). */
+int ref_iluk_symbolic(int n, const int* rp, const int* ci, const double* val, int lof) {
+    CsrMatrix a;
+    load_matrix(&a, n, rp, ci, val);
+    DestroyCsrMatrix(&g_last_f);
+    g_last_f = CsrMatrix();
+    g_last_nzmap.assign(static_cast<size_t>(rp[n]), -1);
+    int knnz = IlukSymbolic(&a, lof, &g_last_f, g_last_nzmap.data());
+    DestroyCsrMatrix(&a);
+    return knnz;
+}
+
+/* Copies the last F (row_ptr[n+1], col_idx[knnz], value[knnz]) and nzmap[nnz(A)].
+ * F's fill entries are left uninitialised by the reference (SetupCsrMatrix does not
+ * zero them); they are written as 0 here, as test/benchmark.cpp:116 does before use. */
+void ref_iluk_fetch(int* f_rp, int* f_ci, double* f_val, int* nzmap) {
+    const int n = g_last_f.size;
+    const int knnz = g_last_f.row_ptr[n];
+    std::copy_n(g_last_f.row_ptr, n + 1, f_rp);
+    std::copy_n(g_last_f.col_idx, knnz, f_ci);
+    if (f_val) {
+        std::fill_n(f_val, knnz, 0.0);
+        for (size_t i = 0; i < g_last_nzmap.size(); ++i) f_val[g_last_nzmap[i]] = g_last_f.value[g_last_nzmap[i]];
+    }
+    if (nzmap) std::copy(g_last_nzmap.begin(), g_last_nzmap.end(), nzmap);
+}
+
+/* diag_ptr[i] = first position in row i with col >= i (src/ilu_solver.cpp:276-289). */
+void ref_diag_ptr(int n, const int* rp, const int* ci, int* diag) {
+    for (int i = 0; i < n; ++i) {
+        for (int ji = rp[i]; ji < rp[i + 1]; ++ji) {
+            if (ci[ji] >= i) {
+                diag[i] = ji;
+                break;
+            }
+        }
+    }
+}
+
+/* Liu elimination tree of the L-DAG (lower != 0) or of the reversed U-DAG, exactly as
+ * SetupMatrix hands them to tree_schedule (src/ilu_solver.cpp:321, :339). Roots get n. */
+void ref_etree(int n, const int* rp, const int* ci, const int* diag, int lower, int* parent) {
+    std::vector<int> stripped(static_cast<size_t>(n), 0);
+    std::vector<int> root(static_cast<size_t>(n) + 1);
+    if (lower) {
+        build_etree_parent(n, 0, n, 1, ConstBiasArray<int>(const_cast<int*>(rp)), diag, ci, stripped.data(),
+                           parent, root.data());
+    } else {
+        build_etree_parent(n, n - 1, -1, -1, ConstBiasArray<int>(const_cast<int*>(diag), 1), rp + 1, ci,
+                           stripped.data(), parent, root.data());
+    }
+}
+
+/* Level depth of every row in the L-DAG (lower != 0) or reversed U-DAG
+ * (Levelization::levelize).  Returns the number of levels. */
+int ref_levels(int n, const int* rp, const int* ci, const int* diag, int lower, int* depth) {
+    Levelization lv;
+    if (lower) {
+        lv.levelize(0, n, 1, ConstBiasArray<int>(const_cast<int*>(rp)), diag, ci);
+    } else {
+        lv.levelize(n - 1, -1, -1, ConstBiasArray<int>(const_cast<int*>(diag), 1), rp + 1, ci);
+    }
+    for (int l = 0; l < lv.nlevels; ++l) {
+        for (int k = lv.lset_ptr[l]; k < lv.lset_ptr[l + 1]; ++k) depth[lv.lset[k]] = l;
+    }
+    return lv.nlevels;
+}
+
+/* In-place ILU on the given pattern (SetupMatrix + Factorize). times[0..1] = setup, factorize (s). */
+void ref_factorize(int n, const int* rp, const int* ci, double* val, int nthreads, double* times) {
+    IluSolver s;
+    s.SetThreads(nthreads);
+    load_matrix(s.GetMatrix(), n, rp, ci, val);
+    double t0 = now_s();
+    s.SetupMatrix();
+    double t1 = now_s();
+    s.Factorize();
+    double t2 = now_s();
+    std::copy_n(s.GetMatrix()->value, rp[n], val);
+    if (times) {
+        times[0] = t1 - t0;
+        times[1] = t2 - t1;
+    }
+}
+
+/* x = U^{-1} L^{-1} b with already-factorised LU values (SetupMatrix + Substitute). */
+void ref_substitute(int n, const int* rp, const int* ci, const double* lu, const double* b, double* x,
+                    int nthreads, int reps, double* seconds) {
+    IluSolver s;
+    s.SetThreads(nthreads);
+    load_matrix(s.GetMatrix(), n, rp, ci, lu);
+    s.SetupMatrix();
+    double t0 = now_s();
+    for (int r = 0; r < std::max(reps, 1); ++r) s.Substitute(b, x);
+    double t1 = now_s();
+    if (seconds) *seconds = (t1 - t0) / std::max(reps, 1);
+}
+
+/* The test/benchmark.cpp:89-131 sequence: IlukSymbolic(A, lof) -> zero F, scatter A
+ * through nzmap -> SetupMatrix -> Factorize -> PreconditionedGmres::Solve(A, rhs, x).
+ * x is in/out (initial guess).  tol is the reference's ABSOLUTE residual tolerance.
+ * times[0..3] = symbolic, setup, factorize, gmres (s); stat[0..1] = mv, precon time.
+ * Returns the reference's success flag; *iters receives its iteration count. */
+int ref_ilu_gmres(int n, const int* rp, const int* ci, const double* val, int lof, const double* rhs,
+                  double* x, double tol, int restart, int maxit, int nthreads, int* iters, double* times,
+                  double* stat) {
+    CsrMatrix a;
+    load_matrix(&a, n, rp, ci, val);
+    IluSolver ilu;
+    ilu.SetThreads(nthreads);
+    PreconditionedGmres gmres;
+    gmres.SetIluPreconditioner(&ilu);
+    gmres.param().tolerance = tol;
+    gmres.param().krylov_subspace_dimension = restart;
+    gmres.param().max_iterations = maxit;
+    const int nnz = rp[n];
+    std::vector<int> nzmap(static_cast<size_t>(nnz));
+    double t0 = now_s();
+    int knnz = IlukSymbolic(&a, lof, ilu.GetMatrix(), nzmap.data());
+    double t1 = now_s();
+    std::memset(ilu.GetMatrix()->value, 0, sizeof(double) * static_cast<size_t>(knnz));
+    for (int i = 0; i < nnz; ++i) ilu.GetMatrix()->value[nzmap[i]] = a.value[i];
+    ilu.SetupMatrix();
+    double t2 = now_s();
+    ilu.Factorize();
+    double t3 = now_s();
+    std::vector<double> b(rhs, rhs + n);
+    auto ret = gmres.Solve(&a, b.data(), x);
+    double t4 = now_s();
+    if (iters) *iters = ret.second;
+    if (times) {
+        times[0] = t1 - t0;
+        times[1] = t2 - t1;
+        times[2] = t3 - t2;
+        times[3] = t4 - t3;
+    }
+    if (stat) {
+        stat[0] = gmres.stat().total_mv_time;
+        stat[1] = gmres.stat().total_precon_time;
+    }
+    DestroyCsrMatrix(&a);
+    return ret.first ? 1 : 0;
+}
+
+/* y = A x through the reference's CsrMatVec (src/csr_matrix.cpp:163-171). */
+void ref_csr_matvec(int n, const int* rp, const int* ci, const double* val, const double* x, double* y) {
+    CsrMatrix a;
+    a.size = n;
+    a.max_nnz = rp[n];
+    a.row_ptr = const_cast<int*>(rp);
+    a.col_idx = const_cast<int*>(ci);
+    a.value = const_cast<double*>(val);
+    CsrMatVec(&a, x, y);
+}
+
+}  // extern "C"

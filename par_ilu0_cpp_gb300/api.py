@@ -1,0 +1,384 @@
+"""Python mirror of the reference's ILU/GMRES interface over the LLJBASH_* C ABI.
+
+The classes follow lljbash::IluSolver / lljbash::PreconditionedGmres
+(include/ilu_solver.hpp:8-30, include/gmres.hpp:9-22 of the reference) and call the
+native library ``lib/libpar-ilu0-gmres_c.so`` through ctypes; every computation runs
+in that library (CUDA kernels for the numeric work, host C++ for the symbolic
+analysis).  There is no Python or CPU fallback: if the library is missing, loading it
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .generators import Csr
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(PKG, "lib")
+C_LIB_PATH = os.path.join(LIB_DIR, "libpar-ilu0-gmres_c.so")
+CORE_LIB_PATH = os.path.join(LIB_DIR, "libpar-ilu0-gmres.so")
+
+_I = ctypes.POINTER(ctypes.c_int)
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+class CsrMatrix(ctypes.Structure):
+    """struct LLJBASH_CsrMatrix (include/csr_matrix.h)."""
+
+    _fields_ = [("size", ctypes.c_int), ("max_nnz", ctypes.c_int), ("row_ptr", _I), ("col_idx", _I),
+                ("value", _D)]
+
+
+class GmresParameters(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("krylov_subspace_dimension", ctypes.c_int),
+                ("max_iterations", ctypes.c_int)]
+
+
+class GmresStat(ctypes.Structure):
+    _fields_ = [("total_init_time", ctypes.c_double), ("total_fgmr_time", ctypes.c_double),
+                ("total_mv_time", ctypes.c_double), ("total_precon_time", ctypes.c_double)]
+
+
+class IluInfo(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("nnz", ctypes.c_int), ("levels_lower", ctypes.c_int),
+                ("levels_upper", ctypes.c_int), ("breakdowns", ctypes.c_int), ("first_breakdown", ctypes.c_int),
+                ("factor_ms", ctypes.c_double)]
+
+
+class GmresReport(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("iterations", ctypes.c_int), ("cycles", ctypes.c_int),
+                ("converged", ctypes.c_int), ("residual", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+
+
+ILU_OPT_COPY_BACK = 1
+GMRES_OPT_MODE = 1
+GMRES_OPT_TAU = 2
+GMRES_OPT_USE_GRAPH = 3
+GMRES_OPT_PROFILE = 4
+GMRES_OPT_KEEP_MATRIX = 5
+GMRES_OPT_VERIFY = 6
+KERNEL_KINDS = ("residual", "sptrsv_lower", "sptrsv_upper", "spmv", "cgs_dot", "cgs_axpy_dot", "cgs_axpy_norm",
+                "update")
+
+_LIB = None
+
+
+def library_path() -> str:
+    return C_LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Loads the C-ABI library (raises OSError / FileNotFoundError if it is not built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.isfile(C_LIB_PATH):
+        raise FileNotFoundError(f"native library not built: {C_LIB_PATH} (run __graft_entry__.build())")
+    lib = ctypes.CDLL(C_LIB_PATH)
+    sig = {
+        "LLJBASH_SetupCsrMatrix": (None, [ctypes.POINTER(CsrMatrix), ctypes.c_int, ctypes.c_int]),
+        "LLJBASH_CopyCsrMatrix": (None, [ctypes.POINTER(CsrMatrix), ctypes.POINTER(CsrMatrix)]),
+        "LLJBASH_CopyCsrMatrixValues": (None, [ctypes.POINTER(CsrMatrix), ctypes.POINTER(CsrMatrix)]),
+        "LLJBASH_DestroyCsrMatrix": (None, [ctypes.POINTER(CsrMatrix)]),
+        "LLJBASH_ReadCsrMatrixMM1": (None, [ctypes.POINTER(CsrMatrix), ctypes.c_char_p]),
+        "LLJBASH_CsrMatVec": (None, [ctypes.POINTER(CsrMatrix), _D, _D]),
+        "LLJBASH_CsrAmdOrder": (ctypes.c_int, [ctypes.POINTER(CsrMatrix), _I, _I]),
+        "LLJBASH_CsrNdOrder": (ctypes.c_int, [ctypes.POINTER(CsrMatrix), _I, _I]),
+        "LLJBASH_IlukSymbolic": (ctypes.c_int, [ctypes.POINTER(CsrMatrix), ctypes.c_int, ctypes.POINTER(CsrMatrix), _I]),
+        "LLJBASH_IluSolverCreate": (ctypes.c_void_p, [ctypes.c_int]),
+        "LLJBASH_IluSolverDestroy": (None, [ctypes.c_void_p]),
+        "LLJBASH_IluSolverGetMatrix": (ctypes.POINTER(CsrMatrix), [ctypes.c_void_p]),
+        "LLJBASH_IluSolverSetup": (ctypes.c_int, [ctypes.c_void_p]),
+        "LLJBASH_IluSolverFactorize": (ctypes.c_int, [ctypes.c_void_p]),
+        "LLJBASH_GmresCreate": (ctypes.c_void_p, []),
+        "LLJBASH_GmresDestroy": (None, [ctypes.c_void_p]),
+        "LLJBASH_GmresGetParameters": (ctypes.POINTER(GmresParameters), [ctypes.c_void_p]),
+        "LLJBASH_GmresGetStat": (ctypes.POINTER(GmresStat), [ctypes.c_void_p]),
+        "LLJBASH_GmresSetPreconditioner": (None, [ctypes.c_void_p, ctypes.c_void_p]),
+        "LLJBASH_GmresSolve": (ctypes.c_bool, [ctypes.c_void_p, ctypes.POINTER(CsrMatrix), _D, _D, _I]),
+        "LLJBASH_Gb300LastError": (ctypes.c_char_p, []),
+        "LLJBASH_IluSolverSubstitute": (ctypes.c_int, [ctypes.c_void_p, _D, _D]),
+        "LLJBASH_IluSolverSetOption": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
+        "LLJBASH_IluSolverSetShift": (ctypes.c_int, [ctypes.c_void_p, _D]),
+        "LLJBASH_IluSolverGetInfo": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(IluInfo)]),
+        "LLJBASH_IluSolverGetAnalysis": (ctypes.c_int, [ctypes.c_void_p, _I, _I, _I, _I, _I]),
+        "LLJBASH_Gb300AnalyzePattern": (ctypes.c_int, [ctypes.c_int, _I, _I, _I, _I, _I, _I, _I, _I]),
+        "LLJBASH_GmresSetOption": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
+        "LLJBASH_GmresGetReport": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GmresReport)]),
+        "LLJBASH_GmresGetKernelTimes": (ctypes.c_int, [ctypes.c_void_p, _D, ctypes.POINTER(ctypes.c_longlong),
+                                                       ctypes.c_int]),
+        "LLJBASH_GmresResetKernelTimes": (ctypes.c_int, [ctypes.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        if hasattr(lib, name):
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().LLJBASH_Gb300LastError().decode()
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_I)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+class HostCsrView:
+    """A CsrMatrix struct pointing at numpy arrays (no copy).  Keep it alive while the
+    library uses it."""
+
+    def __init__(self, a: Csr):
+        self._rp = _i32(a.row_ptr)
+        self._ci = _i32(a.col_idx)
+        self._v = _f64(a.values)
+        self.s = CsrMatrix(a.n, int(self._rp[-1]), _ip(self._rp), _ip(self._ci), _dp(self._v))
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.s)
+
+
+def _fill_owned(dst_ptr, a: Csr) -> None:
+    """SetupCsrMatrix(dst, n, nnz) and copy a's arrays into the library-owned storage."""
+    lib = load()
+    lib.LLJBASH_SetupCsrMatrix(dst_ptr, a.n, a.nnz)
+    m = dst_ptr.contents
+    ctypes.memmove(m.row_ptr, _i32(a.row_ptr).ctypes.data, 4 * (a.n + 1))
+    if a.nnz:
+        ctypes.memmove(m.col_idx, _i32(a.col_idx).ctypes.data, 4 * a.nnz)
+        ctypes.memmove(m.value, _f64(a.values).ctypes.data, 8 * a.nnz)
+
+
+def _owned_to_numpy(m: CsrMatrix) -> Csr:
+    n = m.size
+    rp = np.ctypeslib.as_array(m.row_ptr, shape=(n + 1,)).copy()
+    nnz = int(rp[-1])
+    ci = np.ctypeslib.as_array(m.col_idx, shape=(nnz,)).copy() if nnz else np.zeros(0, np.int32)
+    v = np.ctypeslib.as_array(m.value, shape=(nnz,)).copy() if nnz else np.zeros(0)
+    return Csr(n, rp, ci, v)
+
+
+def iluk_symbolic(a: Csr, lof: int):
+    """IlukSymbolic through the C ABI: returns (F, nzmap) with F's values = A scattered."""
+    lib = load()
+    view = HostCsrView(a)
+    f = CsrMatrix(-1, 0, None, None, None)
+    nzmap = np.empty(a.nnz, dtype=np.int32)
+    knnz = lib.LLJBASH_IlukSymbolic(view.ref, int(lof), ctypes.byref(f), _ip(nzmap))
+    if knnz < 0:
+        raise RuntimeError("IlukSymbolic failed")
+    out = _owned_to_numpy(f)
+    lib.LLJBASH_DestroyCsrMatrix(ctypes.byref(f))
+    return out, nzmap
+
+
+def csr_matvec(a: Csr, x) -> np.ndarray:
+    lib = load()
+    view = HostCsrView(a)
+    xx = _f64(x)
+    y = np.empty(a.n)
+    lib.LLJBASH_CsrMatVec(view.ref, _dp(xx), _dp(y))
+    return y
+
+
+def analyze_pattern(a: Csr):
+    """Host analysis: dict(diag, etree_l, etree_u, depth_l, depth_u, nlev)."""
+    lib = load()
+    n = a.n
+    outs = {k: np.empty(n, dtype=np.int32) for k in ("diag", "etree_l", "etree_u", "depth_l", "depth_u")}
+    nlev = np.zeros(2, dtype=np.int32)
+    rc = lib.LLJBASH_Gb300AnalyzePattern(n, _ip(_i32(a.row_ptr)), _ip(_i32(a.col_idx)), _ip(outs["diag"]),
+                                         _ip(outs["etree_l"]), _ip(outs["etree_u"]), _ip(outs["depth_l"]),
+                                         _ip(outs["depth_u"]), _ip(nlev))
+    if rc != 0:
+        raise RuntimeError(f"analysis failed ({rc}): {last_error()}")
+    outs["nlev"] = nlev
+    return outs
+
+
+class IluSolver:
+    """lljbash::IluSolver over the C ABI (LLJBASH_IluSolver*)."""
+
+    def __init__(self, nthreads: int = 0):
+        self.lib = load()
+        self.h = self.lib.LLJBASH_IluSolverCreate(int(nthreads))
+        self.n = -1
+
+    def close(self):
+        if self.h:
+            self.lib.LLJBASH_IluSolverDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def matrix_ptr(self):
+        return self.lib.LLJBASH_IluSolverGetMatrix(self.h)
+
+    def set_matrix(self, f: Csr) -> None:
+        """GetMatrix() + SetupCsrMatrix + copy (the test/test.c:16-17 pattern)."""
+        _fill_owned(self.matrix_ptr(), f)
+        self.n = f.n
+
+    def set_values(self, values) -> None:
+        m = self.matrix_ptr().contents
+        v = _f64(values)
+        ctypes.memmove(m.value, v.ctypes.data, 8 * v.size)
+
+    def values(self) -> np.ndarray:
+        m = self.matrix_ptr().contents
+        nnz = int(m.row_ptr[m.size])
+        return np.ctypeslib.as_array(m.value, shape=(nnz,)).copy()
+
+    def setup(self) -> int:
+        return self.lib.LLJBASH_IluSolverSetup(self.h)
+
+    def factorize(self) -> int:
+        return self.lib.LLJBASH_IluSolverFactorize(self.h)
+
+    def substitute(self, b) -> np.ndarray:
+        bb = _f64(b).copy()
+        x = np.empty_like(bb)
+        rc = self.lib.LLJBASH_IluSolverSubstitute(self.h, _dp(bb), _dp(x))
+        if rc != 0:
+            raise RuntimeError(f"substitute failed ({rc}): {last_error()}")
+        return x
+
+    def set_option(self, option: int, value: float) -> None:
+        if self.lib.LLJBASH_IluSolverSetOption(self.h, int(option), float(value)) != 0:
+            raise RuntimeError(last_error())
+
+    def set_shift(self, shift) -> None:
+        if shift is None:
+            rc = self.lib.LLJBASH_IluSolverSetShift(self.h, None)
+        else:
+            s = _f64(shift)
+            rc = self.lib.LLJBASH_IluSolverSetShift(self.h, _dp(s))
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def info(self) -> IluInfo:
+        inf = IluInfo()
+        self.lib.LLJBASH_IluSolverGetInfo(self.h, ctypes.byref(inf))
+        return inf
+
+    def analysis(self):
+        n = self.info().n
+        outs = {k: np.empty(n, dtype=np.int32) for k in ("diag", "etree_l", "etree_u", "depth_l", "depth_u")}
+        rc = self.lib.LLJBASH_IluSolverGetAnalysis(self.h, _ip(outs["diag"]), _ip(outs["etree_l"]),
+                                                   _ip(outs["etree_u"]), _ip(outs["depth_l"]), _ip(outs["depth_u"]))
+        if rc != 0:
+            raise RuntimeError(last_error())
+        return outs
+
+
+@dataclass
+class SolveResult:
+    ok: bool
+    iterations: int
+    x: np.ndarray
+    report: GmresReport
+
+
+class Gmres:
+    """lljbash::PreconditionedGmres over the C ABI (LLJBASH_Gmres*)."""
+
+    def __init__(self, tolerance: float = 1e-8, restart: int = 60, max_iterations: int = 200):
+        self.lib = load()
+        self.h = self.lib.LLJBASH_GmresCreate()
+        p = self.params
+        p.tolerance = tolerance
+        p.krylov_subspace_dimension = restart
+        p.max_iterations = max_iterations
+
+    def close(self):
+        if self.h:
+            self.lib.LLJBASH_GmresDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> GmresParameters:
+        return self.lib.LLJBASH_GmresGetParameters(self.h).contents
+
+    @property
+    def stat(self) -> GmresStat:
+        return self.lib.LLJBASH_GmresGetStat(self.h).contents
+
+    def set_preconditioner(self, ilu: IluSolver | None) -> None:
+        self.lib.LLJBASH_GmresSetPreconditioner(self.h, ilu.h if ilu is not None else None)
+
+    def set_option(self, option: int, value: float) -> None:
+        if self.lib.LLJBASH_GmresSetOption(self.h, int(option), float(value)) != 0:
+            raise RuntimeError(last_error())
+
+    def solve(self, a: Csr, rhs, x0=None) -> SolveResult:
+        view = HostCsrView(a)
+        b = _f64(rhs).copy()
+        x = np.zeros(a.n) if x0 is None else _f64(x0).copy()
+        its = ctypes.c_int(0)
+        ok = self.lib.LLJBASH_GmresSolve(self.h, view.ref, _dp(b), _dp(x), ctypes.byref(its))
+        return SolveResult(bool(ok), int(its.value), x, self.report())
+
+    def report(self) -> GmresReport:
+        r = GmresReport()
+        self.lib.LLJBASH_GmresGetReport(self.h, ctypes.byref(r))
+        return r
+
+    def kernel_times(self):
+        k = len(KERNEL_KINDS)
+        ms = np.zeros(k)
+        cnt = np.zeros(k, dtype=np.int64)
+        self.lib.LLJBASH_GmresGetKernelTimes(self.h, _dp(ms), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), k)
+        return {name: (float(ms[i]), int(cnt[i])) for i, name in enumerate(KERNEL_KINDS)}
+
+    def reset_kernel_times(self) -> None:
+        self.lib.LLJBASH_GmresResetKernelTimes(self.h)
+
+
+def ilu_gmres(a: Csr, b, lof: int = 0, tol: float = 1e-8, restart: int = 30, maxit: int = 1000, mode: int = 0,
+              relative: bool = True, x0=None):
+    """The test/benchmark.cpp:89-131 sequence through the C ABI: IlukSymbolic -> set F
+    values -> Setup -> Factorize -> GMRES.  With ``relative`` the absolute tolerance
+    passed to GMRES is tol * ||b||_2 (the reference's test is absolute)."""
+    f, _ = iluk_symbolic(a, lof)
+    ilu = IluSolver()
+    ilu.set_matrix(f)
+    rc = ilu.setup()
+    if rc != 0:
+        raise RuntimeError(f"setup failed ({rc}): {last_error()}")
+    rc = ilu.factorize()
+    if rc != 0:
+        raise RuntimeError(f"factorize failed ({rc}): {last_error()}")
+    g = Gmres(tol * (float(np.linalg.norm(b)) if relative else 1.0), restart, maxit)
+    g.set_preconditioner(ilu)
+    g.set_option(GMRES_OPT_MODE, mode)
+    res = g.solve(a, b, x0)
+    return res, ilu, g

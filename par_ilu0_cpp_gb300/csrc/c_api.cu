@@ -1,0 +1,272 @@
+// C ABI: the reference's LLJBASH_* wrappers (src_c/ilu_solver_c.cpp, src_c/gmres_c.cpp)
+// plus the GB300 extensions of par_ilu0_gb300.h.
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "analysis.hpp"
+#include "gmres.hpp"
+#include "gmres_c.h"
+#include "gmres_impl.hpp"
+#include "ilu_impl.hpp"
+#include "ilu_solver.hpp"
+#include "ilu_solver_c.h"
+#include "par_ilu0_gb300.h"
+
+using lljbash::IluSolver;
+using lljbash::PreconditionedGmres;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(const std::exception& e) {
+    g_last_error = e.what();
+    return std::string(e.what()) == "missing diag" ? -2 : -1;
+}
+
+IluSolver* ilu(IluSolverHdl h) { return static_cast<IluSolver*>(h); }
+PreconditionedGmres* gm(GmresHdl h) { return static_cast<PreconditionedGmres*>(h); }
+
+}  // namespace
+
+extern "C" {
+
+const char* LLJBASH_Gb300LastError(void) { return g_last_error.c_str(); }
+
+IluSolverHdl IluSolverCreate(int nthreads) {
+    auto* h = new IluSolver;
+    h->SetThreads(nthreads);
+    return h;
+}
+
+void IluSolverDestroy(IluSolverHdl hdl) { delete ilu(hdl); }
+
+CsrMatrix* IluSolverGetMatrix(IluSolverHdl hdl) { return ilu(hdl)->GetMatrix(); }
+
+int IluSolverSetup(IluSolverHdl hdl) {
+    try {
+        ilu(hdl)->SetupMatrix();
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+int IluSolverFactorize(IluSolverHdl hdl) {
+    try {
+        ilu(hdl)->Factorize();
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+GmresHdl GmresCreate(void) { return new PreconditionedGmres; }
+
+void GmresDestroy(GmresHdl hdl) { delete gm(hdl); }
+
+GmresParameters* GmresGetParameters(GmresHdl hdl) { return &gm(hdl)->param(); }
+
+const GmresStat* GmresGetStat(GmresHdl hdl) { return &gm(hdl)->stat(); }
+
+void GmresSetPreconditioner(GmresHdl hdl, IluSolverHdl ilu_hdl) { gm(hdl)->SetIluPreconditioner(ilu(ilu_hdl)); }
+
+bool GmresSolve(GmresHdl hdl, const CsrMatrix* mat, double* rhs, double* sol, int* iter) {
+    try {
+        auto ret = gm(hdl)->Solve(mat, rhs, sol);
+        if (iter) *iter = ret.second;
+        return ret.first;
+    } catch (const std::exception& e) {
+        fail(e);
+        if (iter) *iter = 0;
+        return false;
+    }
+}
+
+int LLJBASH_IluSolverSubstitute(IluSolverHdl hdl, const double* b, double* x) {
+    try {
+        ilu(hdl)->Substitute(b, x);
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
+    try {
+        IluSolver* s = ilu(hdl);
+        if (!s->impl()) s->impl_ensure();
+        switch (option) {
+            case LLJBASH_ILU_OPT_COPY_BACK:
+                s->impl()->copy_back = value != 0.0;
+                return 0;
+            default:
+                g_last_error = "unknown ILU option";
+                return -1;
+        }
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int LLJBASH_IluSolverSetShift(IluSolverHdl hdl, const double* shift) {
+    try {
+        IluSolver* s = ilu(hdl);
+        if (!s->impl() || s->impl()->n != s->GetMatrix()->size) throw std::runtime_error("SetupMatrix() must be called first");
+        auto* im = s->impl();
+        if (!shift) {
+            im->shift_active = false;
+            return 0;
+        }
+        im->shift.upload(shift, static_cast<size_t>(im->n), im->stream);
+        GB_CUDA_CHECK(cudaStreamSynchronize(im->stream));
+        im->shift_active = true;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
+    IluSolver* s = ilu(hdl);
+    if (!info) return -1;
+    std::memset(info, 0, sizeof(*info));
+    const auto* im = s->impl();
+    if (!im) {
+        g_last_error = "SetupMatrix() has not been called";
+        return -1;
+    }
+    info->n = im->n;
+    info->nnz = static_cast<int>(im->nnz);
+    info->levels_lower = im->an.nlev_l;
+    info->levels_upper = im->an.nlev_u;
+    info->breakdowns = im->last_breakdowns;
+    info->first_breakdown = im->first_breakdown;
+    info->factor_ms = im->last_factor_ms;
+    return 0;
+}
+
+int LLJBASH_IluSolverGetAnalysis(IluSolverHdl hdl, int* diag, int* etree_lower, int* etree_upper, int* depth_lower,
+                                 int* depth_upper) {
+    const auto* im = ilu(hdl)->impl();
+    if (!im) {
+        g_last_error = "SetupMatrix() has not been called";
+        return -1;
+    }
+    const size_t n = static_cast<size_t>(im->n);
+    auto put = [n](int* dst, const std::vector<int>& v) {
+        if (dst && n) std::memcpy(dst, v.data(), n * sizeof(int));
+    };
+    put(diag, im->an.diag);
+    put(etree_lower, im->an.etree_l);
+    put(etree_upper, im->an.etree_u);
+    put(depth_lower, im->an.depth_l);
+    put(depth_upper, im->an.depth_u);
+    return 0;
+}
+
+int LLJBASH_Gb300AnalyzePattern(int n, const int* row_ptr, const int* col_idx, int* diag, int* etree_lower,
+                                int* etree_upper, int* depth_lower, int* depth_upper, int* nlevels) {
+    try {
+        gb300::Analysis an;
+        gb300::diagonal_pointers(n, row_ptr, col_idx, an.diag);
+        const gb300::DagView gl{row_ptr, col_idx, an.diag.data(), true};
+        const gb300::DagView gu{row_ptr, col_idx, an.diag.data(), false};
+        gb300::elimination_tree(n, gl, an.etree_l);
+        gb300::elimination_tree(n, gu, an.etree_u);
+        an.nlev_l = gb300::level_sets(n, gl, an.depth_l, an.order_l, an.lptr_l);
+        an.nlev_u = gb300::level_sets(n, gu, an.depth_u, an.order_u, an.lptr_u);
+        const size_t sz = static_cast<size_t>(n);
+        auto put = [sz](int* dst, const std::vector<int>& v) {
+            if (dst && sz) std::memcpy(dst, v.data(), sz * sizeof(int));
+        };
+        put(diag, an.diag);
+        put(etree_lower, an.etree_l);
+        put(etree_upper, an.etree_u);
+        put(depth_lower, an.depth_l);
+        put(depth_upper, an.depth_u);
+        if (nlevels) {
+            nlevels[0] = an.nlev_l;
+            nlevels[1] = an.nlev_u;
+        }
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+int LLJBASH_GmresSetOption(GmresHdl hdl, int option, double value) {
+    try {
+        PreconditionedGmres* g = gm(hdl);
+        if (!g->impl()) g->impl_ensure();
+        auto* im = g->impl();
+        switch (option) {
+            case LLJBASH_GMRES_OPT_MODE:
+                if (value != 0.0 && value != 1.0) throw std::runtime_error("mode must be 0 or 1");
+                im->mode = static_cast<int>(value);
+                return 0;
+            case LLJBASH_GMRES_OPT_TAU:
+                if (!(value > 0.0 && value < 1.0)) throw std::runtime_error("tau must be in (0, 1)");
+                im->tau = value;
+                return 0;
+            case LLJBASH_GMRES_OPT_USE_GRAPH:
+                im->use_graph = value != 0.0;
+                return 0;
+            case LLJBASH_GMRES_OPT_PROFILE:
+                im->profile = value != 0.0;
+                return 0;
+            case LLJBASH_GMRES_OPT_KEEP_MATRIX:
+                im->keep_matrix = value != 0.0;
+                return 0;
+            case LLJBASH_GMRES_OPT_VERIFY:
+                im->verify = value != 0.0;
+                return 0;
+            default:
+                g_last_error = "unknown GMRES option";
+                return -1;
+        }
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int LLJBASH_GmresGetReport(GmresHdl hdl, LLJBASH_GmresReport* report) {
+    auto* im = gm(hdl)->impl();
+    if (!report) return -1;
+    std::memset(report, 0, sizeof(*report));
+    if (!im) {
+        report->residual = -1;
+        return 0;
+    }
+    report->mode = im->report.mode;
+    report->iterations = im->report.iterations;
+    report->cycles = im->report.cycles;
+    report->converged = im->report.converged;
+    report->residual = im->report.residual;
+    report->solve_ms = im->report.solve_ms;
+    return 0;
+}
+
+int LLJBASH_GmresGetKernelTimes(GmresHdl hdl, double* ms, long long* launches, int nkinds) {
+    auto* im = gm(hdl)->impl();
+    for (int k = 0; k < nkinds; ++k) {
+        if (ms) ms[k] = (im && k < gb300::kKKinds) ? im->kernel_ms[k] : 0.0;
+        if (launches) launches[k] = (im && k < gb300::kKKinds) ? im->kernel_launches[k] : 0;
+    }
+    return 0;
+}
+
+int LLJBASH_GmresResetKernelTimes(GmresHdl hdl) {
+    auto* im = gm(hdl)->impl();
+    if (im) {
+        for (int k = 0; k < gb300::kKKinds; ++k) {
+            im->kernel_ms[k] = 0.0;
+            im->kernel_launches[k] = 0;
+        }
+    }
+    return 0;
+}
+
+}  // extern "C"

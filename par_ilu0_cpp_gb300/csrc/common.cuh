@@ -1,0 +1,125 @@
+// Shared device helpers: error checking, coherent loads/stores for the sync-free
+// kernels, sentinel values used as "not yet computed" markers, warp reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace gb300 {
+
+#define GB_CUDA_CHECK(expr)                                                                       \
+    do {                                                                                          \
+        cudaError_t gb_err_ = (expr);                                                             \
+        if (gb_err_ != cudaSuccess) {                                                             \
+            throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(gb_err_) + \
+                                     " at " + __FILE__ + ":" + std::to_string(__LINE__));         \
+        }                                                                                         \
+    } while (0)
+
+constexpr int kWarp = 32;
+
+// Device status words (one int array per solver):
+//   [0] a dependency wait gave up (iteration cap reached)
+//   [1] number of zero / non-finite pivots met in the last factorisation
+//   [2] smallest row index with such a pivot (INT_MAX when none)
+enum StatusWord { kStatusTimeout = 0, kStatusBreakdowns = 1, kStatusFirstBreakdown = 2, kStatusWords = 4 };
+
+// Upper bound on polls of one dependency before a wait gives up (about a second).
+constexpr long long kSpinLimit = 1ll << 21;
+
+// "Not yet written" markers for value-as-flag waits.  A computed value is never equal to
+// them: results that are NaN are stored as the canonical quiet NaN instead.
+template <class T>
+struct Sentinel;
+template <>
+struct Sentinel<double> {
+    static constexpr unsigned long long bits = 0xFFFFFFFFFFFFFFFFull;
+    __device__ static double value() { return __longlong_as_double(static_cast<long long>(bits)); }
+    __device__ static bool is(double v) {
+        return static_cast<unsigned long long>(__double_as_longlong(v)) == bits;
+    }
+    __device__ static double canon(double v) { return v != v ? __longlong_as_double(0x7FF8000000000000ll) : v; }
+};
+template <>
+struct Sentinel<float> {
+    static constexpr unsigned int bits = 0xFFFFFFFFu;
+    __device__ static float value() { return __uint_as_float(bits); }
+    __device__ static bool is(float v) { return __float_as_uint(v) == bits; }
+    __device__ static float canon(float v) { return v != v ? __uint_as_float(0x7FC00000u) : v; }
+};
+
+// Loads/stores that go to the point of coherence (L2) at GPU scope.
+__device__ __forceinline__ double ld_relaxed(const double* p) {
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ float ld_relaxed(const float* p) {
+    float v;
+    asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(double* p, double v) {
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(float* p, float v) {
+    asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed_int(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Waits until *p is no longer the sentinel; returns the value.  Gives up after
+// kSpinLimit polls (or as soon as another thread has given up), records the timeout in
+// status[kStatusTimeout] and returns 0.
+template <class T>
+__device__ __forceinline__ T wait_value(const T* p, int* status) {
+    T v = ld_relaxed(p);
+    if (!Sentinel<T>::is(v)) return v;
+    for (long long it = 0; it < kSpinLimit; ++it) {
+        __nanosleep(32);
+        v = ld_relaxed(p);
+        if (!Sentinel<T>::is(v)) return v;
+        if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) return T(0);
+    }
+    atomicExch(status + kStatusTimeout, 1);
+    return T(0);
+}
+
+// Waits until *flag == stamp (acquire).  Same give-up rule as wait_value.
+__device__ __forceinline__ bool wait_flag(const int* flag, int stamp, int* status) {
+    if (ld_acquire(flag) == stamp) return true;
+    for (long long it = 0; it < kSpinLimit; ++it) {
+        __nanosleep(32);
+        if (ld_acquire(flag) == stamp) return true;
+        if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) return false;
+    }
+    atomicExch(status + kStatusTimeout, 1);
+    return false;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class T>
+__host__ __device__ constexpr T ceil_div(T a, T b) {
+    return (a + b - 1) / b;
+}
+
+}  // namespace gb300

@@ -1,0 +1,86 @@
+// Internal state of lljbash::PreconditionedGmres.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device_util.hpp"
+#include "gmres.hpp"
+#include "gmres_kernels.cuh"
+
+namespace gb300 {
+
+// Kernel categories timed in profiling mode.
+enum KernelKind {
+    kKResidual = 0,
+    kKLower,
+    kKUpper,
+    kKSpmv,
+    kKDot,
+    kKAxpyDot,
+    kKAxpyNorm,
+    kKUpdate,
+    kKKinds
+};
+
+// Precision modes of Solve().
+enum SolveMode { kModePlain = 0, kModeMixed = 1 };
+
+struct SolveReport {
+    int mode = 0;
+    int iterations = 0;   // Arnoldi steps over all cycles
+    int cycles = 0;       // restart cycles (outer refinement steps in mixed mode)
+    int converged = 0;    // true FP64 residual <= tolerance at exit (when verified)
+    double residual = -1; // ||b - A x||_2 in FP64 at exit (-1 when not computed)
+    double solve_ms = 0;  // device time of the solve (events around the cycles)
+};
+
+// The per-precision Krylov workspace and its captured cycle graph.
+template <class T>
+struct Krylov {
+    DeviceBuffer<T> V, Z, y;
+    long long ld = 0;
+    int im = 0;
+    int n = 0;
+    cudaGraphExec_t graph = nullptr;
+    const void* graph_key[6] = {};
+    ~Krylov() {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+};
+
+}  // namespace gb300
+
+namespace lljbash {
+
+struct PreconditionedGmres::Impl {
+    gb300::DeviceInfo dev;
+    cudaStream_t stream = nullptr;
+    int n = 0;
+    long long nnz = 0;
+    gb300::DeviceBuffer<int> rp, ci;
+    gb300::DeviceBuffer<double> a64, b, x;
+    gb300::DeviceBuffer<float> a32;
+    gb300::Krylov<double> k64;
+    gb300::Krylov<float> k32;
+    gb300::DeviceBuffer<double> hh, h1, h2, partial;
+    gb300::DeviceBuffer<unsigned> counters;  // [0] reductions
+    gb300::DeviceBuffer<gb300::GmresCtl> ctl;
+    gb300::GmresCtl* ctl_host = nullptr;  // pinned mirror
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int grid_spmv = 0, grid_blas = 0, grid_update = 0;
+
+    int mode = gb300::kModePlain;
+    double tau = 1e-6;             // mixed mode: relative reduction per inner cycle
+    bool use_graph = true;
+    bool profile = false;          // time every kernel with events (no graph)
+    bool keep_matrix = false;      // reuse the device copy of A from the previous Solve
+    bool matrix_loaded = false;
+    bool verify = true;            // compute the FP64 true residual at exit
+    double kernel_ms[gb300::kKKinds] = {};
+    long long kernel_launches[gb300::kKKinds] = {};
+    gb300::SolveReport report;
+
+    ~Impl();
+};
+
+}  // namespace lljbash

@@ -1,0 +1,560 @@
+// Restarted right-preconditioned GMRES(m) on the device: CSR SpMV, the fused CGS2
+// Arnoldi step, Givens / Hessenberg least squares and the solution update.
+//
+// The control flow of the reference's Solve (src/gmres.cpp:138-288) is kept on the
+// device in a GmresCtl record so that a whole restart cycle can be launched as one CUDA
+// graph: the last block of the cycle-start and of each Arnoldi-step kernel evaluates the
+// reference's loop conditions with a single thread and opens the gate of the next step
+// (or closes the cycle); later kernels of the graph check the gate and return at once.
+//
+// Vector layout: Krylov bases V[0..m] and Z[0..m-1] are column blocks of one allocation
+// with leading dimension ld = n rounded up to 256 entries; the padding entries of V are
+// zero and never written with anything else, so whole chunks can be processed without
+// bounds checks.  Basis type T is double (plain path) or float (mixed-precision inner
+// cycles); every reduction (dot products, norms) accumulates in double, and the
+// Hessenberg matrix, rotations and least-squares solution are double.
+#pragma once
+
+#include "common.cuh"
+#include "ilu_kernels.cuh"
+
+namespace gb300 {
+
+constexpr int kMaxKrylov = 128;       // largest supported restart length m
+constexpr int kBlasWarps = 16;        // warps per block of the vector kernels
+constexpr int kBlasThreads = kBlasWarps * kWarp;
+constexpr int kSpmvWarps = 4;
+constexpr int kSpmvStage = 768;       // CSR entries of one 32-row chunk staged in smem
+constexpr int kPartialStride = kMaxKrylov + 8;  // doubles per block in the partial buffers
+
+enum CtlStatus { kCtlRunning = 0, kCtlConverged = 1, kCtlNan = 2 };
+
+// Device-resident state of the reference's Solve loop.
+struct GmresCtl {
+    int its;          // Arnoldi steps over all restarts (reference `its`)
+    int i;            // index of the current / last Arnoldi step of the cycle (`i`)
+    int gate;         // = i while the inner loop continues with step i, else -1
+    int status;       // CtlStatus
+    int im;           // restart length m
+    int maxits;       // max_iterations
+    int steps;        // steps taken in the current cycle
+    int happy;        // the last cycle ended with h_{i+1,i} <= 1e-16
+    double tol;       // absolute tolerance (reference eps1 == tol)
+    double tau;       // relative per-cycle stop (0 = none; mixed-precision inner cycles)
+    double stop;      // per-cycle stop threshold max(tol, tau * beta0)
+    double beta;      // residual norm (cycle start) / its estimate |rs[i+1]|
+    double beta0;     // residual norm at the start of the current cycle
+    double inv_norm;  // 1 / norm of the Krylov vector awaiting normalisation
+};
+
+// Hessenberg storage as in the reference (src/gmres.cpp:152-160): column-major
+// hh[i * (m+1) + j] = H(j, i), followed by c[m+1], s[m+1], rs[m+1].
+struct Hess {
+    double* hh;
+    int im1;
+    __device__ double* c() const { return hh + im1 * (im1 - 1); }
+    __device__ double* s() const { return c() + im1; }
+    __device__ double* rs() const { return s() + im1; }
+};
+
+// ---------------------------------------------------------------------------------
+// Block-level deterministic reductions through per-block partials: every block writes
+// its partial sums, the last block to arrive (atomic counter) adds them up in block
+// order, so results do not depend on scheduling.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+        if (last) *counter = 0u;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// Sums partial[b * kPartialStride + j] over blocks b for j < nv into out[j]; called by
+// the last block only.  Warp w handles j = w, w + 32, ...; lanes stride over blocks.
+__device__ __forceinline__ void reduce_partials(const double* partial, int nblocks, int nv, double* out) {
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    for (int j = w; j < nv; j += kBlasWarps) {
+        double s = 0.0;
+        for (int b = lane; b < nblocks; b += kWarp) s += __ldcg(partial + static_cast<size_t>(b) * kPartialStride + j);
+        s = warp_sum(s);
+        if (lane == 0) out[j] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// CSR SpMV, one warp per chunk of 32 consecutive rows.  The chunk's entries are one
+// contiguous CSR range; they are staged in shared memory with coalesced loads and each
+// lane then sums its row in column order (as CsrMatVec, src/csr_matrix.cpp:163-171).
+// Chunks with more than kSpmvStage entries read their rows directly.
+// ---------------------------------------------------------------------------------
+// Row sums accumulate in the matrix's value type AT (FP64 for the plain path, FP32 for
+// the mixed-precision inner cycles, whose SpMV is FP32 throughout).
+template <class AT, class XT>
+__device__ __forceinline__ AT spmv_row_chunk(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                                             const AT* __restrict__ av, const XT* __restrict__ x, int r0, int* scol,
+                                             AT* sval, int& row_out) {
+    const int lane = threadIdx.x & 31;
+    const int rend = min(r0 + kWarp, n);
+    const int e0 = __ldg(rp + r0);
+    const int e1 = __ldg(rp + rend);
+    const int row = r0 + lane;
+    row_out = row < n ? row : -1;
+    AT acc = AT(0);
+    if (e1 - e0 <= kSpmvStage) {
+        for (int e = e0 + lane; e < e1; e += kWarp) {
+            scol[e - e0] = __ldg(ci + e);
+            sval[e - e0] = __ldg(av + e);
+        }
+        __syncwarp();
+        if (row < n) {
+            const int b = __ldg(rp + row) - e0;
+            const int e = __ldg(rp + row + 1) - e0;
+            for (int p = b; p < e; ++p) acc = fma(sval[p], static_cast<AT>(__ldg(x + scol[p])), acc);
+        }
+        __syncwarp();
+    } else if (row < n) {
+        for (int p = __ldg(rp + row); p < __ldg(rp + row + 1); ++p)
+            acc = fma(__ldg(av + p), static_cast<AT>(__ldg(x + __ldg(ci + p))), acc);
+    }
+    return acc;
+}
+
+// y = A x (gated when launched inside a cycle graph).
+template <class AT, class XT, class YT>
+__global__ void __launch_bounds__(kSpmvWarps * kWarp)
+    spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const AT* __restrict__ av,
+                const XT* __restrict__ x, YT* __restrict__ y, const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    __shared__ int s_col[kSpmvWarps][kSpmvStage];
+    __shared__ AT s_val[kSpmvWarps][kSpmvStage];
+    const int w = threadIdx.x >> 5;
+    const int nchunks = ceil_div(n, kWarp);
+    for (int c = blockIdx.x * kSpmvWarps + w; c < nchunks; c += gridDim.x * kSpmvWarps) {
+        int row;
+        const AT acc = spmv_row_chunk(n, rp, ci, av, x, c * kWarp, s_col[w], s_val[w], row);
+        if (row >= 0) y[row] = static_cast<YT>(acc);
+    }
+}
+
+// Cycle start: r = b - A x (FP64), v0 = r (unnormalised, type T), beta = ||r||_2, then
+// the reference's restart logic (src/gmres.cpp:179-199): stop when beta <= tol,
+// otherwise rs[0] = beta, i = -1 and the inner-loop condition
+// (i < m-1) && (beta > eps1) && (its++ < maxits) opens step 0.
+template <class T>
+__global__ void __launch_bounds__(kSpmvWarps * kWarp)
+    gmres_residual_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ av,
+                          const double* __restrict__ b, const double* __restrict__ x, T* __restrict__ v0, GmresCtl* ctl,
+                          Hess H, double* partial, unsigned* counter) {
+    __shared__ int s_col[kSpmvWarps][kSpmvStage];
+    __shared__ double s_val[kSpmvWarps][kSpmvStage];
+    __shared__ double s_red[kSpmvWarps];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nchunks = ceil_div(n, kWarp);
+    double ss = 0.0;
+    for (int c = blockIdx.x * kSpmvWarps + w; c < nchunks; c += gridDim.x * kSpmvWarps) {
+        int row;
+        const double acc = spmv_row_chunk(n, rp, ci, av, x, c * kWarp, s_col[w], s_val[w], row);
+        if (row >= 0) {
+            const double r = b[row] - acc;
+            v0[row] = static_cast<T>(r);
+            ss = fma(r, r, ss);
+        }
+    }
+    ss = warp_sum(ss);
+    if (lane == 0) s_red[w] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kSpmvWarps; ++k) t += s_red[k];
+        partial[static_cast<size_t>(blockIdx.x) * kPartialStride] = t;
+    }
+    if (!arrive_last(counter)) return;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < static_cast<int>(gridDim.x); ++k) t += __ldcg(partial + static_cast<size_t>(k) * kPartialStride);
+        const double beta = sqrt(t);
+        ctl->beta = beta;
+        ctl->beta0 = beta;
+        ctl->steps = 0;
+        ctl->happy = 0;
+        ctl->i = -1;
+        ctl->gate = -1;
+        ctl->stop = fmax(ctl->tol, ctl->tau * beta);
+        if (beta <= ctl->tol) {
+            ctl->status = kCtlConverged;
+            return;
+        }
+        if (isnan(beta)) {
+            ctl->status = kCtlNan;
+            return;
+        }
+        ctl->inv_norm = 1.0 / beta;
+        H.rs()[0] = beta;
+        if (-1 < ctl->im - 1 && beta > ctl->stop && ctl->its++ < ctl->maxits) {
+            ctl->i = 0;
+            ctl->gate = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Fused CGS2 Arnoldi step.  w = V[s+1] (the SpMV output), basis V[0..s].
+//   dot1:        h1 = V^T w
+//   axpy_dot:    w <- w - V h1;  h2 = V^T w
+//   axpy_norm:   w <- w - V h2;  ||w||; then (last block) H(:,s) = h1 + h2,
+//                H(s+1,s) = ||w||, Givens update and loop control.
+// Work split: each warp owns chunks of R = 32 * RPL consecutive rows.  The updates are
+// row-parallel (lane = rows); the dot products are vector-parallel (lane = basis
+// vector j, summing the chunk sequentially against the chunk of w staged in shared
+// memory), which costs exactly one multiply-add per element and needs no per-chunk
+// reductions — this matters on GB300, whose FP64 rate is far below its bandwidth.
+// For float bases the chunk sums are formed in float and added in double per chunk.
+// ---------------------------------------------------------------------------------
+template <class T>
+struct ChunkCfg;
+template <>
+struct ChunkCfg<double> {
+    static constexpr int RPL = 2;
+    using Acc = double;
+};
+template <>
+struct ChunkCfg<float> {
+    static constexpr int RPL = 4;
+    using Acc = float;
+};
+
+template <class T>
+__device__ __forceinline__ void load_rpl(const T* p, T (&v)[ChunkCfg<T>::RPL]);
+template <>
+__device__ __forceinline__ void load_rpl<double>(const double* p, double (&v)[2]) {
+    const double2 t = *reinterpret_cast<const double2*>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+}
+template <>
+__device__ __forceinline__ void load_rpl<float>(const float* p, float (&v)[4]) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+}
+template <class T>
+__device__ __forceinline__ void store_rpl(T* p, const T (&v)[ChunkCfg<T>::RPL]);
+template <>
+__device__ __forceinline__ void store_rpl<double>(double* p, const double (&v)[2]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+}
+template <>
+__device__ __forceinline__ void store_rpl<float>(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+constexpr int kMaxJPerLane = (kMaxKrylov + 1 + kWarp - 1) / kWarp;
+
+// Accumulates, for the lanes' basis vectors j = lane + 32 k (< nv), the dot product of
+// V[j][r0 : r0 + R) with the chunk of w staged in sw[0 : R).
+template <class T>
+__device__ __forceinline__ void chunk_dots(const T* __restrict__ V, long long ld, int nv, long long r0, const T* sw,
+                                           double (&acc)[kMaxJPerLane]) {
+    constexpr int R = kWarp * ChunkCfg<T>::RPL;
+    using Acc = typename ChunkCfg<T>::Acc;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < kMaxJPerLane; ++k) {
+        const int j = lane + k * kWarp;
+        if (k * kWarp >= nv) break;
+        if (j < nv) {
+            const T* v = V + static_cast<long long>(j) * ld + r0;
+            Acc s = Acc(0);
+#pragma unroll 4
+            for (int r = 0; r < R; r += ChunkCfg<T>::RPL) {
+                T a[ChunkCfg<T>::RPL];
+                load_rpl<T>(v + r, a);
+#pragma unroll
+                for (int u = 0; u < ChunkCfg<T>::RPL; ++u) s = fma(static_cast<Acc>(a[u]), static_cast<Acc>(sw[r + u]), s);
+            }
+            acc[k] += static_cast<double>(s);
+        }
+    }
+}
+
+// Writes each warp's per-j sums to shared memory, sums the warps, stores the block
+// partials.  acc_s is [kBlasWarps][kMaxKrylov + 1].
+__device__ __forceinline__ void block_dots_to_partial(double (*acc_s)[kMaxKrylov + 1], const double (&acc)[kMaxJPerLane],
+                                                      int nv, double* partial) {
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kMaxJPerLane; ++k) {
+        const int j = lane + k * kWarp;
+        if (j < nv) acc_s[w][j] = acc[k];
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < kBlasWarps; ++k) s += acc_s[k][j];
+        partial[static_cast<size_t>(blockIdx.x) * kPartialStride + j] = s;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlasThreads)
+    cgs_dot_kernel(long long nchunks, long long ld, const T* __restrict__ V, int s, double* partial, double* h1,
+                   unsigned* counter, const int* gate) {
+    if (gate_closed(gate, s)) return;
+    constexpr int R = kWarp * ChunkCfg<T>::RPL;
+    __shared__ double acc_s[kBlasWarps][kMaxKrylov + 1];
+    __shared__ __align__(16) T sw[kBlasWarps][R];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nv = s + 1;
+    const T* wv = V + static_cast<long long>(s + 1) * ld;
+    double acc[kMaxJPerLane];
+#pragma unroll
+    for (int k = 0; k < kMaxJPerLane; ++k) acc[k] = 0.0;
+    for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
+         c += static_cast<long long>(gridDim.x) * kBlasWarps) {
+        const long long r0 = c * R;
+        T a[ChunkCfg<T>::RPL];
+        load_rpl<T>(wv + r0 + lane * ChunkCfg<T>::RPL, a);
+        store_rpl<T>(&sw[w][lane * ChunkCfg<T>::RPL], a);
+        __syncwarp();
+        chunk_dots<T>(V, ld, nv, r0, sw[w], acc);
+        __syncwarp();
+    }
+    block_dots_to_partial(acc_s, acc, nv, partial);
+    if (!arrive_last(counter)) return;
+    reduce_partials(partial, gridDim.x, nv, h1);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlasThreads)
+    cgs_axpy_dot_kernel(long long nchunks, long long ld, T* __restrict__ V, int s, const double* __restrict__ h1,
+                        double* partial, double* h2, unsigned* counter, const int* gate) {
+    if (gate_closed(gate, s)) return;
+    constexpr int RPL = ChunkCfg<T>::RPL;
+    constexpr int R = kWarp * RPL;
+    __shared__ double acc_s[kBlasWarps][kMaxKrylov + 1];
+    __shared__ __align__(16) T sw[kBlasWarps][R];
+    __shared__ double sh[kMaxKrylov + 1];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nv = s + 1;
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = __ldcg(h1 + j);
+    __syncthreads();
+    T* wv = V + static_cast<long long>(s + 1) * ld;
+    double acc[kMaxJPerLane];
+#pragma unroll
+    for (int k = 0; k < kMaxJPerLane; ++k) acc[k] = 0.0;
+    for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
+         c += static_cast<long long>(gridDim.x) * kBlasWarps) {
+        const long long r0 = c * R + lane * RPL;
+        using Acc = typename ChunkCfg<T>::Acc;
+        T a[RPL];
+        Acc x[RPL];
+        load_rpl<T>(wv + r0, a);
+#pragma unroll
+        for (int u = 0; u < RPL; ++u) x[u] = static_cast<Acc>(a[u]);
+        for (int j = 0; j < nv; ++j) {
+            T v[RPL];
+            load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
+            const Acc hj = static_cast<Acc>(sh[j]);
+#pragma unroll
+            for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < RPL; ++u) a[u] = static_cast<T>(x[u]);
+        store_rpl<T>(wv + r0, a);
+        store_rpl<T>(&sw[w][lane * RPL], a);
+        __syncwarp();
+        chunk_dots<T>(V, ld, nv, c * R, sw[w], acc);
+        __syncwarp();
+    }
+    block_dots_to_partial(acc_s, acc, nv, partial);
+    if (!arrive_last(counter)) return;
+    reduce_partials(partial, gridDim.x, nv, h2);
+}
+
+// Givens update and loop control for step s (single thread).  Mirrors
+// src/gmres.cpp:218-262 and the loop header at :199.
+__device__ __forceinline__ void arnoldi_control(GmresCtl* ctl, Hess H, int s, const double* h1, const double* h2,
+                                                double t) {
+    constexpr double epsmac = 1e-16;
+    const int im1 = H.im1;
+    const int i = s;
+    const int i1 = i + 1;
+    double* hh = H.hh;
+    double* c = H.c();
+    double* sn = H.s();
+    double* rs = H.rs();
+    const int ptih = i * im1;
+    for (int j = 0; j <= i; ++j) hh[ptih + j] = h1[j] + h2[j];
+    hh[ptih + i1] = t;
+    ctl->i = i;
+    ctl->steps = i + 1;
+    if (t <= epsmac) {  // happy breakdown: leave the inner loop before the rotation
+        ctl->happy = 1;
+        ctl->gate = -1;
+        return;
+    }
+    ctl->inv_norm = 1.0 / t;
+    for (int k = 1; k <= i; ++k) {
+        const int k1 = k - 1;
+        const double tt = hh[ptih + k1];
+        hh[ptih + k1] = c[k1] * tt + sn[k1] * hh[ptih + k];
+        hh[ptih + k] = -sn[k1] * tt + c[k1] * hh[ptih + k];
+    }
+    double gam = sqrt(hh[ptih + i] * hh[ptih + i] + hh[ptih + i1] * hh[ptih + i1]);
+    if (gam == 0.0) gam = epsmac;
+    c[i] = hh[ptih + i] / gam;
+    sn[i] = hh[ptih + i1] / gam;
+    rs[i1] = -sn[i] * rs[i];
+    rs[i] = c[i] * rs[i];
+    hh[ptih + i] = c[i] * hh[ptih + i] + sn[i] * hh[ptih + i1];
+    const double beta = fabs(rs[i1]);
+    ctl->beta = beta;
+    if (isnan(beta)) {
+        ctl->status = kCtlNan;
+        ctl->gate = -1;
+        return;
+    }
+    if (i < ctl->im - 1 && beta > ctl->stop && ctl->its++ < ctl->maxits) {
+        ctl->i = i + 1;
+        ctl->gate = i + 1;
+    } else {
+        ctl->gate = -1;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlasThreads)
+    cgs_axpy_norm_kernel(long long nchunks, long long ld, T* __restrict__ V, int s, const double* __restrict__ h1,
+                         const double* __restrict__ h2, double* partial, unsigned* counter, GmresCtl* ctl, Hess H,
+                         const int* gate) {
+    if (gate_closed(gate, s)) return;
+    constexpr int RPL = ChunkCfg<T>::RPL;
+    constexpr int R = kWarp * RPL;
+    __shared__ double sh[kMaxKrylov + 1];
+    __shared__ double s_red[kBlasWarps];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nv = s + 1;
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = __ldcg(h2 + j);
+    __syncthreads();
+    T* wv = V + static_cast<long long>(s + 1) * ld;
+    double ss = 0.0;
+    for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
+         c += static_cast<long long>(gridDim.x) * kBlasWarps) {
+        const long long r0 = c * R + lane * RPL;
+        using Acc = typename ChunkCfg<T>::Acc;
+        T a[RPL];
+        Acc x[RPL];
+        load_rpl<T>(wv + r0, a);
+#pragma unroll
+        for (int u = 0; u < RPL; ++u) x[u] = static_cast<Acc>(a[u]);
+        for (int j = 0; j < nv; ++j) {
+            T v[RPL];
+            load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
+            const Acc hj = static_cast<Acc>(sh[j]);
+#pragma unroll
+            for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
+        }
+        typename ChunkCfg<T>::Acc q = 0;
+#pragma unroll
+        for (int u = 0; u < RPL; ++u) {
+            a[u] = static_cast<T>(x[u]);
+            q = fma(static_cast<typename ChunkCfg<T>::Acc>(a[u]), static_cast<typename ChunkCfg<T>::Acc>(a[u]), q);
+        }
+        ss += static_cast<double>(q);
+        store_rpl<T>(wv + r0, a);
+    }
+    ss = warp_sum(ss);
+    if (lane == 0) s_red[w] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kBlasWarps; ++k) t += s_red[k];
+        partial[static_cast<size_t>(blockIdx.x) * kPartialStride] = t;
+    }
+    if (!arrive_last(counter)) return;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < static_cast<int>(gridDim.x); ++k) t += __ldcg(partial + static_cast<size_t>(k) * kPartialStride);
+        arnoldi_control(ctl, H, s, h1, h2, sqrt(t));
+    }
+}
+
+// Least-squares back substitution rs[0..i] <- H(0..i, 0..i)^{-1} rs (src/gmres.cpp:265-272),
+// single thread.  Skipped when the cycle took no step or ended on NaN.
+static __global__ void gmres_backsolve_kernel(GmresCtl* ctl, Hess H) {
+    if (threadIdx.x != 0 || ctl->status != kCtlRunning || ctl->steps == 0) return;
+    const int i = ctl->i;
+    const int im1 = H.im1;
+    double* hh = H.hh;
+    double* rs = H.rs();
+    const int ptih = i * im1;
+    rs[i] = rs[i] / hh[ptih + i];
+    for (int ii = i - 1; ii >= 0; --ii) {
+        double t = rs[ii];
+        for (int j = ii + 1; j <= i; ++j) t -= hh[j * im1 + ii] * rs[j];
+        rs[ii] = t / hh[ii * im1 + ii];
+    }
+}
+
+// x += sum_{j<=i} rs[j] Z[j] (src/gmres.cpp:274-276, j ascending) and Z[j] <- sentinel
+// (the backward substitution of the next cycle waits on it).  Row-parallel.
+template <class T>
+__global__ void __launch_bounds__(256)
+    gmres_update_kernel(int n, long long ld, T* __restrict__ Z, double* __restrict__ x, const GmresCtl* ctl, Hess H) {
+    if (ctl->status != kCtlRunning || ctl->steps == 0) return;
+    const int nz = ctl->i + 1;
+    const double* rs = H.rs();
+    // plain path: x += sum_j rs[j] z_j in FP64 in ascending j; mixed path: the
+    // correction sum_j rs[j] z_j is formed in FP32 and added to the FP64 x.
+    using Acc = typename ChunkCfg<T>::Acc;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        Acc d = Acc(0);
+        double xv = x[r];
+        for (int j = 0; j < nz; ++j) {
+            T* zj = Z + static_cast<long long>(j) * ld + r;
+            if constexpr (sizeof(Acc) == sizeof(double)) {
+                xv = fma(rs[j], static_cast<double>(*zj), xv);
+            } else {
+                d = fma(static_cast<Acc>(rs[j]), static_cast<Acc>(*zj), d);
+            }
+            *zj = Sentinel<T>::value();
+        }
+        x[r] = xv + static_cast<double>(d);
+    }
+}
+
+// z = v for an unpreconditioned solve (identity preconditioner), gated.
+template <class T>
+__global__ void copy_scaled_kernel(int n, T* v, const double* scale, T* z, const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    const T sc = static_cast<T>(*scale);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const T a = v[r] * sc;
+        v[r] = a;
+        z[r] = a;
+    }
+}
+
+template <class S, class D>
+__global__ void convert_kernel(long long n, const S* __restrict__ s, D* __restrict__ d) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        d[i] = static_cast<D>(s[i]);
+}
+
+}  // namespace gb300

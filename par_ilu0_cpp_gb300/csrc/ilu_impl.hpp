@@ -1,0 +1,107 @@
+// Internal state of lljbash::IluSolver (shared by the ILU and GMRES translation units).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "device_util.hpp"
+#include "ilu_kernels.cuh"
+#include "ilu_solver.hpp"
+
+namespace gb300 {
+
+// One packed triangular factor (see PackedTri): schedule arrays plus packed values in
+// FP64 and FP32.
+struct TriPack {
+    int ntask = 0;
+    long long slots = 0;
+    DeviceBuffer<int> rows, off, len, cols, src, dsrc;
+    DeviceBuffer<double> v64, d64;
+    DeviceBuffer<float> v32, d32;
+
+    template <class T>
+    PackedTri<T> view() const;
+};
+
+template <>
+inline PackedTri<double> TriPack::view<double>() const {
+    PackedTri<double> p;
+    p.ntask = ntask;
+    p.rows = rows.get();
+    p.off = off.get();
+    p.len = len.get();
+    p.cols = cols.get();
+    p.vals = v64.get();
+    p.dvals = d64.get();
+    return p;
+}
+template <>
+inline PackedTri<float> TriPack::view<float>() const {
+    PackedTri<float> p;
+    p.ntask = ntask;
+    p.rows = rows.get();
+    p.off = off.get();
+    p.len = len.get();
+    p.cols = cols.get();
+    p.vals = v32.get();
+    p.dvals = d32.get();
+    return p;
+}
+
+// Host-side results of the pattern analysis (integer output identical to the
+// reference's; see analysis.hpp).
+struct Analysis {
+    std::vector<int> diag;
+    std::vector<int> etree_l, etree_u;
+    std::vector<int> depth_l, depth_u;
+    std::vector<int> order_l, order_u;
+    std::vector<int> lptr_l, lptr_u;
+    int nlev_l = 0, nlev_u = 0;
+};
+
+}  // namespace gb300
+
+namespace lljbash {
+
+struct IluSolver::Impl {
+    gb300::DeviceInfo dev;
+    cudaStream_t stream = nullptr;
+    int n = 0;
+    long long nnz = 0;
+    gb300::Analysis an;
+
+    gb300::DeviceBuffer<int> rp, ci, diag, order_l;
+    gb300::DeviceBuffer<double> lu;
+    gb300::DeviceBuffer<double> shift;      // per-row diagonal shift (learned), optional
+    gb300::DeviceBuffer<int> done;          // per-row ready stamps of the factorisation
+    gb300::DeviceBuffer<unsigned> counters;  // ticket counters [0] fact, [1] L, [2] U
+    gb300::DeviceBuffer<int> status;         // StatusWord array
+    gb300::TriPack L, U;
+    gb300::DeviceBuffer<double> sb64, sy64, sx64;  // Substitute() work vectors
+    gb300::DeviceBuffer<float> sy32;               // FP32 forward-sweep intermediate
+
+    int stamp = 0;
+    bool factorized = false;
+    bool copy_back = true;       // copy the factors into GetMatrix()->value after Factorize
+    bool shift_active = false;   // add `shift` to the diagonal in the next Factorize
+    int last_breakdowns = 0;
+    int first_breakdown = -1;
+    float last_factor_ms = 0.f;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int grid_fact = 0, grid_solve64 = 0, grid_solve32 = 0;
+
+    ~Impl();
+
+    // Device-side substitution pieces, used by GMRES (gated) and by Substitute().
+    // lower: y = L^{-1}(scale * b) (b rescaled in place when scale != null);
+    // upper: x = U^{-1} y (y reset to the sentinel).
+    template <class T>
+    void launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const;
+    template <class T>
+    void launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const;
+    // Throws when a dependency wait timed out since the last call.
+    void check_status(cudaStream_t s);
+};
+
+}  // namespace lljbash

@@ -1,0 +1,281 @@
+// Sync-free ILU factorisation and triangular-substitution kernels.
+//
+// Scheduling (all kernels here): warps take work items from an atomic ticket counter in
+// a fixed topological order — rows sorted by level of the dependency DAG, ascending row
+// index inside a level (the reference's Levelization lset, src/subtree.hpp:524-551).
+// An item only waits for items with smaller tickets; a ticket is only ever held by a
+// running warp, and a warp processes its tickets in increasing order, so the warp
+// holding the smallest unfinished ticket can always proceed: no deadlock, and no
+// assumption that the whole grid is co-resident.  The next ticket is fetched before the
+// current item is processed (its latency is hidden).  The last warp to fetch (it draws
+// ticket ntask + W - 1, W = warps in the grid) resets the counter for the next launch.
+// Every wait is bounded (common.cuh) and reports a timeout instead of hanging.  This
+// replaces the reference's OpenMP subtree partition + spin-wait queue
+// (src/ilu_solver.cpp:394-443).
+#pragma once
+
+#include "common.cuh"
+
+namespace gb300 {
+
+constexpr int kFactWarps = 8;    // warps per block of the factorisation kernel
+constexpr int kFactCap = 256;    // row length staged in shared memory per warp
+constexpr int kSolveWarps = 8;   // warps per block of the substitution kernels
+
+// Binary search of c in the sorted s[lo, hi); returns the position or -1.
+template <class P>
+__device__ __forceinline__ int find_sorted(const P* s, int lo, int hi, int c) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int v = s[mid];
+        if (v < c) {
+            lo = mid + 1;
+        } else if (v > c) {
+            hi = mid;
+        } else {
+            return mid;
+        }
+    }
+    return -1;
+}
+
+// Draws the warp's next ticket (lane 0 does the atomic); resets the counter when this is
+// the grid's final draw.
+__device__ __forceinline__ int draw_ticket(unsigned* counter, int ntask, int lane) {
+    int t = 0;
+    if (lane == 0) {
+        t = static_cast<int>(atomicAdd(counter, 1u));
+        const int nwarps = static_cast<int>(gridDim.x * (blockDim.x >> 5));
+        if (t == ntask + nwarps - 1) atomicExch(counter, 0u);
+    }
+    return __shfl_sync(0xffffffffu, t, 0);
+}
+
+// Kernels launched inside a GMRES cycle graph carry a gate: they run only while
+// *gate == step (the cycle is still active at that step).
+__device__ __forceinline__ bool gate_closed(const int* gate, int step) {
+    return gate != nullptr && *gate != step;
+}
+
+// Numeric ILU on a fixed pattern, one warp per row (the up-looking row elimination of
+// src/ilu_solver.cpp:553-589).  For row j and each pivot column k of its strict-lower
+// part in ascending order: l_jk = a_jk / u_kk, then a_jc -= u_kc * l_jk for every column
+// c of row k's strict-upper part that is also in row j's pattern.  Lanes split row k's
+// entries; every entry of row j therefore receives its updates in ascending k, the same
+// sequence of operations as the reference.  Row j is staged in shared memory (global
+// memory for rows longer than kFactCap).  Row k's values are read at L2 (ld.cg) after an
+// acquire on row k's ready flag; row j publishes with fence + release.
+// `shift` (optional) is added to the diagonal before elimination.
+static __global__ void __launch_bounds__(kFactWarps * kWarp)
+    ilu_factor_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const int* __restrict__ diag,
+                      const int* __restrict__ order, double* lu, const double* __restrict__ shift, int* done,
+                      int stamp, unsigned* counter, int* status) {
+    __shared__ int s_col[kFactWarps][kFactCap];
+    __shared__ double s_val[kFactWarps][kFactCap];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    int q = draw_ticket(counter, n, lane);
+    while (q < n) {
+        const int qn = draw_ticket(counter, n, lane);
+        const int j = order[q];
+        const int b = rp[j];
+        const int len = rp[j + 1] - b;
+        const int dloc = diag[j] - b;
+        for (int t = lane; t < dloc; t += kWarp) wait_flag(done + ci[b + t], stamp, status);
+        __syncwarp();
+        if (len <= kFactCap) {
+            int* scol = s_col[w];
+            double* sval = s_val[w];
+            for (int t = lane; t < len; t += kWarp) {
+                scol[t] = ci[b + t];
+                double v = lu[b + t];
+                if (shift != nullptr && t == dloc) v += shift[j];
+                sval[t] = v;
+            }
+            __syncwarp();
+            for (int t = 0; t < dloc; ++t) {
+                const int k = scol[t];
+                const int kd = diag[k];
+                const int ke = rp[k + 1];
+                const double l = sval[t] / __ldcg(lu + kd);
+                __syncwarp();
+                if (lane == 0) sval[t] = l;
+                for (int p = kd + 1 + lane; p < ke; p += kWarp) {
+                    const int c = ci[p];
+                    const int pos = find_sorted(scol, t + 1, len, c);
+                    if (pos >= 0) sval[pos] = fma(-__ldcg(lu + p), l, sval[pos]);
+                }
+                __syncwarp();
+            }
+            for (int t = lane; t < len; t += kWarp) lu[b + t] = sval[t];
+            if (lane == 0) {
+                const double u = sval[dloc];
+                if (!(fabs(u) > 0.0) || !isfinite(u)) {
+                    atomicAdd(status + kStatusBreakdowns, 1);
+                    atomicMin(status + kStatusFirstBreakdown, j);
+                }
+            }
+        } else {
+            const int* col = ci + b;
+            double* val = lu + b;
+            if (shift != nullptr && lane == 0) __stcg(val + dloc, __ldcg(val + dloc) + shift[j]);
+            __syncwarp();
+            for (int t = 0; t < dloc; ++t) {
+                const int k = col[t];
+                const int kd = diag[k];
+                const int ke = rp[k + 1];
+                const double l = __ldcg(val + t) / __ldcg(lu + kd);
+                __syncwarp();
+                if (lane == 0) __stcg(val + t, l);
+                for (int p = kd + 1 + lane; p < ke; p += kWarp) {
+                    const int pos = find_sorted(col, t + 1, len, ci[p]);
+                    if (pos >= 0) __stcg(val + pos, fma(-__ldcg(lu + p), l, __ldcg(val + pos)));
+                }
+                __syncwarp();
+            }
+            if (lane == 0) {
+                const double u = __ldcg(val + dloc);
+                if (!(fabs(u) > 0.0) || !isfinite(u)) {
+                    atomicAdd(status + kStatusBreakdowns, 1);
+                    atomicMin(status + kStatusFirstBreakdown, j);
+                }
+            }
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(done + j, stamp);
+        q = qn;
+    }
+}
+
+// Packed triangular factor for the substitution kernels.  Rows are taken in the
+// schedule order and grouped 32 to a task (one lane per row).  Task t owns slots
+// [off[t], off[t] + 32 * len[t]); entry k of lane l sits at off[t] + 32 k + l, so a
+// warp's loads of entry k are one coalesced 128/256-byte access.  Pad slots have
+// col = -1.  L entries are stored in ascending column order and U entries in descending
+// column order: the accumulation order of the reference's substitute_row_L / _U
+// (src/ilu_solver.cpp:687-696, 719-729).
+template <class T>
+struct PackedTri {
+    int ntask = 0;
+    const int* rows = nullptr;   // [32 * ntask], -1 for padding
+    const int* off = nullptr;    // [ntask]
+    const int* len = nullptr;    // [ntask]
+    const int* cols = nullptr;   // [slots]
+    const T* vals = nullptr;     // [slots]
+    const T* dvals = nullptr;    // [32 * ntask] diagonal (upper factor only)
+};
+
+// Gathers packed values from the CSR factor values: dst[s] = src[s] >= 0 ? lu[src[s]] : 0.
+template <class T>
+__global__ void pack_gather_kernel(long long count, const int* __restrict__ src, const double* __restrict__ lu,
+                                   T* __restrict__ dst) {
+    for (long long s = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; s < count;
+         s += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int p = src[s];
+        dst[s] = p >= 0 ? static_cast<T>(lu[p]) : T(0);
+    }
+}
+
+// Forward substitution with the unit lower factor: y = L^{-1} (scale * b).
+// With `scale` non-null, b is rescaled on the fly and the rescaled value is written back
+// to b (GMRES uses this to normalise the new Krylov vector in the same pass).
+// y must hold the sentinel everywhere on entry; each row publishes its value once.
+template <class T>
+__global__ void __launch_bounds__(kSolveWarps * kWarp)
+    sptrsv_lower_kernel(PackedTri<T> L, T* b, const double* scale, T* y, unsigned* counter, int* status,
+                        const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    const int lane = threadIdx.x & 31;
+    const T sc = scale ? static_cast<T>(*scale) : T(1);
+    int t = draw_ticket(counter, L.ntask, lane);
+    while (t < L.ntask) {
+        const int tn = draw_ticket(counter, L.ntask, lane);
+        const int row = L.rows[t * kWarp + lane];
+        const int off = L.off[t];
+        const int K = L.len[t];
+        T acc = T(0);
+        if (row >= 0) {
+            acc = b[row];
+            if (scale) {
+                acc = acc * sc;
+                b[row] = acc;
+            }
+        }
+        for (int k0 = 0; k0 < K; k0 += 8) {
+            int c[8];
+            T v[8], x[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int s = off + (k0 + u) * kWarp + lane;
+                c[u] = (k0 + u < K) ? L.cols[s] : -1;
+                v[u] = (k0 + u < K) ? L.vals[s] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) x[u] = c[u] >= 0 ? ld_relaxed(y + c[u]) : T(0);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (c[u] >= 0) {
+                    if (Sentinel<T>::is(x[u])) x[u] = wait_value(y + c[u], status);
+                    acc = fma(-v[u], x[u], acc);
+                }
+            }
+        }
+        if (row >= 0) st_relaxed(y + row, Sentinel<T>::canon(acc));
+        t = tn;
+    }
+}
+
+// Backward substitution with the upper factor: x = U^{-1} y.  Reads y[row] once, resets
+// it to the sentinel (so y is ready for the next forward sweep), waits on x values of
+// the rows it depends on.  x must hold the sentinel everywhere on entry.
+template <class T>
+__global__ void __launch_bounds__(kSolveWarps * kWarp)
+    sptrsv_upper_kernel(PackedTri<T> U, T* y, T* x, unsigned* counter, int* status, const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    const int lane = threadIdx.x & 31;
+    int t = draw_ticket(counter, U.ntask, lane);
+    while (t < U.ntask) {
+        const int tn = draw_ticket(counter, U.ntask, lane);
+        const int q = t * kWarp + lane;
+        const int row = U.rows[q];
+        const int off = U.off[t];
+        const int K = U.len[t];
+        T acc = T(0);
+        if (row >= 0) {
+            acc = y[row];
+            y[row] = Sentinel<T>::value();
+        }
+        for (int k0 = 0; k0 < K; k0 += 8) {
+            int c[8];
+            T v[8], xv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int s = off + (k0 + u) * kWarp + lane;
+                c[u] = (k0 + u < K) ? U.cols[s] : -1;
+                v[u] = (k0 + u < K) ? U.vals[s] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) xv[u] = c[u] >= 0 ? ld_relaxed(x + c[u]) : T(0);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (c[u] >= 0) {
+                    if (Sentinel<T>::is(xv[u])) xv[u] = wait_value(x + c[u], status);
+                    acc = fma(-v[u], xv[u], acc);
+                }
+            }
+        }
+        if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(acc / U.dvals[q]));
+        t = tn;
+    }
+}
+
+// Fills n entries with the sentinel.
+template <class T>
+__global__ void fill_sentinel_kernel(long long n, T* p) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        p[i] = Sentinel<T>::value();
+}
+
+}  // namespace gb300

@@ -1,0 +1,274 @@
+// lljbash::IluSolver on GB300: host analysis of the pattern (bit-exact with the
+// reference), sync-free ILU factorisation and sync-free triangular substitution on the
+// device.  Replaces src/ilu_solver.cpp (SetupMatrix :225-373, Factorize :616-671,
+// Substitute :736-831).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "analysis.hpp"
+#include "common.cuh"
+#include "device_util.hpp"
+#include "ilu_impl.hpp"
+#include "ilu_kernels.cuh"
+
+namespace gb300 {
+
+// Host construction of a packed factor from a schedule `order` (rows in level order).
+// lower: entries [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1])
+// descending plus the diagonal position.
+static void build_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag,
+                       const std::vector<int>& order, bool lower, TriPack& P, cudaStream_t s) {
+    const int ntask = ceil_div(n, kWarp);
+    std::vector<int> rows(static_cast<size_t>(ntask) * kWarp, -1);
+    std::vector<int> off(ntask), len(ntask);
+    std::vector<int> dsrc(lower ? 0 : static_cast<size_t>(ntask) * kWarp, -1);
+    long long slots = 0;
+    for (int t = 0; t < ntask; ++t) {
+        int k = 0;
+        for (int l = 0; l < kWarp; ++l) {
+            const int q = t * kWarp + l;
+            if (q >= n) break;
+            const int r = order[q];
+            rows[q] = r;
+            const int cnt = lower ? diag[r] - rp[r] : rp[r + 1] - diag[r] - 1;
+            k = std::max(k, cnt);
+            if (!lower) dsrc[q] = diag[r];
+        }
+        off[t] = static_cast<int>(slots);
+        len[t] = k;
+        slots += static_cast<long long>(k) * kWarp;
+        if (slots > INT_MAX) throw std::runtime_error("triangular factor too large for 32-bit slot offsets");
+    }
+    std::vector<int> cols(static_cast<size_t>(slots), -1), src(static_cast<size_t>(slots), -1);
+    for (int t = 0; t < ntask; ++t) {
+        for (int l = 0; l < kWarp; ++l) {
+            const int q = t * kWarp + l;
+            if (q >= n) break;
+            const int r = order[q];
+            int k = 0;
+            if (lower) {
+                for (int p = rp[r]; p < diag[r]; ++p, ++k) {
+                    const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
+                    cols[sidx] = ci[p];
+                    src[sidx] = p;
+                }
+            } else {
+                for (int p = rp[r + 1] - 1; p > diag[r]; --p, ++k) {
+                    const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
+                    cols[sidx] = ci[p];
+                    src[sidx] = p;
+                }
+            }
+        }
+    }
+    P.ntask = ntask;
+    P.slots = slots;
+    P.rows.upload(rows.data(), rows.size(), s);
+    P.off.upload(off.data(), off.size(), s);
+    P.len.upload(len.data(), len.size(), s);
+    P.cols.upload(cols.data(), cols.size(), s);
+    P.src.upload(src.data(), src.size(), s);
+    if (!lower) P.dsrc.upload(dsrc.data(), dsrc.size(), s);
+    P.v64.reserve(static_cast<size_t>(slots));
+    P.v32.reserve(static_cast<size_t>(slots));
+    if (!lower) {
+        P.d64.reserve(static_cast<size_t>(ntask) * kWarp);
+        P.d32.reserve(static_cast<size_t>(ntask) * kWarp);
+    }
+    // host vectors must outlive the asynchronous copies
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+}
+
+static void gather_pack(const TriPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
+    const int threads = 256;
+    auto grid_for = [&](long long count) {
+        long long g = ceil_div<long long>(count, threads);
+        return static_cast<int>(std::max<long long>(1, std::min<long long>(g, 8LL * sms)));
+    };
+    if (P.slots > 0) {
+        pack_gather_kernel<double><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v64.get());
+        pack_gather_kernel<float><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v32.get());
+    }
+    if (!lower) {
+        const long long nd = static_cast<long long>(P.ntask) * kWarp;
+        pack_gather_kernel<double><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d64.get());
+        pack_gather_kernel<float><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
+    }
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+template <class T>
+static void fill_sentinel(T* p, long long n, cudaStream_t s, int sms) {
+    if (n <= 0) return;
+    const int threads = 256;
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(n, threads), 8LL * sms)));
+    fill_sentinel_kernel<T><<<grid, threads, 0, s>>>(n, p);
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+}  // namespace gb300
+
+namespace lljbash {
+
+using namespace gb300;
+
+IluSolver::Impl::~Impl() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+template <class T>
+void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const {
+    const int grid = sizeof(T) == 8 ? grid_solve64 : grid_solve32;
+    sptrsv_lower_kernel<T><<<grid, kSolveWarps * kWarp, 0, s>>>(L.view<T>(), b, scale, y, counters.get() + 1,
+                                                                status.get(), gate, step);
+}
+
+template <class T>
+void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const {
+    const int grid = sizeof(T) == 8 ? grid_solve64 : grid_solve32;
+    sptrsv_upper_kernel<T><<<grid, kSolveWarps * kWarp, 0, s>>>(U.view<T>(), y, x, counters.get() + 2, status.get(),
+                                                                gate, step);
+}
+
+template void IluSolver::Impl::launch_lower<double>(cudaStream_t, double*, const double*, double*, const int*, int) const;
+template void IluSolver::Impl::launch_lower<float>(cudaStream_t, float*, const double*, float*, const int*, int) const;
+template void IluSolver::Impl::launch_upper<double>(cudaStream_t, double*, double*, const int*, int) const;
+template void IluSolver::Impl::launch_upper<float>(cudaStream_t, float*, float*, const int*, int) const;
+
+void IluSolver::Impl::check_status(cudaStream_t s) {
+    int h[kStatusWords];
+    GB_CUDA_CHECK(cudaMemcpyAsync(h, status.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (h[kStatusTimeout] != 0) {
+        const int zero = 0;
+        GB_CUDA_CHECK(cudaMemcpy(status.get() + kStatusTimeout, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        throw std::runtime_error("dependency wait timed out on the device");
+    }
+}
+
+IluSolver::Impl* IluSolver::impl_ensure() {
+    if (!impl_) impl_ = new Impl;
+    return impl_;
+}
+
+IluSolver::~IluSolver() {
+    delete impl_;
+    impl_ = nullptr;
+    DestroyCsrMatrix(&aMatrix_);
+}
+
+void IluSolver::SetupMatrix() {
+    const int n = aMatrix_.size;
+    if (n < 0 || aMatrix_.row_ptr == nullptr) throw std::runtime_error("matrix not set");
+    const int* rp = aMatrix_.row_ptr;
+    const int* ci = aMatrix_.col_idx;
+    Analysis an;
+    diagonal_pointers(n, rp, ci, an.diag);  // throws "missing diag"
+    const DagView gl{rp, ci, an.diag.data(), true};
+    const DagView gu{rp, ci, an.diag.data(), false};
+    elimination_tree(n, gl, an.etree_l);
+    elimination_tree(n, gu, an.etree_u);
+    an.nlev_l = level_sets(n, gl, an.depth_l, an.order_l, an.lptr_l);
+    an.nlev_u = level_sets(n, gu, an.depth_u, an.order_u, an.lptr_u);
+
+    Impl& im = *impl_ensure();
+    im.dev = current_device();
+    if (!im.stream) GB_CUDA_CHECK(cudaStreamCreateWithFlags(&im.stream, cudaStreamNonBlocking));
+    if (!im.ev0) {
+        GB_CUDA_CHECK(cudaEventCreate(&im.ev0));
+        GB_CUDA_CHECK(cudaEventCreate(&im.ev1));
+    }
+    cudaStream_t s = im.stream;
+    im.n = n;
+    im.nnz = rp[n];
+    im.an = std::move(an);
+    im.factorized = false;
+    im.rp.upload(rp, static_cast<size_t>(n) + 1, s);
+    im.ci.upload(ci, static_cast<size_t>(im.nnz), s);
+    im.diag.upload(im.an.diag.data(), static_cast<size_t>(n), s);
+    im.order_l.upload(im.an.order_l.data(), static_cast<size_t>(n), s);
+    im.lu.reserve(static_cast<size_t>(im.nnz));
+    im.done.reserve(static_cast<size_t>(std::max(n, 1)));
+    GB_CUDA_CHECK(cudaMemsetAsync(im.done.get(), 0, sizeof(int) * static_cast<size_t>(std::max(n, 1)), s));
+    im.stamp = 0;
+    im.counters.reserve(8);
+    GB_CUDA_CHECK(cudaMemsetAsync(im.counters.get(), 0, sizeof(unsigned) * 8, s));
+    im.status.reserve(kStatusWords);
+    GB_CUDA_CHECK(cudaMemsetAsync(im.status.get(), 0, sizeof(int) * kStatusWords, s));
+    build_pack(n, rp, ci, im.an.diag, im.an.order_l, true, im.L, s);
+    build_pack(n, rp, ci, im.an.diag, im.an.order_u, false, im.U, s);
+    const size_t nv = static_cast<size_t>(std::max(n, 1));
+    im.sb64.reserve(nv);
+    im.sy64.reserve(nv);
+    im.sx64.reserve(nv);
+    im.sy32.reserve(nv);
+    fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
+    fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
+    im.grid_fact = persistent_grid(ilu_factor_kernel, kFactWarps * kWarp, im.dev.sms);
+    im.grid_solve64 = persistent_grid(sptrsv_lower_kernel<double>, kSolveWarps * kWarp, im.dev.sms);
+    im.grid_solve32 = persistent_grid(sptrsv_lower_kernel<float>, kSolveWarps * kWarp, im.dev.sms);
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+}
+
+bool IluSolver::Factorize() {
+    if (!impl_ || impl_->n != aMatrix_.size) throw std::runtime_error("SetupMatrix() must be called first");
+    Impl& im = *impl_;
+    cudaStream_t s = im.stream;
+    const int n = im.n;
+    im.lu.upload(aMatrix_.value, static_cast<size_t>(im.nnz), s);
+    int init[kStatusWords] = {0, 0, INT_MAX, 0};
+    GB_CUDA_CHECK(cudaMemcpyAsync(im.status.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+    if (++im.stamp == INT_MAX) {
+        im.stamp = 1;
+        GB_CUDA_CHECK(cudaMemsetAsync(im.done.get(), 0, sizeof(int) * static_cast<size_t>(std::max(n, 1)), s));
+    }
+    GB_CUDA_CHECK(cudaEventRecord(im.ev0, s));
+    if (n > 0) {
+        ilu_factor_kernel<<<im.grid_fact, kFactWarps * kWarp, 0, s>>>(
+            n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(),
+            im.shift_active ? im.shift.get() : nullptr, im.done.get(), im.stamp, im.counters.get(), im.status.get());
+        GB_CUDA_CHECK(cudaGetLastError());
+        gather_pack(im.L, true, im.lu.get(), s, im.dev.sms);
+        gather_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+    }
+    GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
+    if (im.copy_back && im.nnz > 0)
+        GB_CUDA_CHECK(cudaMemcpyAsync(aMatrix_.value, im.lu.get(), sizeof(double) * static_cast<size_t>(im.nnz),
+                                      cudaMemcpyDeviceToHost, s));
+    int h[kStatusWords];
+    GB_CUDA_CHECK(cudaMemcpyAsync(h, im.status.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+    GB_CUDA_CHECK(cudaEventElapsedTime(&im.last_factor_ms, im.ev0, im.ev1));
+    if (h[kStatusTimeout] != 0) {
+        im.factorized = false;
+        throw std::runtime_error("dependency wait timed out on the device");
+    }
+    im.last_breakdowns = h[kStatusBreakdowns];
+    im.first_breakdown = h[kStatusBreakdowns] ? h[kStatusFirstBreakdown] : -1;
+    im.factorized = true;
+    return im.last_breakdowns == 0;
+}
+
+void IluSolver::Substitute(const double* b, double* x) {
+    if (!impl_ || !impl_->factorized) throw std::runtime_error("Factorize() must be called first");
+    Impl& im = *impl_;
+    cudaStream_t s = im.stream;
+    const int n = im.n;
+    if (n == 0) return;
+    GB_CUDA_CHECK(cudaMemcpyAsync(im.sb64.get(), b, sizeof(double) * static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
+    fill_sentinel(im.sx64.get(), n, s, im.dev.sms);
+    im.launch_lower<double>(s, im.sb64.get(), nullptr, im.sy64.get(), nullptr, 0);
+    im.launch_upper<double>(s, im.sy64.get(), im.sx64.get(), nullptr, 0);
+    GB_CUDA_CHECK(cudaGetLastError());
+    GB_CUDA_CHECK(cudaMemcpyAsync(x, im.sx64.get(), sizeof(double) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, s));
+    im.check_status(s);
+}
+
+}  // namespace lljbash

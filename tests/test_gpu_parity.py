@@ -1,0 +1,162 @@
+"""GPU parity: the CUDA path, called through the LLJBASH_* C ABI, against the
+reference's own outputs (golden fixtures) and the CPU oracle on larger seeded inputs.
+
+Tolerances (from the task's correctness bar):
+* factors: 1e-12 relative per entry;
+* substitution: 1e-12, relative per entry with a floor of 1e-3 * max|x| for entries
+  near zero (the reference's sums may be reassociated by -ffast-math);
+* GMRES: iteration count within +-1 of the reference, FP64 true residual <= tol.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+from par_ilu0_cpp_gb300 import api
+from par_ilu0_cpp_gb300 import generators as g
+
+pytestmark = pytest.mark.gpu
+
+
+def factorize(f):
+    ilu = api.IluSolver()
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    return ilu
+
+
+def true_residual(a, b, x):
+    return float(np.linalg.norm(b - g.spmv(a, x)))
+
+
+@pytest.fixture(scope="module")
+def port():
+    oracle.build_port()
+    return oracle.Port()
+
+
+def test_golden_factors(golden):
+    ilu = factorize(golden.f_csr())
+    assert rel_err(ilu.values(), golden.lu, floor=1e-300) <= 1e-12
+    an = ilu.analysis()
+    assert np.array_equal(an["diag"], golden.diag)
+    assert np.array_equal(an["etree_l"], golden.etree_l)
+    assert np.array_equal(an["depth_u"], golden.level_u)
+    info = ilu.info()
+    assert info.levels_lower == golden.nlev[0] and info.breakdowns == 0
+
+
+def test_golden_substitution(golden):
+    ilu = factorize(golden.f_csr())
+    x = ilu.substitute(golden.b)
+    assert rel_err(x, golden.x_subs) <= 1e-12
+    x2 = ilu.substitute(golden.b)  # sentinel state is restored between calls
+    assert np.array_equal(x, x2)
+
+
+def test_golden_gmres(golden):
+    res, ilu, gm = api.ilu_gmres(golden.a, golden.b, lof=golden.lof, tol=golden.tol, restart=golden.restart,
+                                 maxit=1000, relative=False)
+    assert res.ok == golden.gmres_ok
+    assert abs(res.iterations - golden.gmres_iters) <= 1, (res.iterations, golden.gmres_iters)
+    assert true_residual(golden.a, golden.b, res.x) <= golden.tol * 1.0001
+    assert res.report.converged == 1
+    assert np.max(np.abs(res.x - golden.gmres_x)) <= 1e-6 * max(1.0, np.max(np.abs(golden.gmres_x)))
+
+
+LARGE = [
+    ("laplace2d_256", lambda: g.laplace2d(256), 0, 30),
+    ("convdiff3d_32", lambda: g.convdiff3d(32), 0, 50),
+    ("lognormal27_16_k1", lambda: g.lognormal27(16, seed=1), 1, 30),
+    ("lognormal27_16_k2", lambda: g.lognormal27(16, seed=1), 2, 30),
+]
+
+
+@pytest.mark.parametrize("name,make,lof,m", LARGE, ids=[c[0] for c in LARGE])
+def test_large_against_oracle(port, name, make, lof, m):
+    a = make()
+    f, _ = port.iluk_symbolic(a, lof)
+    lu_ref, _ = port.factorize(f)
+    ilu = factorize(f)
+    assert rel_err(ilu.values(), lu_ref, floor=1e-300) <= 1e-12
+    x_true, b = g.random_rhs(a, seed=5)
+    xs = ilu.substitute(b)
+    assert rel_err(xs, port.substitute(f, lu_ref, b)) <= 1e-12
+    tol = 1e-8 * float(np.linalg.norm(b))
+    ok, its, x_ref, _ = port.gmres(a, f, lu_ref, b, tol, m, 1000)
+    gm = api.Gmres(tol, m, 1000)
+    gm.set_preconditioner(ilu)
+    res = gm.solve(a, b)
+    assert res.ok and ok
+    assert abs(res.iterations - its) <= 1, (res.iterations, its)
+    assert true_residual(a, b, res.x) <= tol * 1.0001
+
+
+def test_modes_are_deterministic():
+    a = g.convdiff3d(24)
+    x_true, b = g.random_rhs(a, seed=2)
+    tol = 1e-8 * float(np.linalg.norm(b))
+    f, _ = api.iluk_symbolic(a, 0)
+    ilu = factorize(f)
+    xs = []
+    for graph, profile in ((1, 0), (0, 0), (0, 1)):
+        gm = api.Gmres(tol, 50, 1000)
+        gm.set_preconditioner(ilu)
+        gm.set_option(api.GMRES_OPT_USE_GRAPH, graph)
+        gm.set_option(api.GMRES_OPT_PROFILE, profile)
+        res = gm.solve(a, b)
+        assert res.ok
+        xs.append((res.iterations, res.x))
+    assert xs[0][0] == xs[1][0] == xs[2][0]
+    assert np.array_equal(xs[0][1], xs[1][1]) and np.array_equal(xs[0][1], xs[2][1])
+
+
+@pytest.mark.parametrize("make", [lambda: g.laplace2d(128), lambda: g.convdiff3d(32),
+                                  lambda: g.lognormal27(16, seed=4)])
+def test_mixed_precision_reaches_fp64_tolerance(make):
+    a = make()
+    x_true, b = g.random_rhs(a, seed=9)
+    res, ilu, gm = api.ilu_gmres(a, b, tol=1e-8, restart=40, maxit=1000, mode=1)
+    r = true_residual(a, b, res.x)
+    assert res.ok and res.report.converged == 1
+    assert r <= 1e-8 * np.linalg.norm(b) * 1.0001
+    assert res.report.residual <= 1e-8 * np.linalg.norm(b) * 1.0001
+    fwd = np.max(np.abs(res.x - x_true)) / np.max(np.abs(x_true))
+    assert fwd < 1e-4  # forward error stated for the record; bounded by conditioning
+
+
+def test_unpreconditioned_gmres():
+    a = g.laplace2d(16)
+    x_true, b = g.random_rhs(a, seed=1)
+    tol = 1e-8 * float(np.linalg.norm(b))
+    gm = api.Gmres(tol, 60, 1000)
+    res = gm.solve(a, b)
+    assert res.ok
+    assert true_residual(a, b, res.x) <= tol * 1.0001
+
+
+def test_missing_diagonal_setup_code():
+    ilu = api.IluSolver()
+    ilu.set_matrix(g.Csr(2, [0, 1, 2], [1, 1], [1.0, 2.0]))
+    assert ilu.setup() == -2
+
+
+def test_zero_pivot_reported():
+    a = g.Csr(2, [0, 2, 4], [0, 1, 0, 1], [0.0, 1.0, 1.0, 1.0])
+    ilu = api.IluSolver()
+    ilu.set_matrix(a)
+    assert ilu.setup() == 0
+    assert ilu.factorize() == 0  # the reference returns success on a zero pivot too
+    info = ilu.info()
+    assert info.breakdowns >= 1 and info.first_breakdown == 0
+
+
+def test_nan_input_fails_cleanly():
+    a = g.laplace2d(8)
+    vals = a.values.copy()
+    vals[5] = np.nan
+    an = g.Csr(a.n, a.row_ptr, a.col_idx, vals)
+    b = np.ones(a.n)
+    res, ilu, gm = api.ilu_gmres(an, b, tol=1e-8, restart=10, maxit=50)
+    assert not res.ok
