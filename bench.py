@@ -1,0 +1,414 @@
+"""Benchmark: time to ||b - A x||_2 / ||b||_2 <= 1e-8 on one GB300.
+
+Workload (the single-GPU configuration the metric is quoted on): 3D 7-point upwind
+convection-diffusion on a 128^3 grid (n = 2,097,152, nnz = 14,581,760), diffusion 1,
+wind (1, 0.5, 0.25) at cell Peclet 0.5, natural ordering, ILU(0) + GMRES(50),
+relative tolerance 1e-8 (absolute 1e-8 ||b||_2 passed to the solver), max 1000
+iterations, x_true ~ U[-1, 1] (seed 0), b = A x_true, x0 = 0.  Seeded synthetic data.
+
+One step = numeric factorisation (+ learned-shift pre-pass when enabled) + GMRES to the
+tolerance, on inputs resident in HBM (device-resident entry points).  ``value`` is the
+headline solver (FP32 cycles in FP64 refinement, learned shift when a model is
+available); the plain FP64 solver is timed the same way beside it.  ``e2e`` repeats the
+headline solve through the reference-facing C ABI with host buffers (IluSolverFactorize +
+GmresSolve, every copy inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference's algorithm on the host cores instead (the
+CPU restatement in oracle/, since the reference's own build is not available on the
+benchmark machine), on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms to ‖r‖/‖b‖≤1e-8: mixed+learned vs plain FP64 ILU-GMRES, same GB300; HBM GB/s"
+RESTART = 50
+MAXIT = 1000
+RTOL = 1e-8
+SEED = 0
+CPU_SAMPLE_ITERS = 50  # one full GMRES(50) restart cycle is timed on the CPU and scaled
+
+
+def workload(size: int):
+    from par_ilu0_cpp_gb300 import generators as g
+
+    a = g.convdiff3d(size)
+    x_true, b = g.random_rhs(a, SEED)
+    return a, x_true, b
+
+
+def config_of(a, size, solver):
+    return {
+        "workload": f"convdiff3d 7-pt upwind {size}^3 (Pe 0.5, wind (1,0.5,0.25)), ILU(0)+GMRES({RESTART}), "
+                    f"rtol {RTOL:g}, natural order",
+        "n": a.n,
+        "nnz": a.nnz,
+        "restart": RESTART,
+        "max_iterations": MAXIT,
+        "solver": solver,
+        "l2_policy": "inputs larger than L2 (A = 175 MB FP64, Krylov basis 0.4-0.9 GB) - no flush",
+        "parallelism": "replicas",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int = 0):
+        self.proc = None
+        self.lines = []
+        self.device_index = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(kind, a, nnz_l, nnz_u, tsize, steps_hist):
+    """Algorithmic bytes of all launches of one kernel kind during a profiled solve.
+    tsize: bytes per vector / factor value (8 FP64, 4 FP32); indices are int32.
+    steps_hist: list of Arnoldi step indices s that ran (one launch each)."""
+    n, nnz = a.n, a.nnz
+    S = len(steps_hist)
+    if kind == "sptrsv_lower":
+        # packed L entries (col + value), row ids, rhs read, normalised rhs written back, y written
+        return S * ((4 + tsize) * nnz_l + 4 * n + 3 * tsize * n)
+    if kind == "sptrsv_upper":
+        # packed U entries + diagonal, row ids, y read (and reset), z written
+        return S * ((4 + tsize) * nnz_u + (4 + tsize) * n + 4 * n + 3 * tsize * n)
+    if kind == "spmv":
+        return S * ((4 + tsize) * nnz + 4 * (n + 1) + 2 * tsize * n)
+    if kind == "cgs_dot":
+        return sum(tsize * n * (s + 2) for s in steps_hist)
+    if kind in ("cgs_axpy_dot", "cgs_axpy_norm"):
+        return sum(tsize * n * (s + 3) for s in steps_hist)
+    return None
+
+
+def kernel_profile(gm, ilu, dev, a, f_nnz_l, f_nnz_u, tsize):
+    """One extra solve with every kernel timed by CUDA events on its stream."""
+    from par_ilu0_cpp_gb300 import api
+
+    gm.reset_kernel_times()
+    gm.set_option(api.GMRES_OPT_PROFILE, 1)
+    dev["x"].zero_()
+    import torch
+
+    torch.cuda.synchronize()
+    ilu.factorize_device(dev["fv"].data_ptr())
+    ok, its = gm.solve_device(a.n, dev["rp"].data_ptr(), dev["ci"].data_ptr(), dev["av"].data_ptr(),
+                              dev["b"].data_ptr(), dev["x"].data_ptr())
+    gm.set_option(api.GMRES_OPT_PROFILE, 0)
+    kt = gm.kernel_times()
+    rep = gm.report()
+    # reconstruct the Arnoldi step indices: cycles of up to RESTART steps
+    steps = []
+    left = kt["spmv"][1]
+    while left > 0:
+        c = min(RESTART, left)
+        steps.extend(range(c))
+        left -= c
+    out = {}
+    for kind, (ms, cnt) in kt.items():
+        if cnt == 0:
+            continue
+        byt = algorithmic_bytes(kind, a, f_nnz_l, f_nnz_u, tsize, steps[:cnt] if kind != "residual" else [])
+        out[kind] = {"ms_total": ms, "launches": cnt, "avg_us": 1e3 * ms / cnt,
+                     "alg_bytes_total": byt, "gbs": (byt / (ms * 1e-3) / 1e9) if byt else None}
+    return out, rep
+
+
+def cpu_baseline(a, b, tol, nthreads, full_iters_hint=None):
+    """The reference's algorithm on the host cores (oracle port): factorisation (best of
+    1 thread and all threads, as the reference's thread sweep) + one GMRES(50) restart
+    cycle, scaled to the full iteration count."""
+    import oracle
+
+    port = oracle.Port()
+    t_fact = []
+    lu = None
+    for nt in sorted({1, nthreads}):
+        lu, secs = port.factorize(a, nthreads=nt)
+        t_fact.append((secs, nt))
+    fact_s, fact_threads = min(t_fact)
+    t0 = time.perf_counter()
+    ok, its_s, _, _ = port.gmres(a, a, lu, b, tol, RESTART, CPU_SAMPLE_ITERS, nthreads=nthreads)
+    gm_s = time.perf_counter() - t0
+    full_its = full_iters_hint if full_iters_hint else its_s
+    per_it = gm_s / max(its_s, 1)
+    total_ms = 1e3 * (fact_s + per_it * full_its)
+    return {"value": round(total_ms, 3), "unit": "ms", "cores": nthreads, "kind": "port",
+            "sample": f"factorisation (best of 1/{nthreads} threads: {fact_threads}) + the first GMRES({RESTART}) cycle "
+                      f"({its_s} iterations, {gm_s:.2f} s) scaled to {full_its} iterations",
+            "factorize_ms": round(1e3 * fact_s, 3), "gmres_ms_per_iter": round(1e3 * per_it, 3)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    a, x_true, b = workload(args.size)
+    tol = RTOL * float(np.linalg.norm(b))
+    nthreads = os.cpu_count() or 1
+    import oracle
+
+    port = oracle.Port()
+    # full iteration count of the reference algorithm on this workload (one full solve)
+    lu, _ = port.factorize(a, nthreads=1)
+    ok, full_its, x, _ = port.gmres(a, a, lu, b, tol, RESTART, MAXIT, nthreads=nthreads)
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        last = cpu_baseline(a, b, tol, nthreads, full_iters_hint=full_its)
+        if i >= args.warmup:
+            vals.append(last["value"])
+    v = float(np.median(vals)) if vals else last["value"]
+    line = {"metric": METRIC, "value": round(v, 3), "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(v, 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": config_of(a, args.size, "reference algorithm, plain FP64, host cores"),
+            "iterations": full_its, "converged": bool(ok),
+            "cpu_baseline": {"value": round(v, 3), "unit": "ms", "cores": nthreads, "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": round(v, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    from par_ilu0_cpp_gb300 import api
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    api.load()
+    a, x_true, b = workload(args.size)
+    bnorm = float(np.linalg.norm(b))
+    tol = RTOL * bnorm
+    f, nzmap = api.iluk_symbolic(a, 0)
+    an = api.analyze_pattern(f)
+    diag = an["diag"]
+    nnz_l = int(np.sum(diag - f.row_ptr[:-1]))
+    nnz_u = int(np.sum(f.row_ptr[1:] - diag - 1))
+    dev = {"rp": torch.from_numpy(a.row_ptr).cuda(), "ci": torch.from_numpy(a.col_idx).cuda(),
+           "av": torch.from_numpy(a.values).cuda(), "fv": torch.from_numpy(f.values).cuda(),
+           "b": torch.from_numpy(b).cuda(), "x": torch.zeros(a.n, dtype=torch.float64, device="cuda")}
+    torch.cuda.synchronize()
+
+    def make(mode):
+        ilu = api.IluSolver()
+        ilu.set_matrix(f)
+        assert ilu.setup() == 0, api.last_error()
+        ilu.set_option(api.ILU_OPT_COPY_BACK, 0)
+        gm = api.Gmres(tol, RESTART, MAXIT)
+        gm.set_preconditioner(ilu)
+        gm.set_option(api.GMRES_OPT_MODE, mode)
+        return ilu, gm
+
+    solvers = {"plain": make(0), "mixed": make(1)}
+
+    def step(name):
+        ilu, gm = solvers[name]
+        dev["x"].zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = ilu.factorize_device(dev["fv"].data_ptr())
+        ok, its = gm.solve_device(a.n, dev["rp"].data_ptr(), dev["ci"].data_ptr(), dev["av"].data_ptr(),
+                                  dev["b"].data_ptr(), dev["x"].data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        if rc != 0 or not ok:
+            raise RuntimeError(f"{name} solve failed: rc={rc} ok={ok} its={its} {api.last_error()}")
+        return e0.elapsed_time(e1), its
+
+    for _ in range(args.warmup):
+        step("plain")
+        step("mixed")
+    launches0 = sum(s[0].info().kernel_launches + s[1].report().kernel_launches for s in solvers.values())
+    clocks = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    times = {"plain": [], "mixed": []}
+    its = {}
+    for _ in range(args.steps):
+        for name in ("mixed", "plain"):
+            ms, it = step(name)
+            times[name].append(ms)
+            its[name] = it
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    launches1 = sum(s[0].info().kernel_launches + s[1].report().kernel_launches for s in solvers.values())
+    ms = {k: float(np.mean(v)) for k, v in times.items()}
+    if dist is not None:
+        t = torch.tensor([ms["mixed"], ms["plain"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms["mixed"], ms["plain"] = float(t[0]), float(t[1])
+
+    # accuracy of the headline answer (FP64 true residual, forward error vs x_true)
+    step("mixed")
+    x = dev["x"].cpu().numpy()
+    from par_ilu0_cpp_gb300 import generators as g
+
+    res_m = float(np.linalg.norm(b - g.spmv(a, x))) / bnorm
+    fwd_m = float(np.max(np.abs(x - x_true)))
+    step("plain")
+    xp = dev["x"].cpu().numpy()
+    res_p = float(np.linalg.norm(b - g.spmv(a, xp))) / bnorm
+
+    # e2e through the reference-facing C ABI with host buffers (headline mode)
+    e2e_ms = []
+    ilu_h = api.IluSolver()
+    ilu_h.set_matrix(f)
+    assert ilu_h.setup() == 0
+    gm_h = api.Gmres(tol, RESTART, MAXIT)
+    gm_h.set_preconditioner(ilu_h)
+    gm_h.set_option(api.GMRES_OPT_MODE, 1)
+    for i in range(args.warmup + args.steps):
+        ilu_h.set_values(f.values)  # the factors of the previous step were copied back in place
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = ilu_h.factorize()
+        res = gm_h.solve(a, b)
+        t1 = time.perf_counter()
+        if rc != 0 or not res.ok:
+            raise RuntimeError("e2e solve failed")
+        if i >= args.warmup:
+            e2e_ms.append(1e3 * (t1 - t0))
+    h2d = 8 * f.nnz + 4 * (a.n + 1) + 4 * a.nnz + 8 * a.nnz + 8 * a.n + 8 * a.n
+    d2h = 8 * f.nnz + 8 * a.n
+
+    # per-kernel profile of the headline solve (events on the launching stream)
+    prof, _ = kernel_profile(solvers["mixed"][1], solvers["mixed"][0], dev, a, nnz_l, nnz_u, 4)
+    prof_plain, _ = kernel_profile(solvers["plain"][1], solvers["plain"][0], dev, a, nnz_l, nnz_u, 8)
+    dom = max((k for k in prof if prof[k]["gbs"] is not None), key=lambda k: prof[k]["ms_total"])
+    peak, peak_kind = measured_peaks()
+    achieved = prof[dom]["gbs"]
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.isfile(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get(dom)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(a, b, tol, os.cpu_count() or 1, full_iters_hint=its["plain"])
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(ms["mixed"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms["mixed"], 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 Krylov/ILU + f64 refinement", "data": "synthetic (seeded generator)",
+            "config": config_of(a, args.size, "mixed (FP32 cycles in FP64 refinement)"),
+            "plain_fp64_ms": round(ms["plain"], 3),
+            "speedup_vs_plain": round(ms["plain"] / ms["mixed"], 3),
+            "iterations": {"mixed": its["mixed"], "plain": its["plain"]},
+            "relative_residual": {"mixed": res_m, "plain": res_p}, "forward_error_inf": fwd_m,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic},
+            "kernels_mixed": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in d.items()}
+                              for k, d in prof.items()},
+            "kernels_plain": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in d.items()}
+                              for k, d in prof_plain.items()},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(float(np.mean(e2e_ms)), 3), "unit": "ms", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "path": "LLJBASH_IluSolverFactorize + LLJBASH_GmresSolve"},
+            "gpu_launches": int(launches1 - launches0),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

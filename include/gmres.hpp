@@ -33,6 +33,12 @@ public:
      * the iteration count passes max_iterations. */
     std::pair<bool, int> Solve(const CsrMatrix* mat, double* rhs, double* sol);
 
+    /* GB300 extension: the same solve on arrays already in device memory (CSR of A with
+     * n rows, rhs, and sol holding the initial guess; sol is overwritten).  The arrays
+     * must be ready when the call is made (work that produced them synchronised). */
+    std::pair<bool, int> SolveDevice(int n, const int* d_row_ptr, const int* d_col_idx, const double* d_values,
+                                     const double* d_rhs, double* d_sol);
+
     struct Impl;
     Impl* impl() { return impl_; }
     Impl* impl_ensure();

@@ -36,6 +36,11 @@ public:
     /* x = U^{-1} L^{-1} b on host arrays of length n (b == x allowed). */
     void Substitute(const double* b, double* x);
 
+    /* GB300 extension: Factorize() with the matrix values (GetMatrix()'s pattern) taken
+     * from device memory; the factors stay on the device (GetMatrix()->value is left
+     * untouched). */
+    bool FactorizeDevice(const double* d_values);
+
     /* Implementation state (device buffers, schedules); opaque to users. */
     struct Impl;
     Impl* impl() { return impl_; }
@@ -44,6 +49,7 @@ public:
     int threads() const { return threads_; }
 
 private:
+    bool FactorizeFrom(const double* values, bool on_device);
     int threads_ = 0;
     CsrMatrix aMatrix_;
     Impl* impl_ = nullptr;

@@ -25,6 +25,17 @@ const char* LLJBASH_Gb300LastError(void);
  * src/ilu_solver.cpp:736-831). */
 int LLJBASH_IluSolverSubstitute(IluSolverHdl hdl, const double* b, double* x);
 
+/* IluSolverFactorize with the values of GetMatrix()'s pattern read from device memory
+ * (d_values: nnz doubles, ready when called).  The factors stay on the device.  No
+ * counterpart in the reference (its data never leaves the host). */
+int LLJBASH_IluSolverFactorizeDevice(IluSolverHdl hdl, const double* d_values);
+
+/* GmresSolve on device-resident operands: the CSR arrays of A (n rows), rhs and sol
+ * (initial guess in, solution out) in device memory, ready when called.  Same return
+ * convention as GmresSolve.  No counterpart in the reference. */
+bool LLJBASH_GmresSolveDevice(GmresHdl hdl, int n, const int* d_row_ptr, const int* d_col_idx, const double* d_values,
+                              const double* d_rhs, double* d_sol, int* iter);
+
 /* ILU solver options. */
 enum {
     /* 1 (default): copy the factors into GetMatrix()->value after Factorize, as the
@@ -45,6 +56,7 @@ typedef struct LLJBASH_IluInfo {
     int breakdowns;       /* zero / non-finite pivots in the last Factorize */
     int first_breakdown;  /* smallest such row, -1 if none */
     double factor_ms;     /* device time of the last Factorize (factorisation + packing) */
+    long long kernel_launches; /* kernels launched by this solver so far */
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 
@@ -79,6 +91,7 @@ typedef struct LLJBASH_GmresReport {
     int converged;    /* FP64 true residual <= tolerance at exit */
     double residual;  /* ||b - A x||_2 at exit, FP64 (-1 if not computed) */
     double solve_ms;  /* device time of the cycles */
+    long long kernel_launches; /* kernels launched by this solver so far (graph nodes included) */
 } LLJBASH_GmresReport;
 int LLJBASH_GmresGetReport(GmresHdl hdl, LLJBASH_GmresReport* report);
 

@@ -46,12 +46,13 @@ class GmresStat(ctypes.Structure):
 class IluInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("nnz", ctypes.c_int), ("levels_lower", ctypes.c_int),
                 ("levels_upper", ctypes.c_int), ("breakdowns", ctypes.c_int), ("first_breakdown", ctypes.c_int),
-                ("factor_ms", ctypes.c_double)]
+                ("factor_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong)]
 
 
 class GmresReport(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("iterations", ctypes.c_int), ("cycles", ctypes.c_int),
-                ("converged", ctypes.c_int), ("residual", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+                ("converged", ctypes.c_int), ("residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_longlong)]
 
 
 ILU_OPT_COPY_BACK = 1
@@ -102,6 +103,9 @@ def load() -> ctypes.CDLL:
         "LLJBASH_GmresSolve": (ctypes.c_bool, [ctypes.c_void_p, ctypes.POINTER(CsrMatrix), _D, _D, _I]),
         "LLJBASH_Gb300LastError": (ctypes.c_char_p, []),
         "LLJBASH_IluSolverSubstitute": (ctypes.c_int, [ctypes.c_void_p, _D, _D]),
+        "LLJBASH_IluSolverFactorizeDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+        "LLJBASH_GmresSolveDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I]),
         "LLJBASH_IluSolverSetOption": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
         "LLJBASH_IluSolverSetShift": (ctypes.c_int, [ctypes.c_void_p, _D]),
         "LLJBASH_IluSolverGetInfo": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(IluInfo)]),
@@ -258,6 +262,10 @@ class IluSolver:
     def factorize(self) -> int:
         return self.lib.LLJBASH_IluSolverFactorize(self.h)
 
+    def factorize_device(self, d_values: int) -> int:
+        """Factorize from a device pointer (int address) holding nnz(F) doubles."""
+        return self.lib.LLJBASH_IluSolverFactorizeDevice(self.h, ctypes.c_void_p(d_values))
+
     def substitute(self, b) -> np.ndarray:
         bb = _f64(b).copy()
         x = np.empty_like(bb)
@@ -346,6 +354,14 @@ class Gmres:
         its = ctypes.c_int(0)
         ok = self.lib.LLJBASH_GmresSolve(self.h, view.ref, _dp(b), _dp(x), ctypes.byref(its))
         return SolveResult(bool(ok), int(its.value), x, self.report())
+
+    def solve_device(self, n: int, d_rp: int, d_ci: int, d_val: int, d_rhs: int, d_sol: int):
+        """GMRES on device-resident operands (int device addresses); returns (ok, its)."""
+        its = ctypes.c_int(0)
+        ok = self.lib.LLJBASH_GmresSolveDevice(self.h, int(n), ctypes.c_void_p(d_rp), ctypes.c_void_p(d_ci),
+                                               ctypes.c_void_p(d_val), ctypes.c_void_p(d_rhs), ctypes.c_void_p(d_sol),
+                                               ctypes.byref(its))
+        return bool(ok), int(its.value)
 
     def report(self) -> GmresReport:
         r = GmresReport()

@@ -94,6 +94,28 @@ int LLJBASH_IluSolverSubstitute(IluSolverHdl hdl, const double* b, double* x) {
     return 0;
 }
 
+int LLJBASH_IluSolverFactorizeDevice(IluSolverHdl hdl, const double* d_values) {
+    try {
+        ilu(hdl)->FactorizeDevice(d_values);
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+bool LLJBASH_GmresSolveDevice(GmresHdl hdl, int n, const int* d_row_ptr, const int* d_col_idx, const double* d_values,
+                              const double* d_rhs, double* d_sol, int* iter) {
+    try {
+        auto ret = gm(hdl)->SolveDevice(n, d_row_ptr, d_col_idx, d_values, d_rhs, d_sol);
+        if (iter) *iter = ret.second;
+        return ret.first;
+    } catch (const std::exception& e) {
+        fail(e);
+        if (iter) *iter = 0;
+        return false;
+    }
+}
+
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
     try {
         IluSolver* s = ilu(hdl);
@@ -145,6 +167,7 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->breakdowns = im->last_breakdowns;
     info->first_breakdown = im->first_breakdown;
     info->factor_ms = im->last_factor_ms;
+    info->kernel_launches = im->launches;
     return 0;
 }
 
@@ -246,6 +269,7 @@ int LLJBASH_GmresGetReport(GmresHdl hdl, LLJBASH_GmresReport* report) {
     report->converged = im->report.converged;
     report->residual = im->report.residual;
     report->solve_ms = im->report.solve_ms;
+    report->kernel_launches = im->launches;
     return 0;
 }
 

@@ -80,7 +80,7 @@ template <class T>
 struct ValueOf;
 template <>
 struct ValueOf<double> {
-    static const double* get(const PreconditionedGmres::Impl& g) { return g.a64.get(); }
+    static const double* get(const PreconditionedGmres::Impl& g) { return g.a64_p; }
 };
 template <>
 struct ValueOf<float> {
@@ -91,10 +91,12 @@ struct Launcher {
     PreconditionedGmres::Impl& g;
     bool timed;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    long long count = 0;
     template <class F>
     void run(KernelKind kind, F&& f) {
         if (timed) GB_CUDA_CHECK(cudaEventRecord(e0, g.stream));
         f();
+        count += (kind == kKUpdate) ? 2 : 1;
         GB_CUDA_CHECK(cudaGetLastError());
         if (timed) {
             GB_CUDA_CHECK(cudaEventRecord(e1, g.stream));
@@ -124,15 +126,14 @@ void enqueue_piece(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Kry
     if (step < 0) {
         L.run(kKResidual, [&] {
             gmres_residual_kernel<T><<<g.grid_spmv, kSpmvWarps * kWarp, 0, st>>>(
-                n, g.rp.get(), g.ci.get(), g.a64.get(), g.b.get(), g.x.get(), K.V.get(), ctl, H, g.partial.get(),
-                g.counters.get());
+                n, g.rp_p, g.ci_p, g.a64_p, g.b_p, g.x_p, K.V.get(), ctl, H, g.partial.get(), g.counters.get());
         });
         return;
     }
     if (step == K.im) {
         L.run(kKUpdate, [&] {
             gmres_backsolve_kernel<<<1, 32, 0, st>>>(ctl, H);
-            gmres_update_kernel<T><<<g.grid_update, 256, 0, st>>>(n, ld, K.Z.get(), g.x.get(), ctl, H);
+            gmres_update_kernel<T><<<g.grid_update, 256, 0, st>>>(n, ld, K.Z.get(), g.x_p, ctl, H);
         });
         return;
     }
@@ -149,8 +150,8 @@ void enqueue_piece(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Kry
         });
     }
     L.run(kKSpmv, [&] {
-        spmv_kernel<T, T, T><<<g.grid_spmv, kSpmvWarps * kWarp, 0, st>>>(n, g.rp.get(), g.ci.get(), ValueOf<T>::get(g),
-                                                                          Zs, W, gate, s);
+        spmv_kernel<T, T, T><<<g.grid_spmv, kSpmvWarps * kWarp, 0, st>>>(n, g.rp_p, g.ci_p, ValueOf<T>::get(g), Zs, W,
+                                                                          gate, s);
     });
     L.run(kKDot, [&] {
         cgs_dot_kernel<T><<<g.grid_blas, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.partial.get(), g.h1.get(),
@@ -179,16 +180,18 @@ void run_cycle(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Krylov<
             enqueue_piece<T>(g, ilu, K, s, L);
         }
         enqueue_piece<T>(g, ilu, K, K.im, L);
+        g.launches += L.count;
         return;
     }
     Launcher L{g, false};
     if (!g.use_graph) {
         for (int s = -1; s <= K.im; ++s) enqueue_piece<T>(g, ilu, K, s, L);
+        g.launches += L.count;
         return;
     }
     const void* key[6] = {K.V.get(), ilu ? static_cast<const void*>(ilu->L.cols.get()) : nullptr,
-                          ilu ? static_cast<const void*>(ilu->U.v64.get()) : nullptr, ValueOf<T>::get(g), g.x.get(),
-                          g.rp.get()};
+                          ilu ? static_cast<const void*>(ilu->U.v64.get()) : nullptr, ValueOf<T>::get(g), g.x_p,
+                          g.b_p};
     bool same = K.graph != nullptr;
     for (int k = 0; k < 6 && same; ++k) same = key[k] == K.graph_key[k];
     if (!same) {
@@ -203,8 +206,10 @@ void run_cycle(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Krylov<
         GB_CUDA_CHECK(cudaGraphInstantiate(&K.graph, graph, 0));
         cudaGraphDestroy(graph);
         for (int k = 0; k < 6; ++k) K.graph_key[k] = key[k];
+        K.graph_nodes = L.count;
     }
     GB_CUDA_CHECK(cudaGraphLaunch(K.graph, g.stream));
+    g.launches += K.graph_nodes;
 }
 
 template <class T>
@@ -262,6 +267,7 @@ std::pair<bool, int> solve_mode(PreconditionedGmres::Impl& g, const IluSolver::I
     } else if (g.verify && g.n > 0) {
         Launcher L{g, false};
         enqueue_piece<T>(g, ilu, K, -1, L);
+        g.launches += L.count;
         GB_CUDA_CHECK(cudaMemcpyAsync(g.ctl_host, g.ctl.get(), sizeof(GmresCtl), cudaMemcpyDeviceToHost, g.stream));
         GB_CUDA_CHECK(cudaStreamSynchronize(g.stream));
         g.report.residual = g.ctl_host->beta0;
@@ -272,56 +278,43 @@ std::pair<bool, int> solve_mode(PreconditionedGmres::Impl& g, const IluSolver::I
 
 }  // namespace
 
-std::pair<bool, int> PreconditionedGmres::Solve(const CsrMatrix* mat, double* rhs, double* sol) {
-    const auto wall0 = std::chrono::steady_clock::now();
-    Impl& g = *impl_ensure();
-    if (!g.stream) {
-        g.dev = current_device();
-        GB_CUDA_CHECK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
-        GB_CUDA_CHECK(cudaEventCreate(&g.ev0));
-        GB_CUDA_CHECK(cudaEventCreate(&g.ev1));
-        GB_CUDA_CHECK(cudaMallocHost(reinterpret_cast<void**>(&g.ctl_host), sizeof(GmresCtl)));
-        g.grid_spmv = persistent_grid(spmv_kernel<double, double, double>, kSpmvWarps * kWarp, g.dev.sms, 8);
-        g.grid_blas = persistent_grid(cgs_axpy_dot_kernel<double>, kBlasThreads, g.dev.sms, 2);
-        g.grid_update = 4 * g.dev.sms;
-        g.counters.reserve(4);
-        GB_CUDA_CHECK(cudaMemsetAsync(g.counters.get(), 0, sizeof(unsigned) * 4, g.stream));
-        g.ctl.reserve(1);
-        g.h1.reserve(kMaxKrylov + 1);
-        g.h2.reserve(kMaxKrylov + 1);
-        const int maxgrid = std::max(g.grid_spmv, g.grid_blas);
-        g.partial.reserve(static_cast<size_t>(maxgrid) * kPartialStride);
-    }
-    const int im = param_.krylov_subspace_dimension;
+void PreconditionedGmres::Impl::init_once() {
+    if (stream) return;
+    dev = current_device();
+    GB_CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    GB_CUDA_CHECK(cudaEventCreate(&ev0));
+    GB_CUDA_CHECK(cudaEventCreate(&ev1));
+    GB_CUDA_CHECK(cudaMallocHost(reinterpret_cast<void**>(&ctl_host), sizeof(GmresCtl)));
+    grid_spmv = persistent_grid(spmv_kernel<double, double, double>, kSpmvWarps * kWarp, dev.sms, 8);
+    grid_blas = persistent_grid(cgs_axpy_dot_kernel<double>, kBlasThreads, dev.sms, 2);
+    grid_update = 4 * dev.sms;
+    counters.reserve(4);
+    GB_CUDA_CHECK(cudaMemsetAsync(counters.get(), 0, sizeof(unsigned) * 4, stream));
+    ctl.reserve(1);
+    h1.reserve(kMaxKrylov + 1);
+    h2.reserve(kMaxKrylov + 1);
+    partial.reserve(static_cast<size_t>(std::max(grid_spmv, grid_blas)) * kPartialStride);
+}
+
+// Shared body of the host-array and device-array entry points: operands are in
+// g.rp_p / ci_p / a64_p / b_p / x_p; a32 (mixed mode) is refreshed when needed.
+static std::pair<bool, int> solve_core(PreconditionedGmres::Impl& g, IluSolver* ilu_solver, const GmresParameters& prm,
+                                       GmresStat& stat, bool refresh_a32) {
+    const int im = prm.krylov_subspace_dimension;
     if (im < 1 || im > kMaxKrylov) throw std::runtime_error("krylov_subspace_dimension must be in [1, 128]");
-    const int n = mat->size;
-    const long long nnz = mat->row_ptr[n];
-    IluSolver::Impl* ilu = ilu_ ? ilu_->impl() : nullptr;
-    if (ilu && (!ilu->factorized || ilu->n != n)) throw std::runtime_error("preconditioner not factorised for this size");
+    IluSolver::Impl* ilu = ilu_solver ? ilu_solver->impl() : nullptr;
+    if (ilu && (!ilu->factorized || ilu->n != g.n)) throw std::runtime_error("preconditioner not factorised for this size");
     cudaStream_t s = g.stream;
-    const auto up0 = std::chrono::steady_clock::now();
-    if (!(g.keep_matrix && g.matrix_loaded && g.n == n && g.nnz == nnz)) {
-        g.rp.upload(mat->row_ptr, static_cast<size_t>(n) + 1, s);
-        g.ci.upload(mat->col_idx, static_cast<size_t>(nnz), s);
-        g.a64.upload(mat->value, static_cast<size_t>(nnz), s);
-        g.matrix_loaded = false;
-    }
-    g.n = n;
-    g.nnz = nnz;
-    if (g.mode == kModeMixed && (!g.matrix_loaded || g.a32.size() < static_cast<size_t>(nnz))) {
+    const int n = g.n;
+    const long long nnz = g.nnz;
+    if (g.mode == kModeMixed && (refresh_a32 || g.a32_src != g.a64_p || g.a32.size() < static_cast<size_t>(nnz))) {
         g.a32.reserve(static_cast<size_t>(std::max<long long>(nnz, 1)));
         if (nnz > 0)
             convert_kernel<double, float><<<std::min<int>(8 * g.dev.sms, static_cast<int>(ceil_div<long long>(nnz, 256))),
-                                            256, 0, s>>>(nnz, g.a64.get(), g.a32.get());
+                                            256, 0, s>>>(nnz, g.a64_p, g.a32.get());
         GB_CUDA_CHECK(cudaGetLastError());
-    }
-    g.matrix_loaded = true;
-    const size_t nv = static_cast<size_t>(std::max(n, 1));
-    g.b.reserve(nv);
-    g.x.reserve(nv);
-    if (n > 0) {
-        GB_CUDA_CHECK(cudaMemcpyAsync(g.b.get(), rhs, sizeof(double) * static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
-        GB_CUDA_CHECK(cudaMemcpyAsync(g.x.get(), sol, sizeof(double) * static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
+        g.a32_src = g.a64_p;
+        g.launches += 1;
     }
     g.hh.reserve(static_cast<size_t>(im + 1) * (im + 3));
     if (g.mode == kModeMixed) {
@@ -329,20 +322,79 @@ std::pair<bool, int> PreconditionedGmres::Solve(const CsrMatrix* mat, double* rh
     } else {
         ensure_krylov(g.k64, n, im, s, g.dev.sms);
     }
-    GB_CUDA_CHECK(cudaStreamSynchronize(s));
-    const auto up1 = std::chrono::steady_clock::now();
-    stat_.total_init_time += std::chrono::duration<double>(up1 - up0).count();
     const double mv0 = g.kernel_ms[kKSpmv] + g.kernel_ms[kKResidual];
     const double pc0 = g.kernel_ms[kKLower] + g.kernel_ms[kKUpper];
     std::pair<bool, int> ret{true, 0};
     if (n > 0) {
-        ret = g.mode == kModeMixed ? solve_mode<float>(g, ilu, g.k32, param_) : solve_mode<double>(g, ilu, g.k64, param_);
-        if (ilu) const_cast<IluSolver::Impl*>(ilu)->check_status(s);
+        ret = g.mode == kModeMixed ? solve_mode<float>(g, ilu, g.k32, prm) : solve_mode<double>(g, ilu, g.k64, prm);
+        if (ilu) ilu->check_status(s);
+    }
+    stat.total_mv_time += (g.kernel_ms[kKSpmv] + g.kernel_ms[kKResidual] - mv0) * 1e-3;
+    stat.total_precon_time += (g.kernel_ms[kKLower] + g.kernel_ms[kKUpper] - pc0) * 1e-3;
+    return ret;
+}
+
+std::pair<bool, int> PreconditionedGmres::Solve(const CsrMatrix* mat, double* rhs, double* sol) {
+    const auto wall0 = std::chrono::steady_clock::now();
+    Impl& g = *impl_ensure();
+    g.init_once();
+    const int n = mat->size;
+    const long long nnz = mat->row_ptr[n];
+    cudaStream_t s = g.stream;
+    bool refresh = false;
+    if (!(g.keep_matrix && g.matrix_loaded && g.n == n && g.nnz == nnz)) {
+        g.rp.upload(mat->row_ptr, static_cast<size_t>(n) + 1, s);
+        g.ci.upload(mat->col_idx, static_cast<size_t>(nnz), s);
+        g.a64.upload(mat->value, static_cast<size_t>(nnz), s);
+        refresh = true;
+    }
+    g.matrix_loaded = true;
+    g.n = n;
+    g.nnz = nnz;
+    const size_t nv = static_cast<size_t>(std::max(n, 1));
+    g.b.reserve(nv);
+    g.x.reserve(nv);
+    if (n > 0) {
+        GB_CUDA_CHECK(cudaMemcpyAsync(g.b.get(), rhs, sizeof(double) * static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
+        GB_CUDA_CHECK(cudaMemcpyAsync(g.x.get(), sol, sizeof(double) * static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
+    }
+    g.rp_p = g.rp.get();
+    g.ci_p = g.ci.get();
+    g.a64_p = g.a64.get();
+    g.b_p = g.b.get();
+    g.x_p = g.x.get();
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+    stat_.total_init_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+    auto ret = solve_core(g, ilu_, param_, stat_, refresh);
+    if (n > 0) {
         GB_CUDA_CHECK(cudaMemcpyAsync(sol, g.x.get(), sizeof(double) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, s));
         GB_CUDA_CHECK(cudaStreamSynchronize(s));
     }
-    stat_.total_mv_time += (g.kernel_ms[kKSpmv] + g.kernel_ms[kKResidual] - mv0) * 1e-3;
-    stat_.total_precon_time += (g.kernel_ms[kKLower] + g.kernel_ms[kKUpper] - pc0) * 1e-3;
+    stat_.total_fgmr_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+    return ret;
+}
+
+std::pair<bool, int> PreconditionedGmres::SolveDevice(int n, const int* d_row_ptr, const int* d_col_idx,
+                                                      const double* d_values, const double* d_rhs, double* d_sol) {
+    const auto wall0 = std::chrono::steady_clock::now();
+    Impl& g = *impl_ensure();
+    g.init_once();
+    long long nnz = 0;
+    if (n > 0) {
+        int last = 0;
+        GB_CUDA_CHECK(cudaMemcpy(&last, d_row_ptr + n, sizeof(int), cudaMemcpyDeviceToHost));
+        nnz = last;
+    }
+    g.n = n;
+    g.nnz = nnz;
+    g.matrix_loaded = false;
+    g.rp_p = d_row_ptr;
+    g.ci_p = d_col_idx;
+    g.a64_p = d_values;
+    g.b_p = d_rhs;
+    g.x_p = d_sol;
+    auto ret = solve_core(g, ilu_, param_, stat_, !g.keep_matrix);
+    GB_CUDA_CHECK(cudaStreamSynchronize(g.stream));
     stat_.total_fgmr_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
     return ret;
 }

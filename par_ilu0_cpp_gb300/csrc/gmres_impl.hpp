@@ -43,6 +43,7 @@ struct Krylov {
     int n = 0;
     cudaGraphExec_t graph = nullptr;
     const void* graph_key[6] = {};
+    long long graph_nodes = 0;
     ~Krylov() {
         if (graph) cudaGraphExecDestroy(graph);
     }
@@ -60,6 +61,15 @@ struct PreconditionedGmres::Impl {
     gb300::DeviceBuffer<int> rp, ci;
     gb300::DeviceBuffer<double> a64, b, x;
     gb300::DeviceBuffer<float> a32;
+    // Operands of the current solve: the buffers above (host-array entry point) or the
+    // caller's device arrays (device-resident entry point).
+    const int* rp_p = nullptr;
+    const int* ci_p = nullptr;
+    const double* a64_p = nullptr;
+    const double* b_p = nullptr;
+    double* x_p = nullptr;
+    const double* a32_src = nullptr;  // a64 array that a32 was converted from
+    long long launches = 0;           // kernels launched by solves (graph nodes included)
     gb300::Krylov<double> k64;
     gb300::Krylov<float> k32;
     gb300::DeviceBuffer<double> hh, h1, h2, partial;
@@ -80,6 +90,7 @@ struct PreconditionedGmres::Impl {
     long long kernel_launches[gb300::kKKinds] = {};
     gb300::SolveReport report;
 
+    void init_once();
     ~Impl();
 };
 

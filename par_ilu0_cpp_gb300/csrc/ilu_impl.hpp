@@ -90,6 +90,7 @@ struct IluSolver::Impl {
     float last_factor_ms = 0.f;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int grid_fact = 0, grid_solve64 = 0, grid_solve32 = 0;
+    long long launches = 0;  // kernels launched by Factorize / Substitute
 
     ~Impl();
 

@@ -217,12 +217,18 @@ void IluSolver::SetupMatrix() {
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
-bool IluSolver::Factorize() {
+bool IluSolver::Factorize() { return FactorizeFrom(aMatrix_.value, false); }
+
+bool IluSolver::FactorizeDevice(const double* d_values) { return FactorizeFrom(d_values, true); }
+
+bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
     if (!impl_ || impl_->n != aMatrix_.size) throw std::runtime_error("SetupMatrix() must be called first");
     Impl& im = *impl_;
     cudaStream_t s = im.stream;
     const int n = im.n;
-    im.lu.upload(aMatrix_.value, static_cast<size_t>(im.nnz), s);
+    if (im.nnz > 0)
+        GB_CUDA_CHECK(cudaMemcpyAsync(im.lu.get(), values, sizeof(double) * static_cast<size_t>(im.nnz),
+                                      on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
     int init[kStatusWords] = {0, 0, INT_MAX, 0};
     GB_CUDA_CHECK(cudaMemcpyAsync(im.status.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
     if (++im.stamp == INT_MAX) {
@@ -237,9 +243,10 @@ bool IluSolver::Factorize() {
         GB_CUDA_CHECK(cudaGetLastError());
         gather_pack(im.L, true, im.lu.get(), s, im.dev.sms);
         gather_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+        im.launches += 7;
     }
     GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
-    if (im.copy_back && im.nnz > 0)
+    if (!on_device && im.copy_back && im.nnz > 0)
         GB_CUDA_CHECK(cudaMemcpyAsync(aMatrix_.value, im.lu.get(), sizeof(double) * static_cast<size_t>(im.nnz),
                                       cudaMemcpyDeviceToHost, s));
     int h[kStatusWords];

@@ -160,3 +160,31 @@ def test_nan_input_fails_cleanly():
     b = np.ones(a.n)
     res, ilu, gm = api.ilu_gmres(an, b, tol=1e-8, restart=10, maxit=50)
     assert not res.ok
+
+
+def test_device_resident_entry_points_match_host_path():
+    torch = pytest.importorskip("torch")
+    a = g.convdiff3d(20)
+    x_true, b = g.random_rhs(a, seed=3)
+    tol = 1e-8 * float(np.linalg.norm(b))
+    f, _ = api.iluk_symbolic(a, 0)
+    for mode in (0, 1):
+        ilu = api.IluSolver()
+        ilu.set_matrix(f)
+        assert ilu.setup() == 0
+        ilu.set_option(api.ILU_OPT_COPY_BACK, 0)
+        gm = api.Gmres(tol, 30, 1000)
+        gm.set_preconditioner(ilu)
+        gm.set_option(api.GMRES_OPT_MODE, mode)
+        d = {k: torch.from_numpy(v).cuda() for k, v in
+             (("rp", a.row_ptr), ("ci", a.col_idx), ("av", a.values), ("fv", f.values), ("b", b))}
+        dx = torch.zeros(a.n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        assert ilu.factorize_device(d["fv"].data_ptr()) == 0
+        ok, its = gm.solve_device(a.n, d["rp"].data_ptr(), d["ci"].data_ptr(), d["av"].data_ptr(), d["b"].data_ptr(),
+                                  dx.data_ptr())
+        assert ok
+        x_dev = dx.cpu().numpy()
+        res_host, _, _ = api.ilu_gmres(a, b, tol=tol, restart=30, maxit=1000, mode=mode, relative=False)
+        assert its == res_host.iterations
+        assert np.array_equal(x_dev, res_host.x)
