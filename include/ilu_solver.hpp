@@ -41,6 +41,7 @@ public:
      * untouched). */
     bool FactorizeDevice(const double* d_values);
 
+
     /* Implementation state (device buffers, schedules); opaque to users. */
     struct Impl;
     Impl* impl() { return impl_; }

@@ -40,7 +40,10 @@ bool LLJBASH_GmresSolveDevice(GmresHdl hdl, int n, const int* d_row_ptr, const i
 enum {
     /* 1 (default): copy the factors into GetMatrix()->value after Factorize, as the
      * reference's in-place factorisation leaves them; 0: keep them on the device only. */
-    LLJBASH_ILU_OPT_COPY_BACK = 1
+    LLJBASH_ILU_OPT_COPY_BACK = 1,
+    /* rows per substitution block (each CTA keeps one block's solution in shared memory);
+     * 0 = automatic.  Takes effect at the next IluSolverSetup. */
+    LLJBASH_ILU_OPT_BLOCK_ROWS = 2
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 

@@ -124,6 +124,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
             case LLJBASH_ILU_OPT_COPY_BACK:
                 s->impl()->copy_back = value != 0.0;
                 return 0;
+            case LLJBASH_ILU_OPT_BLOCK_ROWS:
+                if (value < 0 || value > 28000) throw std::runtime_error("block rows must be in [0, 28000]");
+                s->impl()->block_rows = static_cast<int>(value);
+                return 0;
             default:
                 g_last_error = "unknown ILU option";
                 return -1;

@@ -132,7 +132,7 @@ void enqueue_piece(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Kry
     }
     if (step == K.im) {
         L.run(kKUpdate, [&] {
-            gmres_backsolve_kernel<<<1, 32, 0, st>>>(ctl, H);
+            gmres_backsolve_kernel<<<1, 256, sizeof(double) * static_cast<size_t>(K.im * K.im + K.im + 1), st>>>(ctl, H);
             gmres_update_kernel<T><<<g.grid_update, 256, 0, st>>>(n, ld, K.Z.get(), g.x_p, ctl, H);
         });
         return;
@@ -189,9 +189,14 @@ void run_cycle(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Krylov<
         g.launches += L.count;
         return;
     }
-    const void* key[6] = {K.V.get(), ilu ? static_cast<const void*>(ilu->L.cols.get()) : nullptr,
-                          ilu ? static_cast<const void*>(ilu->U.v64.get()) : nullptr, ValueOf<T>::get(g), g.x_p,
-                          g.b_p};
+    const void* key[6] = {K.V.get(),
+                          ilu ? (ilu->block_mode ? static_cast<const void*>(ilu->LB.codes.get())
+                                                 : static_cast<const void*>(ilu->L.cols.get()))
+                              : nullptr,
+                          ilu ? (ilu->block_mode ? static_cast<const void*>(ilu->UB.v64.get())
+                                                 : static_cast<const void*>(ilu->U.v64.get()))
+                              : nullptr,
+                          ValueOf<T>::get(g), g.x_p, g.b_p};
     bool same = K.graph != nullptr;
     for (int k = 0; k < 6 && same; ++k) same = key[k] == K.graph_key[k];
     if (!same) {
@@ -288,6 +293,8 @@ void PreconditionedGmres::Impl::init_once() {
     grid_spmv = persistent_grid(spmv_kernel<double, double, double>, kSpmvWarps * kWarp, dev.sms, 8);
     grid_blas = persistent_grid(cgs_axpy_dot_kernel<double>, kBlasThreads, dev.sms, 2);
     grid_update = 4 * dev.sms;
+    GB_CUDA_CHECK(cudaFuncSetAttribute(gmres_backsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(double) * (kMaxKrylov * kMaxKrylov + kMaxKrylov + 1))));
     counters.reserve(4);
     GB_CUDA_CHECK(cudaMemsetAsync(counters.get(), 0, sizeof(unsigned) * 4, stream));
     ctl.reserve(1);

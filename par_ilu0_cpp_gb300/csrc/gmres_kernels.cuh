@@ -178,10 +178,11 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
         partial[static_cast<size_t>(blockIdx.x) * kPartialStride] = t;
     }
     if (!arrive_last(counter)) return;
+    __shared__ double s_norm;
+    reduce_partials(partial, gridDim.x, 1, &s_norm);
+    __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int k = 0; k < static_cast<int>(gridDim.x); ++k) t += __ldcg(partial + static_cast<size_t>(k) * kPartialStride);
-        const double beta = sqrt(t);
+        const double beta = sqrt(s_norm);
         ctl->beta = beta;
         ctl->beta0 = beta;
         ctl->steps = 0;
@@ -385,42 +386,60 @@ __global__ void __launch_bounds__(kBlasThreads)
     reduce_partials(partial, gridDim.x, nv, h2);
 }
 
-// Givens update and loop control for step s (single thread).  Mirrors
-// src/gmres.cpp:218-262 and the loop header at :199.
+// Givens update and loop control for step s.  Mirrors src/gmres.cpp:218-262 and the
+// loop header at :199.  The block stages column s of H (h1 + h2), the rotations c, s
+// and rs in shared memory; one thread then applies the rotations in order (a chain of
+// dependent operations that runs on shared memory instead of global memory).
 __device__ __forceinline__ void arnoldi_control(GmresCtl* ctl, Hess H, int s, const double* h1, const double* h2,
                                                 double t) {
+    __shared__ double col[kMaxKrylov + 2];
+    __shared__ double cs[kMaxKrylov + 1];
+    __shared__ double sn[kMaxKrylov + 1];
     constexpr double epsmac = 1e-16;
     const int im1 = H.im1;
     const int i = s;
     const int i1 = i + 1;
     double* hh = H.hh;
     double* c = H.c();
-    double* sn = H.s();
+    double* sg = H.s();
     double* rs = H.rs();
     const int ptih = i * im1;
-    for (int j = 0; j <= i; ++j) hh[ptih + j] = h1[j] + h2[j];
-    hh[ptih + i1] = t;
+    for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+        col[j] = __ldcg(h1 + j) + __ldcg(h2 + j);
+        cs[j] = c[j];
+        sn[j] = sg[j];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    col[i1] = t;
     ctl->i = i;
     ctl->steps = i + 1;
     if (t <= epsmac) {  // happy breakdown: leave the inner loop before the rotation
+        for (int j = 0; j <= i1; ++j) hh[ptih + j] = col[j];
         ctl->happy = 1;
         ctl->gate = -1;
         return;
     }
     ctl->inv_norm = 1.0 / t;
+    double prev = col[0];
     for (int k = 1; k <= i; ++k) {
         const int k1 = k - 1;
-        const double tt = hh[ptih + k1];
-        hh[ptih + k1] = c[k1] * tt + sn[k1] * hh[ptih + k];
-        hh[ptih + k] = -sn[k1] * tt + c[k1] * hh[ptih + k];
+        const double cur = col[k];
+        col[k1] = cs[k1] * prev + sn[k1] * cur;
+        prev = -sn[k1] * prev + cs[k1] * cur;
     }
-    double gam = sqrt(hh[ptih + i] * hh[ptih + i] + hh[ptih + i1] * hh[ptih + i1]);
+    if (i >= 1) col[i] = prev;
+    double gam = sqrt(col[i] * col[i] + col[i1] * col[i1]);
     if (gam == 0.0) gam = epsmac;
-    c[i] = hh[ptih + i] / gam;
-    sn[i] = hh[ptih + i1] / gam;
-    rs[i1] = -sn[i] * rs[i];
-    rs[i] = c[i] * rs[i];
-    hh[ptih + i] = c[i] * hh[ptih + i] + sn[i] * hh[ptih + i1];
+    const double ci = col[i] / gam;
+    const double si = col[i1] / gam;
+    c[i] = ci;
+    sg[i] = si;
+    const double rsi = rs[i];
+    rs[i1] = -si * rsi;
+    rs[i] = ci * rsi;
+    col[i] = ci * col[i] + si * col[i1];
+    for (int j = 0; j <= i1; ++j) hh[ptih + j] = col[j];
     const double beta = fabs(rs[i1]);
     ctl->beta = beta;
     if (isnan(beta)) {
@@ -487,28 +506,40 @@ __global__ void __launch_bounds__(kBlasThreads)
         partial[static_cast<size_t>(blockIdx.x) * kPartialStride] = t;
     }
     if (!arrive_last(counter)) return;
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int k = 0; k < static_cast<int>(gridDim.x); ++k) t += __ldcg(partial + static_cast<size_t>(k) * kPartialStride);
-        arnoldi_control(ctl, H, s, h1, h2, sqrt(t));
-    }
+    __shared__ double s_norm;
+    reduce_partials(partial, gridDim.x, 1, &s_norm);
+    __syncthreads();
+    arnoldi_control(ctl, H, s, h1, h2, sqrt(s_norm));
 }
 
-// Least-squares back substitution rs[0..i] <- H(0..i, 0..i)^{-1} rs (src/gmres.cpp:265-272),
-// single thread.  Skipped when the cycle took no step or ended on NaN.
-static __global__ void gmres_backsolve_kernel(GmresCtl* ctl, Hess H) {
-    if (threadIdx.x != 0 || ctl->status != kCtlRunning || ctl->steps == 0) return;
+// Least-squares back substitution rs[0..i] <- H(0..i, 0..i)^{-1} rs (src/gmres.cpp:265-272).
+// The block stages H's leading (i+1) x (i+1) triangle and rs in shared memory; one thread
+// then runs the reference's loop in the same order.  Skipped when the cycle took no step
+// or ended on NaN.
+// Dynamic shared memory: (m * m + m + 1) doubles.
+static __global__ void __launch_bounds__(256) gmres_backsolve_kernel(GmresCtl* ctl, Hess H) {
+    extern __shared__ double bs_smem[];
+    if (ctl->status != kCtlRunning || ctl->steps == 0) return;
     const int i = ctl->i;
     const int im1 = H.im1;
-    double* hh = H.hh;
-    double* rs = H.rs();
-    const int ptih = i * im1;
-    rs[i] = rs[i] / hh[ptih + i];
-    for (int ii = i - 1; ii >= 0; --ii) {
-        double t = rs[ii];
-        for (int j = ii + 1; j <= i; ++j) t -= hh[j * im1 + ii] * rs[j];
-        rs[ii] = t / hh[ii * im1 + ii];
+    const int w = i + 1;  // columns 0..i, rows 0..i
+    double* sh = bs_smem;
+    double* srs = bs_smem + (im1 - 1) * (im1 - 1);
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+        const int col = e / w;
+        const int row = e - col * w;
+        sh[col * w + row] = H.hh[col * im1 + row];
     }
+    for (int j = threadIdx.x; j <= i; j += blockDim.x) srs[j] = H.rs()[j];
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    srs[i] = srs[i] / sh[i * w + i];
+    for (int ii = i - 1; ii >= 0; --ii) {
+        double t = srs[ii];
+        for (int j = ii + 1; j <= i; ++j) t -= sh[j * w + ii] * srs[j];
+        srs[ii] = t / sh[ii * w + ii];
+    }
+    for (int j = 0; j <= i; ++j) H.rs()[j] = srs[j];
 }
 
 // x += sum_{j<=i} rs[j] Z[j] (src/gmres.cpp:274-276, j ascending) and Z[j] <- sentinel

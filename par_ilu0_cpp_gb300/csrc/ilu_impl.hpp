@@ -11,9 +11,9 @@
 
 namespace gb300 {
 
-// One packed triangular factor (see PackedTri): schedule arrays plus packed values in
-// FP64 and FP32.
-struct TriPack {
+// One packed triangular factor in the level-ordered warp layout (see PackedTri):
+// schedule arrays plus packed values in FP64 and FP32.
+struct LevelPack {
     int ntask = 0;
     long long slots = 0;
     DeviceBuffer<int> rows, off, len, cols, src, dsrc;
@@ -25,7 +25,7 @@ struct TriPack {
 };
 
 template <>
-inline PackedTri<double> TriPack::view<double>() const {
+inline PackedTri<double> LevelPack::view<double>() const {
     PackedTri<double> p;
     p.ntask = ntask;
     p.rows = rows.get();
@@ -37,13 +37,61 @@ inline PackedTri<double> TriPack::view<double>() const {
     return p;
 }
 template <>
-inline PackedTri<float> TriPack::view<float>() const {
+inline PackedTri<float> LevelPack::view<float>() const {
     PackedTri<float> p;
     p.ntask = ntask;
     p.rows = rows.get();
     p.off = off.get();
     p.len = len.get();
     p.cols = cols.get();
+    p.vals = v32.get();
+    p.dvals = d32.get();
+    return p;
+}
+
+// One packed triangular factor in the block-pipelined layout (see BlockTri): schedule
+// arrays plus packed values in FP64 and FP32.
+struct TriPack {
+    int nblk = 0;
+    int block_rows = 0;  // S, rows per block (the last block may be shorter)
+    int ntask = 0;
+    int levels = 0;      // block-internal levels summed over blocks
+    long long slots = 0;
+    size_t smem64 = 0, smem32 = 0;  // dynamic shared memory of the FP64 / FP32 kernels
+    DeviceBuffer<int> blk_row, blk_lvl, lvl_task, rows, off, len, codes, src, dsrc;
+    DeviceBuffer<double> v64, d64;
+    DeviceBuffer<float> v32, d32;
+
+    template <class T>
+    BlockTri<T> view() const;
+};
+
+template <>
+inline BlockTri<double> TriPack::view<double>() const {
+    BlockTri<double> p;
+    p.nblk = nblk;
+    p.blk_row = blk_row.get();
+    p.blk_lvl = blk_lvl.get();
+    p.lvl_task = lvl_task.get();
+    p.rows = rows.get();
+    p.off = off.get();
+    p.len = len.get();
+    p.codes = codes.get();
+    p.vals = v64.get();
+    p.dvals = d64.get();
+    return p;
+}
+template <>
+inline BlockTri<float> TriPack::view<float>() const {
+    BlockTri<float> p;
+    p.nblk = nblk;
+    p.blk_row = blk_row.get();
+    p.blk_lvl = blk_lvl.get();
+    p.lvl_task = lvl_task.get();
+    p.rows = rows.get();
+    p.off = off.get();
+    p.len = len.get();
+    p.codes = codes.get();
     p.vals = v32.get();
     p.dvals = d32.get();
     return p;
@@ -77,7 +125,9 @@ struct IluSolver::Impl {
     gb300::DeviceBuffer<int> done;          // per-row ready stamps of the factorisation
     gb300::DeviceBuffer<unsigned> counters;  // ticket counters [0] fact, [1] L, [2] U
     gb300::DeviceBuffer<int> status;         // StatusWord array
-    gb300::TriPack L, U;
+    gb300::LevelPack L, U;     // level-ordered warp layout (default)
+    gb300::TriPack LB, UB;     // block-pipelined layout (block_rows > 0)
+    bool block_mode = false;
     gb300::DeviceBuffer<double> sb64, sy64, sx64;  // Substitute() work vectors
     gb300::DeviceBuffer<float> sy32;               // FP32 forward-sweep intermediate
 
@@ -89,7 +139,8 @@ struct IluSolver::Impl {
     int first_breakdown = -1;
     float last_factor_ms = 0.f;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    int grid_fact = 0, grid_solve64 = 0, grid_solve32 = 0;
+    int grid_fact = 0, grid_solve = 0, grid_block64 = 0, grid_block32 = 0;
+    int block_rows = 0;  // rows per substitution block (0 = automatic)
     long long launches = 0;  // kernels launched by Factorize / Substitute
 
     ~Impl();

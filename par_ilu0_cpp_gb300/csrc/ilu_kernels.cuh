@@ -148,7 +148,7 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
     }
 }
 
-// Packed triangular factor for the substitution kernels.  Rows are taken in the
+// Level-ordered packed triangular factor (default substitution layout).  Rows are taken in the
 // schedule order and grouped 32 to a task (one lane per row).  Task t owns slots
 // [off[t], off[t] + 32 * len[t]); entry k of lane l sits at off[t] + 32 k + l, so a
 // warp's loads of entry k are one coalesced 128/256-byte access.  Pad slots have
@@ -165,17 +165,6 @@ struct PackedTri {
     const T* vals = nullptr;     // [slots]
     const T* dvals = nullptr;    // [32 * ntask] diagonal (upper factor only)
 };
-
-// Gathers packed values from the CSR factor values: dst[s] = src[s] >= 0 ? lu[src[s]] : 0.
-template <class T>
-__global__ void pack_gather_kernel(long long count, const int* __restrict__ src, const double* __restrict__ lu,
-                                   T* __restrict__ dst) {
-    for (long long s = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; s < count;
-         s += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int p = src[s];
-        dst[s] = p >= 0 ? static_cast<T>(lu[p]) : T(0);
-    }
-}
 
 // Forward substitution with the unit lower factor: y = L^{-1} (scale * b).
 // With `scale` non-null, b is rescaled on the fly and the rescaled value is written back
@@ -241,6 +230,9 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
         const int row = U.rows[q];
         const int off = U.off[t];
         const int K = U.len[t];
+        // the diagonal is loaded before the dependency waits: the waits are ordered
+        // memory operations, so a load after them would add a full round trip per level
+        const T d = U.dvals[q];
         T acc = T(0);
         if (row >= 0) {
             acc = y[row];
@@ -265,8 +257,139 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
                 }
             }
         }
-        if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(acc / U.dvals[q]));
+        if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(acc / d));
         t = tn;
+    }
+}
+
+// Packed triangular factor for the substitution kernels (block-pipelined layout).
+//
+// Rows are cut into contiguous blocks of at most S rows; one CTA solves one block at a
+// time and keeps the block's solution in shared memory.  Inside a block rows are grouped
+// by their level in the block-internal dependency DAG (dependencies on rows of other
+// blocks do not count) and a level is solved by the whole CTA between two barriers, so
+// every block-internal dependency is a shared-memory read.  Dependencies on other blocks
+// are read from the global solution with a value-as-flag wait; blocks are taken from a
+// ticket counter in dependency order (ascending for L, descending for U), so a block
+// only waits for blocks whose CTAs are already running: no deadlock, no co-residency
+// assumption.  Only the critical path's block boundaries pay the global handoff.
+//
+// Task t (32 rows of one level, one lane per row) owns slots [off[t], off[t] + 32 len[t]):
+// entry k of lane l sits at off[t] + 32 k + l (coalesced).  Entry codes: >= 0 global
+// column (other block), <= -2 local row -2-code (this block), -1 padding.  L entries are
+// kept in ascending column order and U entries in descending column order — the
+// accumulation order of the reference's substitute_row_L / _U (src/ilu_solver.cpp:687-696,
+// 719-729) — so the result is the same sequence of operations.
+template <class T>
+struct BlockTri {
+    int nblk = 0;
+    const int* blk_row = nullptr;   // [nblk + 1] first row of each block
+    const int* blk_lvl = nullptr;   // [nblk + 1] first level (index into lvl_task) of each block
+    const int* lvl_task = nullptr;  // [levels + 1] first task of each level
+    const int* rows = nullptr;      // [32 * ntask], -1 for padding
+    const int* off = nullptr;       // [ntask]
+    const int* len = nullptr;       // [ntask]
+    const int* codes = nullptr;     // [slots]
+    const T* vals = nullptr;        // [slots]
+    const T* dvals = nullptr;       // [32 * ntask] diagonal (upper factor only)
+};
+
+// Gathers packed values from the CSR factor values: dst[s] = src[s] >= 0 ? lu[src[s]] : 0.
+template <class T>
+__global__ void pack_gather_kernel(long long count, const int* __restrict__ src, const double* __restrict__ lu,
+                                   T* __restrict__ dst) {
+    for (long long s = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; s < count;
+         s += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int p = src[s];
+        dst[s] = p >= 0 ? static_cast<T>(lu[p]) : T(0);
+    }
+}
+
+constexpr int kSolveThreads = kSolveWarps * kWarp;
+
+// Draws the CTA's next block ticket (thread 0), broadcast through shared memory; the
+// grid's final draw resets the counter.
+__device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, int* s_slot) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int t = static_cast<int>(atomicAdd(counter, 1u));
+        if (t == nblk + static_cast<int>(gridDim.x) - 1) atomicExch(counter, 0u);
+        *s_slot = t;
+    }
+    __syncthreads();
+    return *s_slot;
+}
+
+// Forward (UPPER = false): out = L^{-1} (scale * in); with `scale`, in is rescaled in
+//   place (GMRES normalises its new Krylov vector in the same pass).
+// Backward (UPPER = true): out = U^{-1} in; in[row] is reset to the sentinel after it is
+//   read (ready for the next forward sweep).
+// out must hold the sentinel for every row on entry.
+template <class T, bool UPPER>
+__global__ void __launch_bounds__(kSolveThreads)
+    sptrsv_block_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
+                        const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);
+    __shared__ int s_ticket;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const T sc = (!UPPER && scale) ? static_cast<T>(*scale) : T(1);
+    for (int tk = draw_block_ticket(counter, P.nblk, &s_ticket); tk < P.nblk;
+         tk = draw_block_ticket(counter, P.nblk, &s_ticket)) {
+        const int c = UPPER ? P.nblk - 1 - tk : tk;
+        const int base = P.blk_row[c];
+        const int l0 = P.blk_lvl[c];
+        const int l1 = P.blk_lvl[c + 1];
+        for (int l = l0; l < l1; ++l) {
+            const int t1 = P.lvl_task[l + 1];
+            for (int t = P.lvl_task[l] + w; t < t1; t += kSolveWarps) {
+                const int q = t * kWarp + lane;
+                const int row = P.rows[q];
+                const int o = P.off[t];
+                const int K = P.len[t];
+                const T d = UPPER ? P.dvals[q] : T(1);
+                T acc = T(0);
+                if (row >= 0) {
+                    acc = in[row];
+                    if (UPPER) {
+                        in[row] = Sentinel<T>::value();
+                    } else if (scale) {
+                        acc = acc * sc;
+                        in[row] = acc;
+                    }
+                }
+                for (int k0 = 0; k0 < K; k0 += 8) {
+                    int cd[8];
+                    T v[8], x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int sidx = o + (k0 + u) * kWarp + lane;
+                        cd[u] = (k0 + u < K) ? P.codes[sidx] : -1;
+                        v[u] = (k0 + u < K) ? P.vals[sidx] : T(0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        x[u] = cd[u] >= 0 ? ld_relaxed(out + cd[u]) : (cd[u] <= -2 ? xs[-2 - cd[u]] : T(0));
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        if (cd[u] != -1) {
+                            if (cd[u] >= 0 && Sentinel<T>::is(x[u])) x[u] = wait_value(out + cd[u], status);
+                            acc = fma(-v[u], x[u], acc);
+                        }
+                    }
+                }
+                if (row >= 0) {
+                    if (UPPER) acc = acc / d;
+                    acc = Sentinel<T>::canon(acc);
+                    xs[row - base] = acc;
+                    st_relaxed(out + row, acc);
+                }
+            }
+            __syncthreads();
+        }
     }
 }
 

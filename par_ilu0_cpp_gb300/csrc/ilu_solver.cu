@@ -21,8 +21,8 @@ namespace gb300 {
 // Host construction of a packed factor from a schedule `order` (rows in level order).
 // lower: entries [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1])
 // descending plus the diagonal position.
-static void build_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag,
-                       const std::vector<int>& order, bool lower, TriPack& P, cudaStream_t s) {
+static void build_level_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag,
+                       const std::vector<int>& order, bool lower, LevelPack& P, cudaStream_t s) {
     const int ntask = ceil_div(n, kWarp);
     std::vector<int> rows(static_cast<size_t>(ntask) * kWarp, -1);
     std::vector<int> off(ntask), len(ntask);
@@ -84,7 +84,7 @@ static void build_pack(int n, const int* rp, const int* ci, const std::vector<in
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
-static void gather_pack(const TriPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
+static void gather_level_pack(const LevelPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
     const int threads = 256;
     auto grid_for = [&](long long count) {
         long long g = ceil_div<long long>(count, threads);
@@ -100,6 +100,148 @@ static void gather_pack(const TriPack& P, bool lower, const double* lu, cudaStre
         pack_gather_kernel<float><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
     }
     GB_CUDA_CHECK(cudaGetLastError());
+}
+
+// Host construction of a block-pipelined packed factor (see BlockTri).
+// lower: entries [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1])
+// descending plus the diagonal position.
+static void build_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
+                       int block_rows, TriPack& P, cudaStream_t s) {
+    const int S = std::max(1, std::min(block_rows, std::max(n, 1)));
+    const int nblk = n > 0 ? ceil_div(n, S) : 0;
+    std::vector<int> blk_row(static_cast<size_t>(nblk) + 1), blk_lvl(static_cast<size_t>(nblk) + 1, 0);
+    std::vector<int> lvl_task(1, 0), rows, off, len, dsrc;
+    std::vector<int> depth(static_cast<size_t>(S)), cnt, ord;
+    auto ebeg = [&](int r) { return lower ? rp[r] : diag[r] + 1; };
+    auto eend = [&](int r) { return lower ? diag[r] : rp[r + 1]; };
+    long long slots = 0;
+    // pass 1: levels, tasks, lengths
+    std::vector<std::vector<int>> blk_order(static_cast<size_t>(nblk));
+    for (int c = 0; c < nblk; ++c) {
+        const int lo = c * S;
+        const int hi = std::min(n, lo + S);
+        blk_row[c] = lo;
+        int nlev = 0;
+        for (int s2 = 0; s2 < hi - lo; ++s2) {
+            const int r = lower ? lo + s2 : hi - 1 - s2;
+            int d = 0;
+            for (int p = ebeg(r); p < eend(r); ++p) {
+                const int col = ci[p];
+                if (col >= lo && col < hi) d = std::max(d, depth[col - lo] + 1);
+            }
+            depth[r - lo] = d;
+            nlev = std::max(nlev, d + 1);
+        }
+        cnt.assign(static_cast<size_t>(nlev) + 1, 0);
+        for (int r = lo; r < hi; ++r) ++cnt[depth[r - lo] + 1];
+        for (int l = 0; l < nlev; ++l) cnt[l + 1] += cnt[l];
+        ord.assign(static_cast<size_t>(hi - lo), 0);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int r = lo; r < hi; ++r) ord[fill[depth[r - lo]]++] = r;
+        for (int l = 0; l < nlev; ++l) {
+            for (int q0 = cnt[l]; q0 < cnt[l + 1]; q0 += kWarp) {
+                int K = 0;
+                for (int u = 0; u < kWarp; ++u) {
+                    const int q = q0 + u;
+                    if (q < cnt[l + 1]) {
+                        const int r = ord[q];
+                        rows.push_back(r);
+                        K = std::max(K, eend(r) - ebeg(r));
+                        if (!lower) dsrc.push_back(diag[r]);
+                    } else {
+                        rows.push_back(-1);
+                        if (!lower) dsrc.push_back(-1);
+                    }
+                }
+                off.push_back(static_cast<int>(slots));
+                len.push_back(K);
+                slots += static_cast<long long>(K) * kWarp;
+                if (slots > INT_MAX) throw std::runtime_error("triangular factor too large for 32-bit slot offsets");
+            }
+            lvl_task.push_back(static_cast<int>(off.size()));
+        }
+        blk_lvl[c + 1] = blk_lvl[c] + nlev;
+    }
+    blk_row[nblk] = n;
+    const int ntask = static_cast<int>(off.size());
+    // pass 2: entry codes and gather sources
+    std::vector<int> codes(static_cast<size_t>(slots), -1), src(static_cast<size_t>(slots), -1);
+    for (int t = 0; t < ntask; ++t) {
+        for (int l = 0; l < kWarp; ++l) {
+            const int r = rows[static_cast<size_t>(t) * kWarp + l];
+            if (r < 0) continue;
+            const int lo = (r / S) * S;
+            const int hi = std::min(n, lo + S);
+            int k = 0;
+            auto put = [&](int p) {
+                const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
+                const int col = ci[p];
+                codes[sidx] = (col >= lo && col < hi) ? -2 - (col - lo) : col;
+                src[sidx] = p;
+                ++k;
+            };
+            if (lower) {
+                for (int p = rp[r]; p < diag[r]; ++p) put(p);
+            } else {
+                for (int p = rp[r + 1] - 1; p > diag[r]; --p) put(p);
+            }
+        }
+    }
+    P.nblk = nblk;
+    P.block_rows = S;
+    P.ntask = ntask;
+    P.levels = blk_lvl[nblk];
+    P.slots = slots;
+    P.smem64 = sizeof(double) * static_cast<size_t>(S);
+    P.smem32 = sizeof(float) * static_cast<size_t>(S);
+    P.blk_row.upload(blk_row.data(), blk_row.size(), s);
+    P.blk_lvl.upload(blk_lvl.data(), blk_lvl.size(), s);
+    P.lvl_task.upload(lvl_task.data(), lvl_task.size(), s);
+    P.rows.upload(rows.data(), rows.size(), s);
+    P.off.upload(off.data(), off.size(), s);
+    P.len.upload(len.data(), len.size(), s);
+    P.codes.upload(codes.data(), codes.size(), s);
+    P.src.upload(src.data(), src.size(), s);
+    if (!lower) P.dsrc.upload(dsrc.data(), dsrc.size(), s);
+    P.v64.reserve(static_cast<size_t>(slots));
+    P.v32.reserve(static_cast<size_t>(slots));
+    if (!lower) {
+        P.d64.reserve(rows.size());
+        P.d32.reserve(rows.size());
+    }
+    // host vectors must outlive the asynchronous copies
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+}
+
+static void gather_pack(const TriPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
+    const int threads = 256;
+    auto grid_for = [&](long long count) {
+        long long g = ceil_div<long long>(count, threads);
+        return static_cast<int>(std::max<long long>(1, std::min<long long>(g, 8LL * sms)));
+    };
+    if (P.slots > 0) {
+        pack_gather_kernel<double><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v64.get());
+        pack_gather_kernel<float><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v32.get());
+    }
+    if (!lower && P.ntask > 0) {
+        const long long nd = static_cast<long long>(P.ntask) * kWarp;
+        pack_gather_kernel<double><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d64.get());
+        pack_gather_kernel<float><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
+    }
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+// Raises the dynamic shared-memory limit of both substitution kernels of type T to
+// `smem` bytes; returns the persistent grid (CTAs resident at that footprint).
+template <class T>
+static int configure_block_kernels(size_t smem, int sms) {
+    const int bytes = static_cast<int>(std::max<size_t>(smem, 16));
+    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    int per_sm = 0;
+    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_block_kernel<T, false>, kSolveThreads,
+                                                               static_cast<size_t>(bytes)));
+    return std::max(1, per_sm) * sms;
 }
 
 template <class T>
@@ -125,15 +267,31 @@ IluSolver::Impl::~Impl() {
 
 template <class T>
 void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const {
-    const int grid = sizeof(T) == 8 ? grid_solve64 : grid_solve32;
-    sptrsv_lower_kernel<T><<<grid, kSolveWarps * kWarp, 0, s>>>(L.view<T>(), b, scale, y, counters.get() + 1,
+    if (block_mode) {
+        if (LB.nblk == 0) return;
+        const int grid = sizeof(T) == 8 ? grid_block64 : grid_block32;
+        const size_t smem = sizeof(T) == 8 ? LB.smem64 : LB.smem32;
+        sptrsv_block_kernel<T, false><<<std::min(grid, LB.nblk), kSolveThreads, smem, s>>>(
+            LB.view<T>(), b, scale, y, counters.get() + 1, status.get(), gate, step);
+        return;
+    }
+    if (L.ntask == 0) return;
+    sptrsv_lower_kernel<T><<<grid_solve, kSolveThreads, 0, s>>>(L.view<T>(), b, scale, y, counters.get() + 1,
                                                                 status.get(), gate, step);
 }
 
 template <class T>
 void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const {
-    const int grid = sizeof(T) == 8 ? grid_solve64 : grid_solve32;
-    sptrsv_upper_kernel<T><<<grid, kSolveWarps * kWarp, 0, s>>>(U.view<T>(), y, x, counters.get() + 2, status.get(),
+    if (block_mode) {
+        if (UB.nblk == 0) return;
+        const int grid = sizeof(T) == 8 ? grid_block64 : grid_block32;
+        const size_t smem = sizeof(T) == 8 ? UB.smem64 : UB.smem32;
+        sptrsv_block_kernel<T, true><<<std::min(grid, UB.nblk), kSolveThreads, smem, s>>>(
+            UB.view<T>(), y, nullptr, x, counters.get() + 2, status.get(), gate, step);
+        return;
+    }
+    if (U.ntask == 0) return;
+    sptrsv_upper_kernel<T><<<grid_solve, kSolveThreads, 0, s>>>(U.view<T>(), y, x, counters.get() + 2, status.get(),
                                                                 gate, step);
 }
 
@@ -202,8 +360,14 @@ void IluSolver::SetupMatrix() {
     GB_CUDA_CHECK(cudaMemsetAsync(im.counters.get(), 0, sizeof(unsigned) * 8, s));
     im.status.reserve(kStatusWords);
     GB_CUDA_CHECK(cudaMemsetAsync(im.status.get(), 0, sizeof(int) * kStatusWords, s));
-    build_pack(n, rp, ci, im.an.diag, im.an.order_l, true, im.L, s);
-    build_pack(n, rp, ci, im.an.diag, im.an.order_u, false, im.U, s);
+    im.block_mode = im.block_rows > 0;
+    if (im.block_mode) {
+        build_pack(n, rp, ci, im.an.diag, true, im.block_rows, im.LB, s);
+        build_pack(n, rp, ci, im.an.diag, false, im.block_rows, im.UB, s);
+    } else {
+        build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, im.L, s);
+        build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, im.U, s);
+    }
     const size_t nv = static_cast<size_t>(std::max(n, 1));
     im.sb64.reserve(nv);
     im.sy64.reserve(nv);
@@ -212,8 +376,14 @@ void IluSolver::SetupMatrix() {
     fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
     fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
     im.grid_fact = persistent_grid(ilu_factor_kernel, kFactWarps * kWarp, im.dev.sms);
-    im.grid_solve64 = persistent_grid(sptrsv_lower_kernel<double>, kSolveWarps * kWarp, im.dev.sms);
-    im.grid_solve32 = persistent_grid(sptrsv_lower_kernel<float>, kSolveWarps * kWarp, im.dev.sms);
+    // One CTA of the level-ordered kernel per SM: fewer spinning warps contend less for
+    // L2 and the ready values propagate faster (measured: 1/SM beats full occupancy by
+    // 1.8x on the 128^3 7-point factor).
+    im.grid_solve = im.dev.sms;
+    if (im.block_mode) {
+        im.grid_block64 = configure_block_kernels<double>(std::max(im.LB.smem64, im.UB.smem64), im.dev.sms);
+        im.grid_block32 = configure_block_kernels<float>(std::max(im.LB.smem32, im.UB.smem32), im.dev.sms);
+    }
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
@@ -241,8 +411,13 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
             n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(),
             im.shift_active ? im.shift.get() : nullptr, im.done.get(), im.stamp, im.counters.get(), im.status.get());
         GB_CUDA_CHECK(cudaGetLastError());
-        gather_pack(im.L, true, im.lu.get(), s, im.dev.sms);
-        gather_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+        if (im.block_mode) {
+            gather_pack(im.LB, true, im.lu.get(), s, im.dev.sms);
+            gather_pack(im.UB, false, im.lu.get(), s, im.dev.sms);
+        } else {
+            gather_level_pack(im.L, true, im.lu.get(), s, im.dev.sms);
+            gather_level_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+        }
         im.launches += 7;
     }
     GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
@@ -279,3 +454,4 @@ void IluSolver::Substitute(const double* b, double* x) {
 }
 
 }  // namespace lljbash
+

@@ -188,3 +188,21 @@ def test_device_resident_entry_points_match_host_path():
         res_host, _, _ = api.ilu_gmres(a, b, tol=tol, restart=30, maxit=1000, mode=mode, relative=False)
         assert its == res_host.iterations
         assert np.array_equal(x_dev, res_host.x)
+
+
+@pytest.mark.parametrize("block_rows", [1, 7, 64, 1000])
+def test_block_partition_does_not_change_results(golden, block_rows):
+    """Any block size gives the same operations in the same order: identical results."""
+    ref = factorize(golden.f_csr())
+    x_ref = ref.substitute(golden.b)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
+    ilu.set_matrix(golden.f_csr())
+    assert ilu.setup() == 0
+    assert ilu.factorize() == 0
+    x = ilu.substitute(golden.b)
+    assert np.array_equal(x, x_ref)
+    gm = api.Gmres(golden.tol, golden.restart, 1000)
+    gm.set_preconditioner(ilu)
+    res = gm.solve(golden.a, golden.b)
+    assert res.ok and abs(res.iterations - golden.gmres_iters) <= 1
