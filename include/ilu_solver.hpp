@@ -41,6 +41,12 @@ public:
      * untouched). */
     bool FactorizeDevice(const double* d_values);
 
+    /* GB300 extension: Substitute() on device arrays (d_b read, d_x written, n entries)
+     * that allocates nothing: its intermediate vector and counters live in a static
+     * device array of the library (at most 2,097,152 rows).  The first call on a device
+     * resolves that array's address and should come before any stream capture; calls
+     * that overlap on the GPU share the array and race. */
+    void SubstituteDeviceNoAlloc(const double* d_b, double* d_x);
 
     /* Implementation state (device buffers, schedules); opaque to users. */
     struct Impl;

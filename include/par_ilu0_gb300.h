@@ -36,6 +36,18 @@ int LLJBASH_IluSolverFactorizeDevice(IluSolverHdl hdl, const double* d_values);
 bool LLJBASH_GmresSolveDevice(GmresHdl hdl, int n, const int* d_row_ptr, const int* d_col_idx, const double* d_values,
                               const double* d_rhs, double* d_sol, int* iter);
 
+/* x = U^{-1} L^{-1} b on device arrays (d_b: n doubles read, d_x: n doubles written),
+ * allocating nothing.  No counterpart in the reference.  For callers that cannot call
+ * cudaMalloc when they apply the preconditioner: an application that reserved all
+ * device memory for its own pool, or one that must not let a library call
+ * cudaMalloc / cudaFree (which may synchronise the device) inside its pipelined work.
+ * The forward-sweep vector and the kernels' counters live in one static device array
+ * of the library, so n is limited to 2,097,152 rows (larger n returns -1).  The first
+ * call on a device resolves that array's address (cudaGetSymbolAddress) and should be
+ * made before any stream capture.  Every call shares the array; calls whose GPU work
+ * overlaps race on it.  Same return codes as the other entry points. */
+int LLJBASH_IluSolverSubstituteDeviceNoAlloc(IluSolverHdl hdl, const double* d_b, double* d_x);
+
 /* ILU solver options. */
 enum {
     /* 1 (default): copy the factors into GetMatrix()->value after Factorize, as the

@@ -105,6 +105,7 @@ def load() -> ctypes.CDLL:
         "LLJBASH_Gb300LastError": (ctypes.c_char_p, []),
         "LLJBASH_IluSolverSubstitute": (ctypes.c_int, [ctypes.c_void_p, _D, _D]),
         "LLJBASH_IluSolverFactorizeDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+        "LLJBASH_IluSolverSubstituteDeviceNoAlloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
         "LLJBASH_GmresSolveDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I]),
         "LLJBASH_IluSolverSetOption": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),

@@ -94,6 +94,15 @@ int LLJBASH_IluSolverSubstitute(IluSolverHdl hdl, const double* b, double* x) {
     return 0;
 }
 
+int LLJBASH_IluSolverSubstituteDeviceNoAlloc(IluSolverHdl hdl, const double* d_b, double* d_x) {
+    try {
+        ilu(hdl)->SubstituteDeviceNoAlloc(d_b, d_x);
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
 int LLJBASH_IluSolverFactorizeDevice(IluSolverHdl hdl, const double* d_values) {
     try {
         ilu(hdl)->FactorizeDevice(d_values);

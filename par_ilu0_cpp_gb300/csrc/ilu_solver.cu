@@ -7,7 +7,9 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "analysis.hpp"
@@ -455,3 +457,97 @@ void IluSolver::Substitute(const double* b, double* x) {
 
 }  // namespace lljbash
 
+// ---------------------------------------------------------------------------------
+// Allocation-free substitution.
+//
+// Some callers cannot allocate device memory at the moment they need a preconditioner
+// application: an application that reserves all device memory up front for its own
+// pool (cudaMalloc then fails), or one that must not let a library call cudaMalloc /
+// cudaFree because those may synchronise the whole device in the middle of its
+// pipelined work.  IluSolver::SubstituteDeviceNoAlloc serves them: the intermediate
+// vector of the forward sweep and the kernels' ticket counters and status words live
+// in one statically sized device array of this file (g_noalloc_scratch, 16 MiB + 256 B,
+// reserved on every GPU that loads the library until the process exits), so the call
+// itself allocates nothing.  Its limit is kNoAllocMaxRows rows.
+//
+// The array's host-side name is only a stand-in: host code obtains its device address
+// with cudaGetSymbolAddress, once per device, the first time the entry point runs on
+// that device (with that device current).  That first call should therefore come
+// before any stream capture.  All calls share the array and it keeps the previous
+// call's contents, so every call re-initialises what must start at zero or at the
+// sentinel; calls whose GPU work overlaps (different streams, threads or solvers at
+// the same time) race on it.
+// ---------------------------------------------------------------------------------
+namespace gb300 {
+
+constexpr long long kNoAllocMaxRows = 1ll << 21;
+constexpr size_t kNoAllocScratchBytes = static_cast<size_t>(kNoAllocMaxRows) * sizeof(double) + 256;
+// layout: [0, 8 * kNoAllocMaxRows) forward-sweep vector; then 4 ticket counters
+// (unsigned) and kStatusWords status ints.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+std::vector<void*> g_noalloc_addr;  // per device ordinal, nullptr until set up
+
+void* noalloc_scratch_address(int device) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (device >= static_cast<int>(g_noalloc_addr.size())) g_noalloc_addr.resize(static_cast<size_t>(device) + 1, nullptr);
+    if (g_noalloc_addr[device] == nullptr) {
+        void* ptr = nullptr;
+        const cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (err != cudaSuccess || ptr == nullptr) {
+            throw std::runtime_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") +
+                                     cudaGetErrorString(err));
+        }
+        g_noalloc_addr[device] = ptr;
+    }
+    return g_noalloc_addr[device];
+}
+}  // namespace
+
+}  // namespace gb300
+
+namespace lljbash {
+
+void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
+    using namespace gb300;
+    if (!impl_ || !impl_->factorized) throw std::runtime_error("Factorize() must be called first");
+    Impl& im = *impl_;
+    const int n = im.n;
+    if (n > kNoAllocMaxRows)
+        throw std::runtime_error("SubstituteDeviceNoAlloc supports at most 2097152 rows (static scratch limit)");
+    if (n == 0) return;
+    int device = 0;
+    GB_CUDA_CHECK(cudaGetDevice(&device));
+    unsigned char* base = static_cast<unsigned char*>(noalloc_scratch_address(device));
+    double* y = reinterpret_cast<double*>(base);
+    unsigned* counters = reinterpret_cast<unsigned*>(base + kNoAllocMaxRows * sizeof(double));
+    int* status = reinterpret_cast<int*>(counters + 4);
+    cudaStream_t s = im.stream;
+    // what must start at zero (counters, status) and at the sentinel (y, x)
+    GB_CUDA_CHECK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned) + kStatusWords * sizeof(int), s));
+    fill_sentinel(y, n, s, im.dev.sms);
+    fill_sentinel(d_x, n, s, im.dev.sms);
+    double* b = const_cast<double*>(d_b);  // read only: no scale is passed to the forward sweep
+    if (im.block_mode) {
+        if (im.LB.nblk > 0) {
+            sptrsv_block_kernel<double, false><<<std::min(im.grid_block64, im.LB.nblk), kSolveThreads, im.LB.smem64, s>>>(
+                im.LB.view<double>(), b, nullptr, y, counters + 1, status, nullptr, 0);
+            sptrsv_block_kernel<double, true><<<std::min(im.grid_block64, im.UB.nblk), kSolveThreads, im.UB.smem64, s>>>(
+                im.UB.view<double>(), y, nullptr, d_x, counters + 2, status, nullptr, 0);
+        }
+    } else if (im.L.ntask > 0) {
+        sptrsv_lower_kernel<double><<<im.grid_solve, kSolveThreads, 0, s>>>(im.L.view<double>(), b, nullptr, y,
+                                                                            counters + 1, status, nullptr, 0);
+        sptrsv_upper_kernel<double><<<im.grid_solve, kSolveThreads, 0, s>>>(im.U.view<double>(), y, d_x, counters + 2,
+                                                                            status, nullptr, 0);
+    }
+    GB_CUDA_CHECK(cudaGetLastError());
+    int h[kStatusWords];
+    GB_CUDA_CHECK(cudaMemcpyAsync(h, status, sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (h[kStatusTimeout] != 0) throw std::runtime_error("dependency wait timed out on the device");
+}
+
+}  // namespace lljbash
