@@ -41,6 +41,13 @@ public:
      * untouched). */
     bool FactorizeDevice(const double* d_values);
 
+    /* GB300 extension: learned diagonal shift.  With a model set (369 FP32 MLP
+     * parameters), every factorisation first runs the fused feature + MLP pre-pass and
+     * factorises A + diag(shift); a zero or non-finite pivot makes it fall back to plain
+     * ILU.  Rows whose predicted relative shift is below min_shift get none.  nullptr
+     * removes the model. */
+    void SetShiftModel(const float* params, int nparams, float min_shift);
+
     /* GB300 extension: Substitute() on device arrays (d_b read, d_x written, n entries)
      * that allocates nothing: its intermediate vector and counters live in a static
      * device array of the library (at most 2,097,152 rows).  The first call on a device

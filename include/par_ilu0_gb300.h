@@ -63,6 +63,37 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
  * length n; NULL removes it).  The learned-shift path sets it from the MLP. */
 int LLJBASH_IluSolverSetShift(IluSolverHdl hdl, const double* shift);
 
+/* Learned diagonal shift (no counterpart in the reference).  params: the 369 FP32
+ * parameters of the 4-16-16-1 MLP (layout in csrc/mlp.cuh), NULL to remove the model.
+ * Every later factorisation runs the fused feature + MLP pre-pass and factorises
+ * A + diag(shift); a zero / non-finite pivot falls back to plain ILU (reported by
+ * LLJBASH_IluInfo.shift_applied).  Rows with predicted relative shift < min_shift get
+ * none. */
+int LLJBASH_IluSolverSetShiftModel(IluSolverHdl hdl, const float* params, int nparams, double min_shift);
+
+/* Number of MLP parameters (369). */
+int LLJBASH_ShiftModelNumParams(void);
+
+/* Per-row MLP features X[n][4] of a host CSR matrix (rows column-sorted, diagonal
+ * present), computed on the device; depth: level depth per row (NULL = 0) of nlev
+ * levels.  With params, y[n] receives the MLP outputs (relative shifts). */
+int LLJBASH_ShiftFeatures(int n, const int* row_ptr, const int* col_idx, const double* values, const int* depth,
+                          int nlev, float* X, const float* params, float* y);
+
+/* GPU trainer of the shift MLP (hand-written forward / backward / Adam kernels). */
+typedef void* LLJBASH_ShiftTrainerHdl;
+LLJBASH_ShiftTrainerHdl LLJBASH_ShiftTrainerCreate(unsigned seed);
+void LLJBASH_ShiftTrainerDestroy(LLJBASH_ShiftTrainerHdl tr);
+int LLJBASH_ShiftTrainerSetData(LLJBASH_ShiftTrainerHdl tr, const float* X, const float* targets, int n);
+int LLJBASH_ShiftTrainerSetParams(LLJBASH_ShiftTrainerHdl tr, const float* params);
+int LLJBASH_ShiftTrainerGetParams(LLJBASH_ShiftTrainerHdl tr, float* params);
+/* One Adam step on the samples idx[0..batch) (host array); *loss = mean squared error. */
+int LLJBASH_ShiftTrainerStep(LLJBASH_ShiftTrainerHdl tr, const int* idx, int batch, float lr, double* loss);
+/* Mean-squared-error loss and its gradient over the whole data set (no update). */
+int LLJBASH_ShiftTrainerGradient(LLJBASH_ShiftTrainerHdl tr, float* grad, double* loss);
+/* MLP outputs for the whole data set. */
+int LLJBASH_ShiftTrainerPredict(LLJBASH_ShiftTrainerHdl tr, float* y);
+
 typedef struct LLJBASH_IluInfo {
     int n;
     int nnz;
@@ -72,6 +103,7 @@ typedef struct LLJBASH_IluInfo {
     int first_breakdown;  /* smallest such row, -1 if none */
     double factor_ms;     /* device time of the last Factorize (factorisation + packing) */
     long long kernel_launches; /* kernels launched by this solver so far */
+    int shift_applied;    /* the last Factorize used a diagonal shift (learned or explicit) */
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

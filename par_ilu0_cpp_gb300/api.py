@@ -24,6 +24,7 @@ CORE_LIB_PATH = os.path.join(LIB_DIR, "libpar-ilu0-gmres.so")
 
 _I = ctypes.POINTER(ctypes.c_int)
 _D = ctypes.POINTER(ctypes.c_double)
+_F = ctypes.POINTER(ctypes.c_float)
 
 
 class CsrMatrix(ctypes.Structure):
@@ -46,7 +47,7 @@ class GmresStat(ctypes.Structure):
 class IluInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("nnz", ctypes.c_int), ("levels_lower", ctypes.c_int),
                 ("levels_upper", ctypes.c_int), ("breakdowns", ctypes.c_int), ("first_breakdown", ctypes.c_int),
-                ("factor_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong)]
+                ("factor_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong), ("shift_applied", ctypes.c_int)]
 
 
 class GmresReport(ctypes.Structure):
@@ -118,6 +119,18 @@ def load() -> ctypes.CDLL:
         "LLJBASH_GmresGetKernelTimes": (ctypes.c_int, [ctypes.c_void_p, _D, ctypes.POINTER(ctypes.c_longlong),
                                                        ctypes.c_int]),
         "LLJBASH_GmresResetKernelTimes": (ctypes.c_int, [ctypes.c_void_p]),
+        "LLJBASH_IluSolverSetShiftModel": (ctypes.c_int, [ctypes.c_void_p, _F, ctypes.c_int, ctypes.c_double]),
+        "LLJBASH_ShiftModelNumParams": (ctypes.c_int, []),
+        "LLJBASH_ShiftFeatures": (ctypes.c_int, [ctypes.c_int, _I, _I, _D, _I, ctypes.c_int, _F, _F, _F]),
+        "LLJBASH_ShiftTrainerCreate": (ctypes.c_void_p, [ctypes.c_uint]),
+        "LLJBASH_ShiftTrainerDestroy": (None, [ctypes.c_void_p]),
+        "LLJBASH_ShiftTrainerSetData": (ctypes.c_int, [ctypes.c_void_p, _F, _F, ctypes.c_int]),
+        "LLJBASH_ShiftTrainerSetParams": (ctypes.c_int, [ctypes.c_void_p, _F]),
+        "LLJBASH_ShiftTrainerGetParams": (ctypes.c_int, [ctypes.c_void_p, _F]),
+        "LLJBASH_ShiftTrainerStep": (ctypes.c_int, [ctypes.c_void_p, _I, ctypes.c_int, ctypes.c_float,
+                                                    ctypes.POINTER(ctypes.c_double)]),
+        "LLJBASH_ShiftTrainerGradient": (ctypes.c_int, [ctypes.c_void_p, _F, ctypes.POINTER(ctypes.c_double)]),
+        "LLJBASH_ShiftTrainerPredict": (ctypes.c_int, [ctypes.c_void_p, _F]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):
@@ -146,6 +159,10 @@ def _ip(a):
 
 def _dp(a):
     return a.ctypes.data_as(_D)
+
+
+def _fp(a):
+    return a.ctypes.data_as(_F) if a is not None else None
 
 
 class HostCsrView:
@@ -289,6 +306,16 @@ class IluSolver:
         if rc != 0:
             raise RuntimeError(last_error())
 
+    def set_shift_model(self, params, min_shift: float = 0.0) -> None:
+        """Learned-shift MLP parameters (369 floats) for later factorisations; None removes it."""
+        if params is None:
+            rc = self.lib.LLJBASH_IluSolverSetShiftModel(self.h, None, 0, 0.0)
+        else:
+            p = np.ascontiguousarray(params, dtype=np.float32)
+            rc = self.lib.LLJBASH_IluSolverSetShiftModel(self.h, _fp(p), int(p.size), float(min_shift))
+        if rc != 0:
+            raise RuntimeError(last_error())
+
     def info(self) -> IluInfo:
         inf = IluInfo()
         self.lib.LLJBASH_IluSolverGetInfo(self.h, ctypes.byref(inf))
@@ -400,3 +427,79 @@ def ilu_gmres(a: Csr, b, lof: int = 0, tol: float = 1e-8, restart: int = 30, max
     g.set_option(GMRES_OPT_MODE, mode)
     res = g.solve(a, b, x0)
     return res, ilu, g
+
+
+def shift_features(a: Csr, depth=None, nlev: int = 1, params=None):
+    """Per-row MLP features X[n, 4] (and MLP outputs y[n] with params), on the device."""
+    lib = load()
+    X = np.empty((a.n, 4), dtype=np.float32)
+    y = np.empty(a.n, dtype=np.float32) if params is not None else None
+    p = np.ascontiguousarray(params, dtype=np.float32) if params is not None else None
+    d = _i32(depth) if depth is not None else None
+    rc = lib.LLJBASH_ShiftFeatures(a.n, _ip(_i32(a.row_ptr)), _ip(_i32(a.col_idx)), _dp(_f64(a.values)),
+                                   _ip(d) if d is not None else None, int(nlev), _fp(X), _fp(p), _fp(y))
+    if rc != 0:
+        raise RuntimeError(last_error())
+    return (X, y) if params is not None else X
+
+
+class ShiftTrainer:
+    """GPU trainer of the shift MLP (hand-written forward / backward / Adam kernels)."""
+
+    def __init__(self, seed: int = 0):
+        self.lib = load()
+        self.h = self.lib.LLJBASH_ShiftTrainerCreate(int(seed))
+        if not self.h:
+            raise RuntimeError(last_error())
+        self.nparams = self.lib.LLJBASH_ShiftModelNumParams()
+
+    def close(self):
+        if self.h:
+            self.lib.LLJBASH_ShiftTrainerDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_data(self, X, targets):
+        self._X = np.ascontiguousarray(X, dtype=np.float32)
+        self._T = np.ascontiguousarray(targets, dtype=np.float32)
+        self.n = self._T.size
+        if self.lib.LLJBASH_ShiftTrainerSetData(self.h, _fp(self._X), _fp(self._T), int(self.n)) != 0:
+            raise RuntimeError(last_error())
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.empty(self.nparams, dtype=np.float32)
+        if self.lib.LLJBASH_ShiftTrainerGetParams(self.h, _fp(p)) != 0:
+            raise RuntimeError(last_error())
+        return p
+
+    @params.setter
+    def params(self, p):
+        q = np.ascontiguousarray(p, dtype=np.float32)
+        if self.lib.LLJBASH_ShiftTrainerSetParams(self.h, _fp(q)) != 0:
+            raise RuntimeError(last_error())
+
+    def step(self, idx, lr: float) -> float:
+        ii = _i32(idx)
+        loss = ctypes.c_double(0.0)
+        if self.lib.LLJBASH_ShiftTrainerStep(self.h, _ip(ii), int(ii.size), float(lr), ctypes.byref(loss)) != 0:
+            raise RuntimeError(last_error())
+        return float(loss.value)
+
+    def gradient(self):
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = ctypes.c_double(0.0)
+        if self.lib.LLJBASH_ShiftTrainerGradient(self.h, _fp(g), ctypes.byref(loss)) != 0:
+            raise RuntimeError(last_error())
+        return g, float(loss.value)
+
+    def predict(self) -> np.ndarray:
+        y = np.empty(self.n, dtype=np.float32)
+        if self.lib.LLJBASH_ShiftTrainerPredict(self.h, _fp(y)) != 0:
+            raise RuntimeError(last_error())
+        return y

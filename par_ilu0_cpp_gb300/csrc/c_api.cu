@@ -12,6 +12,8 @@
 #include "ilu_impl.hpp"
 #include "ilu_solver.hpp"
 #include "ilu_solver_c.h"
+#include "mlp.cuh"
+#include "mlp_impl.hpp"
 #include "par_ilu0_gb300.h"
 
 using lljbash::IluSolver;
@@ -164,6 +166,76 @@ int LLJBASH_IluSolverSetShift(IluSolverHdl hdl, const double* shift) {
     return 0;
 }
 
+int LLJBASH_IluSolverSetShiftModel(IluSolverHdl hdl, const float* params, int nparams, double min_shift) {
+    try {
+        ilu(hdl)->SetShiftModel(params, nparams, static_cast<float>(min_shift));
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+int LLJBASH_ShiftModelNumParams(void) { return gb300::kMlpParams; }
+
+int LLJBASH_ShiftFeatures(int n, const int* row_ptr, const int* col_idx, const double* values, const int* depth,
+                          int nlev, float* X, const float* params, float* y) {
+    try {
+        gb300::shift_features_host(n, row_ptr, col_idx, values, depth, nlev, X, params, y);
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+    return 0;
+}
+
+LLJBASH_ShiftTrainerHdl LLJBASH_ShiftTrainerCreate(unsigned seed) {
+    try {
+        return new gb300::ShiftTrainer(seed);
+    } catch (const std::exception& e) {
+        fail(e);
+        return nullptr;
+    }
+}
+
+void LLJBASH_ShiftTrainerDestroy(LLJBASH_ShiftTrainerHdl tr) { delete static_cast<gb300::ShiftTrainer*>(tr); }
+
+#define GB_TRY(stmt)                       \
+    try {                                  \
+        stmt;                              \
+    } catch (const std::exception& e) {    \
+        return fail(e);                    \
+    }                                      \
+    return 0
+
+int LLJBASH_ShiftTrainerSetData(LLJBASH_ShiftTrainerHdl tr, const float* X, const float* targets, int n) {
+    GB_TRY(static_cast<gb300::ShiftTrainer*>(tr)->set_data(X, targets, n));
+}
+
+int LLJBASH_ShiftTrainerSetParams(LLJBASH_ShiftTrainerHdl tr, const float* params) {
+    GB_TRY(static_cast<gb300::ShiftTrainer*>(tr)->set_params(params));
+}
+
+int LLJBASH_ShiftTrainerGetParams(LLJBASH_ShiftTrainerHdl tr, float* params) {
+    GB_TRY(static_cast<gb300::ShiftTrainer*>(tr)->get_params(params));
+}
+
+int LLJBASH_ShiftTrainerStep(LLJBASH_ShiftTrainerHdl tr, const int* idx, int batch, float lr, double* loss) {
+    GB_TRY({
+        const double l = static_cast<gb300::ShiftTrainer*>(tr)->run(idx, batch, lr, true, nullptr);
+        if (loss) *loss = l;
+    });
+}
+
+int LLJBASH_ShiftTrainerGradient(LLJBASH_ShiftTrainerHdl tr, float* grad, double* loss) {
+    GB_TRY({
+        const double l = static_cast<gb300::ShiftTrainer*>(tr)->run(nullptr, 0, 0.f, false, grad);
+        if (loss) *loss = l;
+    });
+}
+
+int LLJBASH_ShiftTrainerPredict(LLJBASH_ShiftTrainerHdl tr, float* y) {
+    GB_TRY(static_cast<gb300::ShiftTrainer*>(tr)->predict(y));
+}
+
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     IluSolver* s = ilu(hdl);
     if (!info) return -1;
@@ -181,6 +253,7 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->first_breakdown = im->first_breakdown;
     info->factor_ms = im->last_factor_ms;
     info->kernel_launches = im->launches;
+    info->shift_applied = im->shift_applied ? 1 : 0;
     return 0;
 }
 

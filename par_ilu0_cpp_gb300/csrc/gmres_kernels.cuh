@@ -547,25 +547,42 @@ static __global__ void __launch_bounds__(256) gmres_backsolve_kernel(GmresCtl* c
 template <class T>
 __global__ void __launch_bounds__(256)
     gmres_update_kernel(int n, long long ld, T* __restrict__ Z, double* __restrict__ x, const GmresCtl* ctl, Hess H) {
+    __shared__ double srs[kMaxKrylov];
     if (ctl->status != kCtlRunning || ctl->steps == 0) return;
     const int nz = ctl->i + 1;
-    const double* rs = H.rs();
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) srs[j] = H.rs()[j];
+    __syncthreads();
     // plain path: x += sum_j rs[j] z_j in FP64 in ascending j; mixed path: the
-    // correction sum_j rs[j] z_j is formed in FP32 and added to the FP64 x.
+    // correction sum_j rs[j] z_j is formed in FP32 and added to the FP64 x.  Eight
+    // independent loads are in flight per thread; the sentinel stores follow the loads.
     using Acc = typename ChunkCfg<T>::Acc;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         Acc d = Acc(0);
         double xv = x[r];
-        for (int j = 0; j < nz; ++j) {
-            T* zj = Z + static_cast<long long>(j) * ld + r;
-            if constexpr (sizeof(Acc) == sizeof(double)) {
-                xv = fma(rs[j], static_cast<double>(*zj), xv);
-            } else {
-                d = fma(static_cast<Acc>(rs[j]), static_cast<Acc>(*zj), d);
+        int j = 0;
+        for (; j + 8 <= nz; j += 8) {
+            T z[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) z[u] = Z[static_cast<long long>(j + u) * ld + r];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if constexpr (sizeof(Acc) == sizeof(double)) {
+                    xv = fma(srs[j + u], static_cast<double>(z[u]), xv);
+                } else {
+                    d = fma(static_cast<Acc>(srs[j + u]), static_cast<Acc>(z[u]), d);
+                }
             }
-            *zj = Sentinel<T>::value();
+        }
+        for (; j < nz; ++j) {
+            const T z = Z[static_cast<long long>(j) * ld + r];
+            if constexpr (sizeof(Acc) == sizeof(double)) {
+                xv = fma(srs[j], static_cast<double>(z), xv);
+            } else {
+                d = fma(static_cast<Acc>(srs[j]), static_cast<Acc>(z), d);
+            }
         }
         x[r] = xv + static_cast<double>(d);
+        for (j = 0; j < nz; ++j) Z[static_cast<long long>(j) * ld + r] = Sentinel<T>::value();
     }
 }
 

@@ -8,6 +8,7 @@
 #include "device_util.hpp"
 #include "ilu_kernels.cuh"
 #include "ilu_solver.hpp"
+#include "mlp_impl.hpp"
 
 namespace gb300 {
 
@@ -135,6 +136,13 @@ struct IluSolver::Impl {
     bool factorized = false;
     bool copy_back = true;       // copy the factors into GetMatrix()->value after Factorize
     bool shift_active = false;   // add `shift` to the diagonal in the next Factorize
+    // learned shift: MLP parameters on the device, the fused feature/inference pre-pass
+    bool model_active = false;
+    float min_shift = 0.f;
+    gb300::DeviceBuffer<float> mlp;
+    gb300::DeviceBuffer<int> depth_l;  // level depth of every row (MLP feature)
+    gb300::ShiftPrepass prepass;
+    bool shift_applied = false;        // the last Factorize used a (learned or explicit) shift
     int last_breakdowns = 0;
     int first_breakdown = -1;
     float last_factor_ms = 0.f;

@@ -257,7 +257,8 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
                 }
             }
         }
-        if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(acc / d));
+        // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
+        if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(sizeof(T) == 8 ? acc / d : acc * d));
         t = tn;
     }
 }
@@ -302,6 +303,17 @@ __global__ void pack_gather_kernel(long long count, const int* __restrict__ src,
          s += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int p = src[s];
         dst[s] = p >= 0 ? static_cast<T>(lu[p]) : T(0);
+    }
+}
+
+// FP32 diagonal of the upper factor stored as its reciprocal (computed in FP64, rounded
+// once): the mixed-precision backward sweep multiplies instead of dividing.
+static __global__ void pack_gather_recip_kernel(long long count, const int* __restrict__ src, const double* __restrict__ lu,
+                                         float* __restrict__ dst) {
+    for (long long s = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; s < count;
+         s += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int p = src[s];
+        dst[s] = p >= 0 ? static_cast<float>(1.0 / lu[p]) : 0.f;
     }
 }
 
@@ -382,7 +394,7 @@ __global__ void __launch_bounds__(kSolveThreads)
                     }
                 }
                 if (row >= 0) {
-                    if (UPPER) acc = acc / d;
+                    if (UPPER) acc = sizeof(T) == 8 ? acc / d : acc * d;
                     acc = Sentinel<T>::canon(acc);
                     xs[row - base] = acc;
                     st_relaxed(out + row, acc);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -17,6 +18,7 @@
 #include "device_util.hpp"
 #include "ilu_impl.hpp"
 #include "ilu_kernels.cuh"
+#include "mlp.cuh"
 
 namespace gb300 {
 
@@ -99,7 +101,7 @@ static void gather_level_pack(const LevelPack& P, bool lower, const double* lu, 
     if (!lower) {
         const long long nd = static_cast<long long>(P.ntask) * kWarp;
         pack_gather_kernel<double><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d64.get());
-        pack_gather_kernel<float><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
+        pack_gather_recip_kernel<<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
     }
     GB_CUDA_CHECK(cudaGetLastError());
 }
@@ -228,7 +230,7 @@ static void gather_pack(const TriPack& P, bool lower, const double* lu, cudaStre
     if (!lower && P.ntask > 0) {
         const long long nd = static_cast<long long>(P.ntask) * kWarp;
         pack_gather_kernel<double><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d64.get());
-        pack_gather_kernel<float><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
+        pack_gather_recip_kernel<<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
     }
     GB_CUDA_CHECK(cudaGetLastError());
 }
@@ -354,6 +356,9 @@ void IluSolver::SetupMatrix() {
     im.ci.upload(ci, static_cast<size_t>(im.nnz), s);
     im.diag.upload(im.an.diag.data(), static_cast<size_t>(n), s);
     im.order_l.upload(im.an.order_l.data(), static_cast<size_t>(n), s);
+    im.depth_l.upload(im.an.depth_l.data(), static_cast<size_t>(n), s);
+    im.shift.reserve(static_cast<size_t>(std::max(n, 1)));
+    im.prepass.ensure(im.dev.sms);
     im.lu.reserve(static_cast<size_t>(im.nnz));
     im.done.reserve(static_cast<size_t>(std::max(n, 1)));
     GB_CUDA_CHECK(cudaMemsetAsync(im.done.get(), 0, sizeof(int) * static_cast<size_t>(std::max(n, 1)), s));
@@ -398,46 +403,87 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
     Impl& im = *impl_;
     cudaStream_t s = im.stream;
     const int n = im.n;
-    if (im.nnz > 0)
-        GB_CUDA_CHECK(cudaMemcpyAsync(im.lu.get(), values, sizeof(double) * static_cast<size_t>(im.nnz),
-                                      on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-    int init[kStatusWords] = {0, 0, INT_MAX, 0};
-    GB_CUDA_CHECK(cudaMemcpyAsync(im.status.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
-    if (++im.stamp == INT_MAX) {
-        im.stamp = 1;
-        GB_CUDA_CHECK(cudaMemsetAsync(im.done.get(), 0, sizeof(int) * static_cast<size_t>(std::max(n, 1)), s));
-    }
-    GB_CUDA_CHECK(cudaEventRecord(im.ev0, s));
-    if (n > 0) {
-        ilu_factor_kernel<<<im.grid_fact, kFactWarps * kWarp, 0, s>>>(
-            n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(),
-            im.shift_active ? im.shift.get() : nullptr, im.done.get(), im.stamp, im.counters.get(), im.status.get());
-        GB_CUDA_CHECK(cudaGetLastError());
-        if (im.block_mode) {
-            gather_pack(im.LB, true, im.lu.get(), s, im.dev.sms);
-            gather_pack(im.UB, false, im.lu.get(), s, im.dev.sms);
-        } else {
-            gather_level_pack(im.L, true, im.lu.get(), s, im.dev.sms);
-            gather_level_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+    // One numeric factorisation of `values` with an optional diagonal shift; returns the
+    // status words.  With the learned model the shift comes from the fused pre-pass.
+    auto factor_once = [&](int shift_kind) {  // 0 none, 1 explicit, 2 learned
+        if (im.nnz > 0)
+            GB_CUDA_CHECK(cudaMemcpyAsync(im.lu.get(), values, sizeof(double) * static_cast<size_t>(im.nnz),
+                                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        int init[kStatusWords] = {0, 0, INT_MAX, 0};
+        GB_CUDA_CHECK(cudaMemcpyAsync(im.status.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+        if (++im.stamp == INT_MAX) {
+            im.stamp = 1;
+            GB_CUDA_CHECK(cudaMemsetAsync(im.done.get(), 0, sizeof(int) * static_cast<size_t>(std::max(n, 1)), s));
         }
-        im.launches += 7;
+        GB_CUDA_CHECK(cudaEventRecord(im.ev0, s));
+        if (n > 0) {
+            const double* shift = nullptr;
+            if (shift_kind == 2) {
+                im.prepass.run(s, im.dev.sms, n, im.rp.get(), im.ci.get(), im.lu.get(), im.diag.get(), im.depth_l.get(),
+                               im.an.nlev_l, im.mlp.get(), im.min_shift, im.shift.get(), nullptr, nullptr);
+                im.launches += 2;
+                shift = im.shift.get();
+            } else if (shift_kind == 1) {
+                shift = im.shift.get();
+            }
+            ilu_factor_kernel<<<im.grid_fact, kFactWarps * kWarp, 0, s>>>(
+                n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(), shift, im.done.get(),
+                im.stamp, im.counters.get(), im.status.get());
+            GB_CUDA_CHECK(cudaGetLastError());
+            if (im.block_mode) {
+                gather_pack(im.LB, true, im.lu.get(), s, im.dev.sms);
+                gather_pack(im.UB, false, im.lu.get(), s, im.dev.sms);
+            } else {
+                gather_level_pack(im.L, true, im.lu.get(), s, im.dev.sms);
+                gather_level_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+            }
+            im.launches += 7;
+        }
+        GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
+        std::array<int, kStatusWords> h{};
+        GB_CUDA_CHECK(cudaMemcpyAsync(h.data(), im.status.get(), sizeof(int) * kStatusWords, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_CHECK(cudaStreamSynchronize(s));
+        float ms = 0.f;
+        GB_CUDA_CHECK(cudaEventElapsedTime(&ms, im.ev0, im.ev1));
+        im.last_factor_ms += ms;
+        if (h[kStatusTimeout] != 0) {
+            im.factorized = false;
+            throw std::runtime_error("dependency wait timed out on the device");
+        }
+        return h;
+    };
+    im.last_factor_ms = 0.f;
+    const int kind = im.model_active ? 2 : (im.shift_active ? 1 : 0);
+    auto h = factor_once(kind);
+    im.shift_applied = kind != 0;
+    if (kind == 2 && h[kStatusBreakdowns] != 0) {
+        // learned shift met a zero / non-finite pivot: plain ILU is the fallback
+        h = factor_once(0);
+        im.shift_applied = false;
     }
-    GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
-    if (!on_device && im.copy_back && im.nnz > 0)
+    if (!on_device && im.copy_back && im.nnz > 0) {
         GB_CUDA_CHECK(cudaMemcpyAsync(aMatrix_.value, im.lu.get(), sizeof(double) * static_cast<size_t>(im.nnz),
                                       cudaMemcpyDeviceToHost, s));
-    int h[kStatusWords];
-    GB_CUDA_CHECK(cudaMemcpyAsync(h, im.status.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
-    GB_CUDA_CHECK(cudaStreamSynchronize(s));
-    GB_CUDA_CHECK(cudaEventElapsedTime(&im.last_factor_ms, im.ev0, im.ev1));
-    if (h[kStatusTimeout] != 0) {
-        im.factorized = false;
-        throw std::runtime_error("dependency wait timed out on the device");
+        GB_CUDA_CHECK(cudaStreamSynchronize(s));
     }
     im.last_breakdowns = h[kStatusBreakdowns];
     im.first_breakdown = h[kStatusBreakdowns] ? h[kStatusFirstBreakdown] : -1;
     im.factorized = true;
     return im.last_breakdowns == 0;
+}
+
+void IluSolver::SetShiftModel(const float* params, int nparams, float min_shift) {
+    Impl& im = *impl_ensure();
+    if (params == nullptr || nparams == 0) {
+        im.model_active = false;
+        return;
+    }
+    if (nparams != kMlpParams) throw std::runtime_error("shift model must have 369 parameters");
+    if (!im.stream) throw std::runtime_error("SetupMatrix() must be called first");
+    im.mlp.upload(params, static_cast<size_t>(kMlpParams), im.stream);
+    GB_CUDA_CHECK(cudaStreamSynchronize(im.stream));
+    im.min_shift = min_shift;
+    im.model_active = true;
 }
 
 void IluSolver::Substitute(const double* b, double* x) {

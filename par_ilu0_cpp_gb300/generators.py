@@ -275,12 +275,10 @@ def cdr2d(nx: int, seed: int, sigma: float = 1.5, max_peclet: float = 5.0, corr_
     pe = rng.uniform(0.0, max_peclet)
     ang = rng.uniform(0.0, 2.0 * np.pi)
     wdir = np.array([np.cos(ang), np.sin(ang)])
-    base = variable_poisson2d(nx, nx, sigma=sigma, corr_len=corr_len, seed=int(rng.integers(1 << 31)))
     # cell Peclet relative to a unit diffusion: |w| h / (2 D) = pe -> w h = 2 pe
     wind = 2.0 * pe * wdir
     a0 = variable_poisson2d(nx, nx, sigma=sigma, corr_len=corr_len, seed=int(rng.integers(1 << 31)),
                             wind=wind)
-    del base
     lam = _lambda_min_estimate(a0, seed=int(rng.integers(1 << 31)))
     s = rng.uniform(0.0, reaction_frac * max(lam, 0.0))
     vals = a0.values.copy()
