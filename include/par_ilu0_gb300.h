@@ -120,6 +120,30 @@ int LLJBASH_IluSolverGetAnalysis(IluSolverHdl hdl, int* diag, int* etree_lower, 
 int LLJBASH_Gb300AnalyzePattern(int n, const int* row_ptr, const int* col_idx, int* diag, int* etree_lower,
                                 int* etree_upper, int* depth_lower, int* depth_upper, int* nlevels /* [2] */);
 
+/* Batched persistent solver (no counterpart in the reference): nsys independent
+ * systems of uneven size, nrhs right-hand sides each, solved in ONE persistent kernel
+ * launch — ILU(0) with FP32 factors (optionally with the learned shift) and GMRES(restart)
+ * in FP32 cycles inside FP64 refinement to ||b - A x||_2 <= rtol ||b||_2 (FP64).
+ * row_ptr: the systems' row pointers one after the other (n[s] + 1 entries each);
+ * col_idx / values: their entries (columns local to each system).  rhs / x: for every
+ * system in order, nrhs vectors of n[s] doubles. */
+typedef void* LLJBASH_BatchHdl;
+LLJBASH_BatchHdl LLJBASH_BatchCreate(int nsys, const int* n, const int* row_ptr, const int* col_idx,
+                                     const double* values, int nrhs, int restart, double rtol, int maxit);
+/* As LLJBASH_BatchCreate, with separate values to factorise (same layout as values,
+ * e.g. A plus a diagonal shift); GMRES iterates on values. */
+LLJBASH_BatchHdl LLJBASH_BatchCreateEx(int nsys, const int* n, const int* row_ptr, const int* col_idx,
+                                       const double* values, const double* factor_values, int nrhs, int restart,
+                                       double rtol, int maxit);
+void LLJBASH_BatchDestroy(LLJBASH_BatchHdl hdl);
+int LLJBASH_BatchSetShiftModel(LLJBASH_BatchHdl hdl, const float* params, int nparams, double min_shift);
+/* Picks the launch shape (CTAs per SM, system order) by timing a sample of the batch. */
+int LLJBASH_BatchAutotune(LLJBASH_BatchHdl hdl, int* ctas_per_sm, int* largest_first);
+/* iters / resid / converged: nsys * nrhs entries (any may be NULL); *ms: device time of
+ * the launch. */
+int LLJBASH_BatchSolve(LLJBASH_BatchHdl hdl, const double* rhs, double* x, int* iters, double* resid, int* converged,
+                       double* ms);
+
 /* GMRES options. */
 enum {
     LLJBASH_GMRES_OPT_MODE = 1,        /* 0 plain FP64 (default), 1 FP32 cycles in FP64 refinement */

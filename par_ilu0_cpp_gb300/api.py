@@ -131,6 +131,14 @@ def load() -> ctypes.CDLL:
                                                     ctypes.POINTER(ctypes.c_double)]),
         "LLJBASH_ShiftTrainerGradient": (ctypes.c_int, [ctypes.c_void_p, _F, ctypes.POINTER(ctypes.c_double)]),
         "LLJBASH_ShiftTrainerPredict": (ctypes.c_int, [ctypes.c_void_p, _F]),
+        "LLJBASH_BatchCreate": (ctypes.c_void_p, [ctypes.c_int, _I, _I, _I, _D, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.c_double, ctypes.c_int]),
+        "LLJBASH_BatchCreateEx": (ctypes.c_void_p, [ctypes.c_int, _I, _I, _I, _D, _D, ctypes.c_int, ctypes.c_int,
+                                                    ctypes.c_double, ctypes.c_int]),
+        "LLJBASH_BatchDestroy": (None, [ctypes.c_void_p]),
+        "LLJBASH_BatchSetShiftModel": (ctypes.c_int, [ctypes.c_void_p, _F, ctypes.c_int, ctypes.c_double]),
+        "LLJBASH_BatchAutotune": (ctypes.c_int, [ctypes.c_void_p, _I, _I]),
+        "LLJBASH_BatchSolve": (ctypes.c_int, [ctypes.c_void_p, _D, _D, _I, _D, _I, ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):
@@ -503,3 +511,67 @@ class ShiftTrainer:
         if self.lib.LLJBASH_ShiftTrainerPredict(self.h, _fp(y)) != 0:
             raise RuntimeError(last_error())
         return y
+
+
+class BatchSolver:
+    """Batched persistent ILU(0) + GMRES over many systems x right-hand sides (one launch)."""
+
+    def __init__(self, systems, nrhs: int, restart: int = 30, rtol: float = 1e-8, maxit: int = 1000,
+                 factor_values=None):
+        """factor_values (optional): per system, the values to factorise (e.g. A plus a
+        diagonal shift); GMRES iterates on A."""
+        self.lib = load()
+        self.systems = systems
+        self.nrhs = nrhs
+        n = np.array([a.n for a in systems], dtype=np.int32)
+        rp = np.concatenate([a.row_ptr for a in systems]).astype(np.int32)
+        ci = np.concatenate([a.col_idx for a in systems]).astype(np.int32)
+        val = np.concatenate([a.values for a in systems]).astype(np.float64)
+        if factor_values is None:
+            self.h = self.lib.LLJBASH_BatchCreate(len(systems), _ip(n), _ip(rp), _ip(ci), _dp(val), int(nrhs),
+                                                  int(restart), float(rtol), int(maxit))
+        else:
+            fv = np.concatenate(factor_values).astype(np.float64)
+            self.h = self.lib.LLJBASH_BatchCreateEx(len(systems), _ip(n), _ip(rp), _ip(ci), _dp(val), _dp(fv),
+                                                    int(nrhs), int(restart), float(rtol), int(maxit))
+        if not self.h:
+            raise RuntimeError(last_error())
+        self.total = int(sum(a.n for a in systems)) * nrhs
+
+    def close(self):
+        if self.h:
+            self.lib.LLJBASH_BatchDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_shift_model(self, params, min_shift: float = 0.0):
+        p = np.ascontiguousarray(params, dtype=np.float32) if params is not None else None
+        rc = self.lib.LLJBASH_BatchSetShiftModel(self.h, _fp(p), int(p.size) if p is not None else 0, float(min_shift))
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def autotune(self):
+        c = ctypes.c_int(0)
+        lf = ctypes.c_int(0)
+        if self.lib.LLJBASH_BatchAutotune(self.h, ctypes.byref(c), ctypes.byref(lf)) != 0:
+            raise RuntimeError(last_error())
+        return int(c.value), bool(lf.value)
+
+    def solve(self, rhs):
+        """rhs: flat array (systems in order, nrhs vectors each).  Returns dict."""
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        assert b.size == self.total
+        x = np.empty_like(b)
+        k = len(self.systems) * self.nrhs
+        its = np.empty(k, dtype=np.int32)
+        res = np.empty(k)
+        conv = np.empty(k, dtype=np.int32)
+        ms = ctypes.c_double(0.0)
+        if self.lib.LLJBASH_BatchSolve(self.h, _dp(b), _dp(x), _ip(its), _dp(res), _ip(conv), ctypes.byref(ms)) != 0:
+            raise RuntimeError(last_error())
+        return dict(x=x, iterations=its, residual=res, converged=conv.astype(bool), ms=float(ms.value))

@@ -6,6 +6,7 @@
 #include <string>
 
 #include "analysis.hpp"
+#include "batched_impl.hpp"
 #include "gmres.hpp"
 #include "gmres_c.h"
 #include "gmres_impl.hpp"
@@ -234,6 +235,53 @@ int LLJBASH_ShiftTrainerGradient(LLJBASH_ShiftTrainerHdl tr, float* grad, double
 
 int LLJBASH_ShiftTrainerPredict(LLJBASH_ShiftTrainerHdl tr, float* y) {
     GB_TRY(static_cast<gb300::ShiftTrainer*>(tr)->predict(y));
+}
+
+LLJBASH_BatchHdl LLJBASH_BatchCreate(int nsys, const int* n, const int* row_ptr, const int* col_idx,
+                                     const double* values, int nrhs, int restart, double rtol, int maxit) {
+    try {
+        return new gb300::BatchSolver(nsys, n, row_ptr, col_idx, values, nrhs, restart, rtol, maxit);
+    } catch (const std::exception& e) {
+        fail(e);
+        return nullptr;
+    }
+}
+
+LLJBASH_BatchHdl LLJBASH_BatchCreateEx(int nsys, const int* n, const int* row_ptr, const int* col_idx,
+                                       const double* values, const double* factor_values, int nrhs, int restart,
+                                       double rtol, int maxit) {
+    try {
+        return new gb300::BatchSolver(nsys, n, row_ptr, col_idx, values, nrhs, restart, rtol, maxit, factor_values);
+    } catch (const std::exception& e) {
+        fail(e);
+        return nullptr;
+    }
+}
+
+void LLJBASH_BatchDestroy(LLJBASH_BatchHdl hdl) { delete static_cast<gb300::BatchSolver*>(hdl); }
+
+int LLJBASH_BatchSetShiftModel(LLJBASH_BatchHdl hdl, const float* params, int nparams, double min_shift) {
+    GB_TRY({
+        if (params && nparams != gb300::kMlpParams) throw std::runtime_error("shift model must have 369 parameters");
+        static_cast<gb300::BatchSolver*>(hdl)->set_model(params, static_cast<float>(min_shift));
+    });
+}
+
+int LLJBASH_BatchAutotune(LLJBASH_BatchHdl hdl, int* ctas_per_sm, int* largest_first) {
+    GB_TRY({
+        auto* b = static_cast<gb300::BatchSolver*>(hdl);
+        b->autotune();
+        if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm();
+        if (largest_first) *largest_first = b->largest_first() ? 1 : 0;
+    });
+}
+
+int LLJBASH_BatchSolve(LLJBASH_BatchHdl hdl, const double* rhs, double* x, int* iters, double* resid, int* converged,
+                       double* ms) {
+    GB_TRY({
+        const float t = static_cast<gb300::BatchSolver*>(hdl)->solve(rhs, x, iters, resid, converged);
+        if (ms) *ms = t;
+    });
 }
 
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {

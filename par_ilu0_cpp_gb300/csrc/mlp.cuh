@@ -83,7 +83,8 @@ __device__ __forceinline__ void make_features(double d, double offsum, double of
     const double md = mean_d > 0.0 ? mean_d : 1.0;
     x[0] = static_cast<float>(log(fmax(d, 1e-300) / md));
     x[1] = static_cast<float>(log(fmax(off2, 1e-300) / md));
-    x[2] = static_cast<float>(fmin(offsum > 0.0 ? d / offsum : static_cast<double>(kDominanceCap), kDominanceCap));
+    x[2] = static_cast<float>(
+        fmin(offsum > 0.0 ? d / offsum : static_cast<double>(kDominanceCap), static_cast<double>(kDominanceCap)));
     x[3] = static_cast<float>(depth) / static_cast<float>(nlev > 1 ? nlev - 1 : 1);
 }
 

@@ -130,21 +130,55 @@ def label_matrix(a: g.Csr, b, solver: Solver | None = None):
     return best[3].astype(np.float32), dict(alpha=best[1], beta=best[2], its=best[0][0], trials=trials)
 
 
-def build_dataset(specs, log=None):
+def combos():
+    return [(al, be) for al in ALPHAS for be in BETAS]
+
+
+def build_dataset(specs, log=None, chunk: int = 200):
+    """Features and labels for the matrices of `specs`.  The label search runs every
+    (matrix, shift-family member) pair as one system of the batched persistent solver
+    (GMRES iterates on A, the factorisation sees A + diag(shift)), `chunk` matrices per
+    launch."""
     Xs, Ys, recs = [], [], []
+    cmb = combos()
     t0 = time.time()
-    for k, (side, seed) in enumerate(specs):
-        a = g.cdr2d(side, seed=seed)
-        _, b = g.random_rhs(a, seed=seed + 1)
-        solver = Solver(a)
-        y, rec = label_matrix(a, b, solver)
-        X = api.shift_features(solver.f, solver.analysis["depth_l"], solver.nlev)
-        Xs.append(X)
-        Ys.append(y)
-        rec.update(side=side, seed=seed, plain_its=[t[2] for t in rec["trials"] if t[0] == 0.0 and t[1] == 0.0][0])
-        recs.append(rec)
-        if log and (k + 1) % 50 == 0:
-            log(f"labelled {k + 1}/{len(specs)} matrices in {time.time() - t0:.1f}s")
+    for c0 in range(0, len(specs), chunk):
+        part = specs[c0:c0 + chunk]
+        mats, rhs, fvals, systems, ys = [], [], [], [], []
+        for side, seed in part:
+            a = g.cdr2d(side, seed=seed)
+            _, b = g.random_rhs(a, seed=seed + 1)
+            mats.append(a)
+            rows = np.repeat(np.arange(a.n), np.diff(a.row_ptr))
+            isdiag = a.col_idx == rows
+            yk = []
+            for alpha, beta in cmb:
+                y, shift = family(a, alpha, beta)
+                fv = a.values.copy()
+                fv[isdiag] += shift[rows[isdiag]]
+                systems.append(a)
+                fvals.append(fv)
+                rhs.append(b)
+                yk.append(y)
+            ys.append(yk)
+        bs = api.BatchSolver(systems, nrhs=1, restart=RESTART, maxit=LABEL_MAXIT, factor_values=fvals)
+        out = bs.solve(np.concatenate(rhs))
+        bs.close()
+        for k, (side, seed) in enumerate(part):
+            a = mats[k]
+            its = []
+            for j in range(len(cmb)):
+                q = k * len(cmb) + j
+                its.append(int(out["iterations"][q]) if out["converged"][q] else LABEL_MAXIT + 1)
+            best = min(range(len(cmb)), key=lambda j: (its[j], float(np.mean(ys[k][j]))))
+            f, _ = api.iluk_symbolic(a, 0)
+            an = api.analyze_pattern(f)
+            Xs.append(api.shift_features(f, an["depth_l"], int(an["nlev"][0])))
+            Ys.append(ys[k][best].astype(np.float32))
+            recs.append(dict(side=side, seed=seed, alpha=cmb[best][0], beta=cmb[best][1], its=its[best],
+                             plain_its=its[0], trials=its))
+        if log:
+            log(f"labelled {min(c0 + chunk, len(specs))}/{len(specs)} matrices in {time.time() - t0:.1f}s")
     return np.concatenate(Xs), np.concatenate(Ys), recs
 
 
