@@ -180,6 +180,99 @@ def kernel_profile(gm, ilu, dev, a, f_nnz_l, f_nnz_u, tsize):
     return out, rep
 
 
+def batched_section(nsys: int, nrhs: int, learned, seed: int = 5):
+    """Batched configuration: nsys variable-coefficient 5-point systems (lognormal field
+    sigma 1, sides ~ U[32, 224]), nrhs right-hand sides each, x_true ~ U[-1, 1], ILU(0)
+    FP32 factors (+ learned shift) + GMRES(30) in one persistent launch, FP64 residuals to
+    1e-8 relative.  Returns the JSON section."""
+    from par_ilu0_cpp_gb300 import api
+    from par_ilu0_cpp_gb300 import generators as g
+
+    t0 = time.perf_counter()
+    systems = g.batched_systems(nsys, seed)
+    rhs, xt = [], []
+    for k, a in enumerate(systems):
+        x, b = g.random_rhs(a, seed=seed * 100000 + k, nrhs=nrhs)
+        xt.append(np.atleast_2d(x))
+        rhs.append(np.atleast_2d(b))
+    gen_s = time.perf_counter() - t0
+    bs = api.BatchSolver(systems, nrhs=nrhs, restart=30, rtol=RTOL, maxit=MAXIT)
+    if learned.get("params") is not None:
+        bs.set_shift_model(learned["params"], learned.get("min_shift", 0.0))
+    cps, lf = bs.autotune()
+    flat = np.concatenate([b.ravel() for b in rhs])
+    bs.solve(flat)  # warm-up
+    out = bs.solve(flat)
+    # FP64 true residuals and forward errors, recomputed on the host
+    worst, fwd, pos = 0.0, 0.0, 0
+    for k, a in enumerate(systems):
+        for r in range(nrhs):
+            xr = out["x"][pos:pos + a.n]
+            worst = max(worst, float(np.linalg.norm(rhs[k][r] - g.spmv(a, xr)) / np.linalg.norm(rhs[k][r])))
+            fwd = max(fwd, float(np.max(np.abs(xr - xt[k][r]))))
+            pos += a.n
+    unknowns = int(sum(a.n for a in systems)) * nrhs
+    # CPU reference algorithm (oracle port, plain FP64) on a sample of (system, rhs) pairs
+    import oracle
+
+    port = oracle.Port()
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(systems), size=min(8, len(systems)), replace=False)
+    t1 = time.perf_counter()
+    for k in pick:
+        a = systems[k]
+        lu, _ = port.factorize(a)
+        port.gmres(a, a, lu, rhs[k][0], RTOL * float(np.linalg.norm(rhs[k][0])), 30, MAXIT)
+    cpu_per_job = (time.perf_counter() - t1) / len(pick)
+    return {"workload": f"{nsys} variable-coefficient 5-pt systems (sides U[32,224], lognormal sigma 1) x {nrhs} RHS, "
+                        "ILU(0) FP32 + GMRES(30), FP64 refinement to rtol 1e-8, one persistent launch",
+            "systems": nsys, "rhs_per_system": nrhs, "unknowns": unknowns, "ms": round(out["ms"], 3),
+            "solves_per_s": round(nsys * nrhs / (out["ms"] * 1e-3), 1),
+            "converged_fraction": float(np.mean(out["converged"])), "max_rel_residual": worst,
+            "max_forward_error": fwd, "iterations_mean": float(np.mean(out["iterations"])),
+            "iterations_max": int(np.max(out["iterations"])), "autotune": {"ctas_per_sm": cps, "largest_first": lf},
+            "learned_shift": learned.get("params") is not None, "generation_s": round(gen_s, 2),
+            "cpu_baseline": {"value": round(1e3 * cpu_per_job * nsys * nrhs, 1), "unit": "ms", "cores": 1,
+                             "kind": "port", "sample": f"{len(pick)} (system, rhs) pairs, plain FP64 ILU(0)+GMRES(30), "
+                                                       "scaled to all pairs"}}
+
+
+def other_configs(api, g):
+    """Secondary configurations, one solve each (plain FP64 and mixed): the 2D 256^2
+    Laplacian with ILU(0)+GMRES(30) and the 64^3 27-point lognormal operator with
+    ILU(1) / ILU(2)+GMRES(30) (symbolic ILU(k) on the host included in its own timer)."""
+    out = {}
+    cases = [("laplace2d_256_ilu0", lambda: g.laplace2d(256), 0),
+             ("lognormal27_64_ilu1", lambda: g.lognormal27(64, seed=0), 1),
+             ("lognormal27_64_ilu2", lambda: g.lognormal27(64, seed=0), 2)]
+    for name, make, lof in cases:
+        a = make()
+        x_true, b = g.random_rhs(a, SEED)
+        t0 = time.perf_counter()
+        f, _ = api.iluk_symbolic(a, lof)
+        sym_ms = 1e3 * (time.perf_counter() - t0)
+        rec = {"n": a.n, "nnz": a.nnz, "nnz_factor": f.nnz, "symbolic_ms": round(sym_ms, 1)}
+        for mode, label in ((0, "plain"), (1, "mixed")):
+            ilu = api.IluSolver()
+            ilu.set_option(api.ILU_OPT_COPY_BACK, 0)
+            ilu.set_matrix(f)
+            ilu.setup()
+            gm = api.Gmres(RTOL * float(np.linalg.norm(b)), 30, MAXIT)
+            gm.set_preconditioner(ilu)
+            gm.set_option(api.GMRES_OPT_MODE, mode)
+            gm.set_option(api.GMRES_OPT_KEEP_MATRIX, 1)
+            for rep in range(2):
+                ilu.set_values(f.values)
+                t0 = time.perf_counter()
+                ilu.factorize()
+                res = gm.solve(a, b)
+                ms = 1e3 * (time.perf_counter() - t0)
+            rec[label] = {"ms": round(ms, 2), "iterations": res.iterations,
+                          "rel_residual": float(np.linalg.norm(b - g.spmv(a, res.x)) / np.linalg.norm(b))}
+        out[name] = rec
+    return out
+
+
 def cpu_baseline(a, b, tol, nthreads, full_iters_hint=None):
     """The reference's algorithm on the host cores (oracle port): factorisation (best of
     1 thread and all threads, as the reference's thread sweep) + one GMRES(50) restart
@@ -276,6 +369,20 @@ def run_ours(args):
 
     solvers = {"plain": make(0), "mixed": make(1)}
 
+    # Learned shift for the headline solver: the committed model's pre-pass runs in the
+    # factorisation; its decision rule (plain ILU when the shifted factors do not beat
+    # the plain iteration count on this matrix) is taken once, on the first warm-up
+    # solve, and kept for the timed solves.
+    learned = {"model": None, "applied": False}
+    model_path = os.path.join(ROOT, "par_ilu0_cpp_gb300", "shift_model.json")
+    if os.path.isfile(model_path):
+        from par_ilu0_cpp_gb300 import learned_shift as ls
+
+        params, meta = ls.load_model(model_path)
+        learned["model"] = os.path.relpath(model_path, ROOT)
+        learned["params"] = params
+        learned["min_shift"] = float(meta.get("min_shift", 0.0))
+
     def step(name):
         ilu, gm = solvers[name]
         dev["x"].zero_()
@@ -292,6 +399,16 @@ def run_ours(args):
             raise RuntimeError(f"{name} solve failed: rc={rc} ok={ok} its={its} {api.last_error()}")
         return e0.elapsed_time(e1), its
 
+    if learned["model"] is not None:
+        ilu_m = solvers["mixed"][0]
+        _, its_plain_f = step("mixed")
+        ilu_m.set_shift_model(learned["params"], learned["min_shift"])
+        _, its_learned = step("mixed")
+        applied = bool(ilu_m.info().shift_applied) and its_learned < its_plain_f
+        learned.update(iterations_with_shift=its_learned, iterations_plain_factors=its_plain_f, applied=applied,
+                       decision="learned shift kept" if applied else "plain ILU kept (shift did not beat plain)")
+        if not applied:
+            ilu_m.set_shift_model(None)
     for _ in range(args.warmup):
         step("plain")
         step("mixed")
@@ -338,6 +455,8 @@ def run_ours(args):
     gm_h = api.Gmres(tol, RESTART, MAXIT)
     gm_h.set_preconditioner(ilu_h)
     gm_h.set_option(api.GMRES_OPT_MODE, 1)
+    if learned.get("applied"):
+        ilu_h.set_shift_model(learned["params"], learned["min_shift"])
     for i in range(args.warmup + args.steps):
         ilu_h.set_values(f.values)  # the factors of the previous step were copied back in place
         torch.cuda.synchronize()
@@ -364,6 +483,14 @@ def run_ours(args):
         with open(tpath) as fh:
             traffic = json.load(fh).get(dom)
 
+    batched = None
+    others = None
+    if rank == 0 and not args.quick:
+        batched = batched_section(args.batch_systems, args.batch_rhs, learned)
+        from par_ilu0_cpp_gb300 import generators as gg
+
+        others = other_configs(api, gg)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(a, b, tol, os.cpu_count() or 1, full_iters_hint=its["plain"])
@@ -373,7 +500,8 @@ def run_ours(args):
             "metric": METRIC, "value": round(ms["mixed"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms["mixed"], 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 Krylov/ILU + f64 refinement", "data": "synthetic (seeded generator)",
-            "config": config_of(a, args.size, "mixed (FP32 cycles in FP64 refinement)"),
+            "config": config_of(a, args.size, "mixed (FP32 cycles in FP64 refinement) + learned shift policy"),
+            "learned_shift": {k: v for k, v in learned.items() if k != "params"},
             "plain_fp64_ms": round(ms["plain"], 3),
             "speedup_vs_plain": round(ms["plain"] / ms["mixed"], 3),
             "iterations": {"mixed": its["mixed"], "plain": its["plain"]},
@@ -388,6 +516,8 @@ def run_ours(args):
             "e2e": {"value": round(float(np.mean(e2e_ms)), 3), "unit": "ms", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "path": "LLJBASH_IluSolverFactorize + LLJBASH_GmresSolve"},
             "gpu_launches": int(launches1 - launches0),
+            "batched": batched,
+            "other_configs": others,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -403,6 +533,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true", help="skip the batched and secondary configurations")
+    ap.add_argument("--batch-systems", type=int, default=512)
+    ap.add_argument("--batch-rhs", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

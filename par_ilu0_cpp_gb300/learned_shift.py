@@ -103,6 +103,32 @@ class Solver:
         return out
 
 
+class PolicySolver(Solver):
+    """Learned shift with the per-matrix decision rule: the first solve runs the shifted
+    and the plain factors and keeps the one with fewer iterations (plain on ties, on
+    breakdown and on non-convergence); later solves of the same matrix reuse it."""
+
+    def __init__(self, a: g.Csr, params, min_shift: float = 0.0, **kw):
+        super().__init__(a, **kw)
+        self.params = params
+        self.min_shift = min_shift
+        self.use_shift = None
+        self.first = None
+
+    def solve_policy(self, b, maxit=None):
+        if self.use_shift is None:
+            learned = self.solve(b, model=self.params, min_shift=self.min_shift, maxit=maxit, fallback=False)
+            plain = self.solve(b, maxit=maxit)
+            self.use_shift = bool(learned["shift_applied"] and learned["converged"]
+                                  and learned["iterations"] < plain["iterations"])
+            self.first = dict(learned=learned["iterations"], plain=plain["iterations"],
+                              learned_converged=learned["converged"], plain_converged=plain["converged"])
+            return learned if self.use_shift else plain
+        if self.use_shift:
+            return self.solve(b, model=self.params, min_shift=self.min_shift, maxit=maxit)
+        return self.solve(b, maxit=maxit)
+
+
 def make_training_set(n_train: int, seed: int, lo: int = 32, hi: int = 128):
     rng = np.random.default_rng(seed)
     sides = rng.integers(lo, hi + 1, size=n_train)
