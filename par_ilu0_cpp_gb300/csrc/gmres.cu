@@ -151,7 +151,7 @@ void enqueue_piece(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Kry
     }
     L.run(kKSpmv, [&] {
         spmv_kernel<T, T, T><<<g.grid_spmv, kSpmvWarps * kWarp, 0, st>>>(n, g.rp_p, g.ci_p, ValueOf<T>::get(g), Zs, W,
-                                                                          gate, s);
+                                                                          gate, s, ilu ? K.y.get() : nullptr);
     });
     L.run(kKDot, [&] {
         cgs_dot_kernel<T><<<g.grid_blas, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.partial.get(), g.h1.get(),

@@ -127,12 +127,19 @@ __device__ __forceinline__ AT spmv_row_chunk(int n, const int* __restrict__ rp, 
     return acc;
 }
 
-// y = A x (gated when launched inside a cycle graph).
+// y = A x (gated when launched inside a cycle graph).  `reset` (optional) is set to the
+// sentinel on rows [0, n): the forward-sweep vector of the preconditioner, which must hold
+// the sentinel before the next forward substitution (done here, in a bandwidth-bound
+// kernel, instead of inside the latency-bound backward substitution).
 template <class AT, class XT, class YT>
 __global__ void __launch_bounds__(kSpmvWarps * kWarp)
     spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const AT* __restrict__ av,
-                const XT* __restrict__ x, YT* __restrict__ y, const int* gate, int step) {
+                const XT* __restrict__ x, YT* __restrict__ y, const int* gate, int step, YT* __restrict__ reset) {
     if (gate_closed(gate, step)) return;
+    if (reset) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            reset[i] = Sentinel<YT>::value();
+    }
     __shared__ int s_col[kSpmvWarps][kSpmvStage];
     __shared__ AT s_val[kSpmvWarps][kSpmvStage];
     const int w = threadIdx.x >> 5;

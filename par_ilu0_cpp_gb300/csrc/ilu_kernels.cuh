@@ -166,6 +166,81 @@ struct PackedTri {
     const T* dvals = nullptr;    // [32 * ntask] diagonal (upper factor only)
 };
 
+constexpr int kLaneEntries = 8;  // rows with at most this many entries use the per-lane path
+
+// Per-lane progressive solve of a warp's 32 rows (one per lane), for rows with at most
+// kLaneEntries entries held in registers (c: column or -1, v: value).  Every round a
+// lane issues the loads of all its pending dependencies at once, consumes the ready
+// prefix in entry order (the reference's accumulation order, so the operations are the
+// same as a sequential sweep) and publishes its row the moment its last entry is
+// consumed.  A row therefore never waits for the slowest row of its warp; the warp
+// leaves the loop when all 32 rows are published.  Rounds are bounded: past kSpinLimit
+// (or once another wait has given up) the status word is set and the loop ends.
+template <class T, bool UPPER>
+__device__ __forceinline__ void progressive_rows(int row, int K, const int (&c)[kLaneEntries],
+                                                 const T (&v)[kLaneEntries], T acc, T d, const T* dep, T* out,
+                                                 int* status) {
+    int k = 0;
+    bool done = row < 0;
+    long long rounds = 0;
+    while (!__all_sync(0xffffffffu, done)) {
+        if (!done) {
+            T xs[kLaneEntries];
+#pragma unroll
+            for (int u = 0; u < kLaneEntries; ++u)
+                xs[u] = (u >= k && u < K && c[u] >= 0) ? ld_relaxed(dep + c[u]) : T(0);
+#pragma unroll
+            for (int u = 0; u < kLaneEntries; ++u) {
+                if (k == u && u < K) {
+                    if (c[u] < 0) {
+                        ++k;
+                    } else if (!Sentinel<T>::is(xs[u])) {
+                        acc = fma(-v[u], xs[u], acc);
+                        ++k;
+                    }
+                }
+            }
+            if (k >= K) {
+                // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
+                const T r = UPPER ? (sizeof(T) == 8 ? acc / d : acc * d) : acc;
+                st_relaxed(out + row, Sentinel<T>::canon(r));
+                done = true;
+            }
+        }
+        if (++rounds >= kSpinLimit) {
+            if (!done) atomicExch(status + kStatusTimeout, 1);
+            break;
+        }
+        if ((rounds & 1023) == 0 && ld_relaxed_int(status + kStatusTimeout) != 0) break;
+    }
+}
+
+// Blocking solve of one row (any number of entries), the reference's entry order.
+template <class T>
+__device__ __forceinline__ T blocking_row(int off, int K, int lane, const int* cols, const T* vals, T acc, const T* dep,
+                                          int* status) {
+    for (int k0 = 0; k0 < K; k0 += 8) {
+        int c[8];
+        T v[8], x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int s = off + (k0 + u) * kWarp + lane;
+            c[u] = (k0 + u < K) ? cols[s] : -1;
+            v[u] = (k0 + u < K) ? vals[s] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = c[u] >= 0 ? ld_relaxed(dep + c[u]) : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (c[u] >= 0) {
+                if (Sentinel<T>::is(x[u])) x[u] = wait_value(dep + c[u], status);
+                acc = fma(-v[u], x[u], acc);
+            }
+        }
+    }
+    return acc;
+}
+
 // Forward substitution with the unit lower factor: y = L^{-1} (scale * b).
 // With `scale` non-null, b is rescaled on the fly and the rescaled value is written back
 // to b (GMRES uses this to normalise the new Krylov vector in the same pass).
@@ -186,38 +261,34 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
         T acc = T(0);
         if (row >= 0) {
             acc = b[row];
-            if (scale) {
-                acc = acc * sc;
-                b[row] = acc;
-            }
+            if (scale) acc = acc * sc;
         }
-        for (int k0 = 0; k0 < K; k0 += 8) {
-            int c[8];
-            T v[8], x[8];
+        const T acc0 = acc;
+        if (K <= kLaneEntries) {
+            int c[kLaneEntries];
+            T v[kLaneEntries];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int s = off + (k0 + u) * kWarp + lane;
-                c[u] = (k0 + u < K) ? L.cols[s] : -1;
-                v[u] = (k0 + u < K) ? L.vals[s] : T(0);
+            for (int u = 0; u < kLaneEntries; ++u) {
+                const int s = off + u * kWarp + lane;
+                c[u] = (u < K) ? L.cols[s] : -1;
+                v[u] = (u < K) ? L.vals[s] : T(0);
             }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) x[u] = c[u] >= 0 ? ld_relaxed(y + c[u]) : T(0);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (c[u] >= 0) {
-                    if (Sentinel<T>::is(x[u])) x[u] = wait_value(y + c[u], status);
-                    acc = fma(-v[u], x[u], acc);
-                }
-            }
+            progressive_rows<T, false>(row, K, c, v, acc, T(1), y, y, status);
+        } else {
+            acc = blocking_row(off, K, lane, L.cols, L.vals, acc, y, status);
+            if (row >= 0) st_relaxed(y + row, Sentinel<T>::canon(acc));
         }
-        if (row >= 0) st_relaxed(y + row, Sentinel<T>::canon(acc));
+        // the normalised Krylov vector is written back after the row is published: a
+        // plain store ahead of the waits would delay them
+        if (scale && row >= 0) b[row] = acc0;
         t = tn;
     }
 }
 
-// Backward substitution with the upper factor: x = U^{-1} y.  Reads y[row] once, resets
-// it to the sentinel (so y is ready for the next forward sweep), waits on x values of
-// the rows it depends on.  x must hold the sentinel everywhere on entry.
+// Backward substitution with the upper factor: x = U^{-1} y, waiting on x values of the
+// rows it depends on.  x must hold the sentinel everywhere on entry.  y is left as it
+// is (the caller resets it to the sentinel before the next forward sweep, off the
+// dependency chain: a store into y here doubles this kernel's time).
 template <class T>
 __global__ void __launch_bounds__(kSolveWarps * kWarp)
     sptrsv_upper_kernel(PackedTri<T> U, T* y, T* x, unsigned* counter, int* status, const int* gate, int step) {
@@ -233,32 +304,21 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
         // the diagonal is loaded before the dependency waits: the waits are ordered
         // memory operations, so a load after them would add a full round trip per level
         const T d = U.dvals[q];
-        T acc = T(0);
-        if (row >= 0) {
-            acc = y[row];
-            y[row] = Sentinel<T>::value();
-        }
-        for (int k0 = 0; k0 < K; k0 += 8) {
-            int c[8];
-            T v[8], xv[8];
+        const T acc = row >= 0 ? y[row] : T(0);
+        if (K <= kLaneEntries) {
+            int c[kLaneEntries];
+            T v[kLaneEntries];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int s = off + (k0 + u) * kWarp + lane;
-                c[u] = (k0 + u < K) ? U.cols[s] : -1;
-                v[u] = (k0 + u < K) ? U.vals[s] : T(0);
+            for (int u = 0; u < kLaneEntries; ++u) {
+                const int s = off + u * kWarp + lane;
+                c[u] = (u < K) ? U.cols[s] : -1;
+                v[u] = (u < K) ? U.vals[s] : T(0);
             }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) xv[u] = c[u] >= 0 ? ld_relaxed(x + c[u]) : T(0);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (c[u] >= 0) {
-                    if (Sentinel<T>::is(xv[u])) xv[u] = wait_value(x + c[u], status);
-                    acc = fma(-v[u], xv[u], acc);
-                }
-            }
+            progressive_rows<T, true>(row, K, c, v, acc, d, x, x, status);
+        } else {
+            const T r = blocking_row(off, K, lane, U.cols, U.vals, acc, x, status);
+            if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(sizeof(T) == 8 ? r / d : r * d));
         }
-        // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
-        if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(sizeof(T) == 8 ? acc / d : acc * d));
         t = tn;
     }
 }
@@ -334,8 +394,7 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
 
 // Forward (UPPER = false): out = L^{-1} (scale * in); with `scale`, in is rescaled in
 //   place (GMRES normalises its new Krylov vector in the same pass).
-// Backward (UPPER = true): out = U^{-1} in; in[row] is reset to the sentinel after it is
-//   read (ready for the next forward sweep).
+// Backward (UPPER = true): out = U^{-1} in (in is left as it is).
 // out must hold the sentinel for every row on entry.
 template <class T, bool UPPER>
 __global__ void __launch_bounds__(kSolveThreads)
@@ -365,9 +424,7 @@ __global__ void __launch_bounds__(kSolveThreads)
                 T acc = T(0);
                 if (row >= 0) {
                     acc = in[row];
-                    if (UPPER) {
-                        in[row] = Sentinel<T>::value();
-                    } else if (scale) {
+                    if (!UPPER && scale) {
                         acc = acc * sc;
                         in[row] = acc;
                     }

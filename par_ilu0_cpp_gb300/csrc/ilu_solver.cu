@@ -494,6 +494,7 @@ void IluSolver::Substitute(const double* b, double* x) {
     if (n == 0) return;
     GB_CUDA_CHECK(cudaMemcpyAsync(im.sb64.get(), b, sizeof(double) * static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
     fill_sentinel(im.sx64.get(), n, s, im.dev.sms);
+    fill_sentinel(im.sy64.get(), n, s, im.dev.sms);
     im.launch_lower<double>(s, im.sb64.get(), nullptr, im.sy64.get(), nullptr, 0);
     im.launch_upper<double>(s, im.sy64.get(), im.sx64.get(), nullptr, 0);
     GB_CUDA_CHECK(cudaGetLastError());
