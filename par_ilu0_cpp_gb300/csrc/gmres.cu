@@ -47,7 +47,7 @@ PreconditionedGmres::~PreconditionedGmres() {
 
 namespace {
 
-constexpr long long kLdAlign = 256;
+constexpr long long kLdAlign = 512;  // whole CGS chunks of 512 rows
 
 template <class T>
 void ensure_krylov(Krylov<T>& K, int n, int im, cudaStream_t s, int sms) {

@@ -8,7 +8,7 @@
 // (or closes the cycle); later kernels of the graph check the gate and return at once.
 //
 // Vector layout: Krylov bases V[0..m] and Z[0..m-1] are column blocks of one allocation
-// with leading dimension ld = n rounded up to 256 entries; the padding entries of V are
+// with leading dimension ld = n rounded up to 512 entries; the padding entries of V are
 // zero and never written with anything else, so whole chunks can be processed without
 // bounds checks.  Basis type T is double (plain path) or float (mixed-precision inner
 // cycles); every reduction (dot products, norms) accumulates in double, and the
@@ -220,93 +220,94 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
 //   axpy_dot:    w <- w - V h1;  h2 = V^T w
 //   axpy_norm:   w <- w - V h2;  ||w||; then (last block) H(:,s) = h1 + h2,
 //                H(s+1,s) = ||w||, Givens update and loop control.
-// Work split: each warp owns chunks of R = 32 * RPL consecutive rows.  The updates are
-// row-parallel (lane = rows); the dot products are vector-parallel (lane = basis
-// vector j, summing the chunk sequentially against the chunk of w staged in shared
-// memory), which costs exactly one multiply-add per element and needs no per-chunk
-// reductions — this matters on GB300, whose FP64 rate is far below its bandwidth.
-// For float bases the chunk sums are formed in float and added in double per chunk.
+// Work split: each warp owns chunks of R = 32 * RPL consecutive rows, lane l the RPL
+// contiguous rows [l RPL, (l+1) RPL) of a chunk, so every load of a basis vector is one
+// fully coalesced 1-2 KB access per warp.  The chunk of w stays in registers; for each
+// basis vector the lane's RPL products are summed in registers and reduced across the
+// warp once per chunk (one shuffle tree per 256/512 rows — cheap even with GB300's slow
+// FP64 pipe), and lane 0 adds the warp's sum into a per-warp shared-memory row.  FP32
+// bases form the chunk sums in FP32 and accumulate them in FP64.
 // ---------------------------------------------------------------------------------
 template <class T>
 struct ChunkCfg;
 template <>
 struct ChunkCfg<double> {
-    static constexpr int RPL = 2;
+    static constexpr int RPL = 16;
     using Acc = double;
 };
 template <>
 struct ChunkCfg<float> {
-    static constexpr int RPL = 4;
+    static constexpr int RPL = 8;
     using Acc = float;
 };
 
 template <class T>
 __device__ __forceinline__ void load_rpl(const T* p, T (&v)[ChunkCfg<T>::RPL]);
 template <>
-__device__ __forceinline__ void load_rpl<double>(const double* p, double (&v)[2]) {
-    const double2 t = *reinterpret_cast<const double2*>(p);
-    v[0] = t.x;
-    v[1] = t.y;
+__device__ __forceinline__ void load_rpl<double>(const double* p, double (&v)[16]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const double2 t = reinterpret_cast<const double2*>(p)[k];
+        v[2 * k] = t.x;
+        v[2 * k + 1] = t.y;
+    }
 }
 template <>
-__device__ __forceinline__ void load_rpl<float>(const float* p, float (&v)[4]) {
-    const float4 t = *reinterpret_cast<const float4*>(p);
-    v[0] = t.x;
-    v[1] = t.y;
-    v[2] = t.z;
-    v[3] = t.w;
+__device__ __forceinline__ void load_rpl<float>(const float* p, float (&v)[8]) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float4 t = reinterpret_cast<const float4*>(p)[k];
+        v[4 * k] = t.x;
+        v[4 * k + 1] = t.y;
+        v[4 * k + 2] = t.z;
+        v[4 * k + 3] = t.w;
+    }
 }
 template <class T>
 __device__ __forceinline__ void store_rpl(T* p, const T (&v)[ChunkCfg<T>::RPL]);
 template <>
-__device__ __forceinline__ void store_rpl<double>(double* p, const double (&v)[2]) {
-    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+__device__ __forceinline__ void store_rpl<double>(double* p, const double (&v)[16]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) reinterpret_cast<double2*>(p)[k] = make_double2(v[2 * k], v[2 * k + 1]);
 }
 template <>
-__device__ __forceinline__ void store_rpl<float>(float* p, const float (&v)[4]) {
-    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+__device__ __forceinline__ void store_rpl<float>(float* p, const float (&v)[8]) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+        reinterpret_cast<float4*>(p)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
 }
 
-constexpr int kMaxJPerLane = (kMaxKrylov + 1 + kWarp - 1) / kWarp;
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_any(double v) { return warp_sum(v); }
+__device__ __forceinline__ float warp_sum_any(float v) { return warp_sum_f(v); }
 
-// Accumulates, for the lanes' basis vectors j = lane + 32 k (< nv), the dot product of
-// V[j][r0 : r0 + R) with the chunk of w staged in sw[0 : R).
+// Adds, for j < nv, the dot product of V[j] with the lane's chunk of w (wv, registers) to
+// the warp's shared-memory row acc_row[j] (lane 0 writes).  r0: the lane's first row.
 template <class T>
-__device__ __forceinline__ void chunk_dots(const T* __restrict__ V, long long ld, int nv, long long r0, const T* sw,
-                                           double (&acc)[kMaxJPerLane]) {
-    constexpr int R = kWarp * ChunkCfg<T>::RPL;
+__device__ __forceinline__ void chunk_dots_rows(const T* __restrict__ V, long long ld, int nv, long long r0,
+                                                const typename ChunkCfg<T>::Acc (&wv)[ChunkCfg<T>::RPL],
+                                                double* acc_row) {
     using Acc = typename ChunkCfg<T>::Acc;
+    constexpr int RPL = ChunkCfg<T>::RPL;
     const int lane = threadIdx.x & 31;
+#pragma unroll 2
+    for (int j = 0; j < nv; ++j) {
+        T v[RPL];
+        load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
+        Acc p = Acc(0);
 #pragma unroll
-    for (int k = 0; k < kMaxJPerLane; ++k) {
-        const int j = lane + k * kWarp;
-        if (k * kWarp >= nv) break;
-        if (j < nv) {
-            const T* v = V + static_cast<long long>(j) * ld + r0;
-            Acc s = Acc(0);
-#pragma unroll 4
-            for (int r = 0; r < R; r += ChunkCfg<T>::RPL) {
-                T a[ChunkCfg<T>::RPL];
-                load_rpl<T>(v + r, a);
-#pragma unroll
-                for (int u = 0; u < ChunkCfg<T>::RPL; ++u) s = fma(static_cast<Acc>(a[u]), static_cast<Acc>(sw[r + u]), s);
-            }
-            acc[k] += static_cast<double>(s);
-        }
+        for (int u = 0; u < RPL; ++u) p = fma(static_cast<Acc>(v[u]), wv[u], p);
+        p = warp_sum_any(p);
+        if (lane == 0) acc_row[j] += static_cast<double>(p);
     }
 }
 
-// Writes each warp's per-j sums to shared memory, sums the warps, stores the block
-// partials.  acc_s is [kBlasWarps][kMaxKrylov + 1].
-__device__ __forceinline__ void block_dots_to_partial(double (*acc_s)[kMaxKrylov + 1], const double (&acc)[kMaxJPerLane],
-                                                      int nv, double* partial) {
-    const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < kMaxJPerLane; ++k) {
-        const int j = lane + k * kWarp;
-        if (j < nv) acc_s[w][j] = acc[k];
-    }
+// Sums the per-warp rows acc_s[w][j] over warps into the block partials (all threads).
+__device__ __forceinline__ void warp_rows_to_partial(double (*acc_s)[kMaxKrylov + 1], int nv, double* partial) {
     __syncthreads();
     for (int j = threadIdx.x; j < nv; j += blockDim.x) {
         double s = 0.0;
@@ -315,32 +316,37 @@ __device__ __forceinline__ void block_dots_to_partial(double (*acc_s)[kMaxKrylov
     }
 }
 
+__device__ __forceinline__ void zero_warp_rows(double (*acc_s)[kMaxKrylov + 1], int nv) {
+    for (int e = threadIdx.x; e < kBlasWarps * (kMaxKrylov + 1); e += blockDim.x) (&acc_s[0][0])[e] = 0.0;
+    __syncthreads();
+    (void)nv;
+}
+
 template <class T>
 __global__ void __launch_bounds__(kBlasThreads)
     cgs_dot_kernel(long long nchunks, long long ld, const T* __restrict__ V, int s, double* partial, double* h1,
                    unsigned* counter, const int* gate) {
     if (gate_closed(gate, s)) return;
-    constexpr int R = kWarp * ChunkCfg<T>::RPL;
+    using Acc = typename ChunkCfg<T>::Acc;
+    constexpr int RPL = ChunkCfg<T>::RPL;
+    constexpr int R = kWarp * RPL;
     __shared__ double acc_s[kBlasWarps][kMaxKrylov + 1];
-    __shared__ __align__(16) T sw[kBlasWarps][R];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int nv = s + 1;
-    const T* wv = V + static_cast<long long>(s + 1) * ld;
-    double acc[kMaxJPerLane];
-#pragma unroll
-    for (int k = 0; k < kMaxJPerLane; ++k) acc[k] = 0.0;
+    zero_warp_rows(acc_s, nv);
+    const T* wvec = V + static_cast<long long>(s + 1) * ld;
     for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
          c += static_cast<long long>(gridDim.x) * kBlasWarps) {
-        const long long r0 = c * R;
-        T a[ChunkCfg<T>::RPL];
-        load_rpl<T>(wv + r0 + lane * ChunkCfg<T>::RPL, a);
-        store_rpl<T>(&sw[w][lane * ChunkCfg<T>::RPL], a);
-        __syncwarp();
-        chunk_dots<T>(V, ld, nv, r0, sw[w], acc);
-        __syncwarp();
+        const long long r0 = c * R + lane * RPL;
+        T a[RPL];
+        load_rpl<T>(wvec + r0, a);
+        Acc wv[RPL];
+#pragma unroll
+        for (int u = 0; u < RPL; ++u) wv[u] = static_cast<Acc>(a[u]);
+        chunk_dots_rows<T>(V, ld, nv, r0, wv, acc_s[w]);
     }
-    block_dots_to_partial(acc_s, acc, nv, partial);
+    warp_rows_to_partial(acc_s, nv, partial);
     if (!arrive_last(counter)) return;
     reduce_partials(partial, gridDim.x, nv, h1);
 }
@@ -350,27 +356,23 @@ __global__ void __launch_bounds__(kBlasThreads)
     cgs_axpy_dot_kernel(long long nchunks, long long ld, T* __restrict__ V, int s, const double* __restrict__ h1,
                         double* partial, double* h2, unsigned* counter, const int* gate) {
     if (gate_closed(gate, s)) return;
+    using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     constexpr int R = kWarp * RPL;
     __shared__ double acc_s[kBlasWarps][kMaxKrylov + 1];
-    __shared__ __align__(16) T sw[kBlasWarps][R];
     __shared__ double sh[kMaxKrylov + 1];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int nv = s + 1;
     for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = __ldcg(h1 + j);
-    __syncthreads();
-    T* wv = V + static_cast<long long>(s + 1) * ld;
-    double acc[kMaxJPerLane];
-#pragma unroll
-    for (int k = 0; k < kMaxJPerLane; ++k) acc[k] = 0.0;
+    zero_warp_rows(acc_s, nv);
+    T* wvec = V + static_cast<long long>(s + 1) * ld;
     for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
          c += static_cast<long long>(gridDim.x) * kBlasWarps) {
         const long long r0 = c * R + lane * RPL;
-        using Acc = typename ChunkCfg<T>::Acc;
         T a[RPL];
         Acc x[RPL];
-        load_rpl<T>(wv + r0, a);
+        load_rpl<T>(wvec + r0, a);
 #pragma unroll
         for (int u = 0; u < RPL; ++u) x[u] = static_cast<Acc>(a[u]);
         for (int j = 0; j < nv; ++j) {
@@ -381,14 +383,14 @@ __global__ void __launch_bounds__(kBlasThreads)
             for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
         }
 #pragma unroll
-        for (int u = 0; u < RPL; ++u) a[u] = static_cast<T>(x[u]);
-        store_rpl<T>(wv + r0, a);
-        store_rpl<T>(&sw[w][lane * RPL], a);
-        __syncwarp();
-        chunk_dots<T>(V, ld, nv, c * R, sw[w], acc);
-        __syncwarp();
+        for (int u = 0; u < RPL; ++u) {
+            a[u] = static_cast<T>(x[u]);
+            x[u] = static_cast<Acc>(a[u]);  // the dots use the stored (rounded) values
+        }
+        store_rpl<T>(wvec + r0, a);
+        chunk_dots_rows<T>(V, ld, nv, r0, x, acc_s[w]);
     }
-    block_dots_to_partial(acc_s, acc, nv, partial);
+    warp_rows_to_partial(acc_s, nv, partial);
     if (!arrive_last(counter)) return;
     reduce_partials(partial, gridDim.x, nv, h2);
 }
