@@ -53,8 +53,12 @@ enum {
     /* 1 (default): copy the factors into GetMatrix()->value after Factorize, as the
      * reference's in-place factorisation leaves them; 0: keep them on the device only. */
     LLJBASH_ILU_OPT_COPY_BACK = 1,
-    /* rows per substitution block (each CTA keeps one block's solution in shared memory);
-     * 0 = automatic.  Takes effect at the next IluSolverSetup. */
+    /* substitution schedule, taking effect at the next IluSolverSetup:
+     *   > 0: contiguous blocks of that many rows, block-pipelined kernel (each CTA keeps a
+     *        block's solution in shared memory and streams its levels in by bulk copies);
+     *        a value type (FP64 / FP32) whose block does not fit keeps the level kernel;
+     *   0:   automatic (the level-ordered sync-free kernel);
+     *   -1:  the level-ordered sync-free kernel. */
     LLJBASH_ILU_OPT_BLOCK_ROWS = 2
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);

@@ -137,7 +137,7 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 s->impl()->copy_back = value != 0.0;
                 return 0;
             case LLJBASH_ILU_OPT_BLOCK_ROWS:
-                if (value < 0 || value > 28000) throw std::runtime_error("block rows must be in [0, 28000]");
+                if (value < -1 || value > 1e8) throw std::runtime_error("block rows must be -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);
                 return 0;
             default:

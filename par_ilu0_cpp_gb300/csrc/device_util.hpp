@@ -49,12 +49,14 @@ private:
 struct DeviceInfo {
     int device = 0;
     int sms = 0;
+    int smem_optin = 0;  // largest dynamic + static shared memory of one CTA (bytes)
 };
 
 inline DeviceInfo current_device() {
     DeviceInfo d;
     GB_CUDA_CHECK(cudaGetDevice(&d.device));
     GB_CUDA_CHECK(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, d.device));
+    GB_CUDA_CHECK(cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, d.device));
     return d;
 }
 

@@ -189,16 +189,14 @@ void run_cycle(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Krylov<
         g.launches += L.count;
         return;
     }
-    const void* key[6] = {K.V.get(),
-                          ilu ? (ilu->block_mode ? static_cast<const void*>(ilu->LB.codes.get())
-                                                 : static_cast<const void*>(ilu->L.cols.get()))
-                              : nullptr,
-                          ilu ? (ilu->block_mode ? static_cast<const void*>(ilu->UB.v64.get())
-                                                 : static_cast<const void*>(ilu->U.v64.get()))
-                              : nullptr,
-                          ValueOf<T>::get(g), g.x_p, g.b_p};
+    const void* key[kGraphKey] = {K.V.get(),
+                                  ilu ? ilu->subst_key<T>() : nullptr,
+                                  ilu ? reinterpret_cast<const void*>(static_cast<uintptr_t>(ilu->setup_gen)) : nullptr,
+                                  ValueOf<T>::get(g),
+                                  g.x_p,
+                                  g.b_p};
     bool same = K.graph != nullptr;
-    for (int k = 0; k < 6 && same; ++k) same = key[k] == K.graph_key[k];
+    for (int k = 0; k < kGraphKey && same; ++k) same = key[k] == K.graph_key[k];
     if (!same) {
         if (K.graph) {
             cudaGraphExecDestroy(K.graph);
@@ -210,7 +208,7 @@ void run_cycle(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Krylov<
         GB_CUDA_CHECK(cudaStreamEndCapture(g.stream, &graph));
         GB_CUDA_CHECK(cudaGraphInstantiate(&K.graph, graph, 0));
         cudaGraphDestroy(graph);
-        for (int k = 0; k < 6; ++k) K.graph_key[k] = key[k];
+        for (int k = 0; k < kGraphKey; ++k) K.graph_key[k] = key[k];
         K.graph_nodes = L.count;
     }
     GB_CUDA_CHECK(cudaGraphLaunch(K.graph, g.stream));

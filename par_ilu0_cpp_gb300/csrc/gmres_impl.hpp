@@ -34,6 +34,10 @@ struct SolveReport {
     double solve_ms = 0;  // device time of the solve (events around the cycles)
 };
 
+// Identity of a captured cycle graph: the basis, the preconditioner's substitution data,
+// its setup generation, the matrix values and the solution / right-hand side.
+constexpr int kGraphKey = 6;
+
 // The per-precision Krylov workspace and its captured cycle graph.
 template <class T>
 struct Krylov {
@@ -42,7 +46,7 @@ struct Krylov {
     int im = 0;
     int n = 0;
     cudaGraphExec_t graph = nullptr;
-    const void* graph_key[6] = {};
+    const void* graph_key[kGraphKey] = {};
     long long graph_nodes = 0;
     ~Krylov() {
         if (graph) cudaGraphExecDestroy(graph);

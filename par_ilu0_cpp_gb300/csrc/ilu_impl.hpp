@@ -50,53 +50,40 @@ inline PackedTri<float> LevelPack::view<float>() const {
     return p;
 }
 
-// One packed triangular factor in the block-pipelined layout (see BlockTri): schedule
-// arrays plus packed values in FP64 and FP32.
-struct TriPack {
+// One packed triangular factor in the block-pipelined layout (see BandTri) for one
+// value type: the row partition, the slices and their gather instructions.
+struct BandPack {
+    int elem = 0;         // sizeof(T)
     int nblk = 0;
-    int block_rows = 0;  // S, rows per block (the last block may be shorter)
-    int ntask = 0;
-    int levels = 0;      // block-internal levels summed over blocks
-    long long slots = 0;
-    size_t smem64 = 0, smem32 = 0;  // dynamic shared memory of the FP64 / FP32 kernels
-    DeviceBuffer<int> blk_row, blk_lvl, lvl_task, rows, off, len, codes, src, dsrc;
-    DeviceBuffer<double> v64, d64;
-    DeviceBuffer<float> v32, d32;
+    int block_rows = 0;   // rows per block (the last block may be shorter)
+    int levels = 0;       // block-internal levels summed over blocks
+    int max_levels = 0;   // largest block-internal level count
+    int stages = 0;
+    unsigned stage_bytes = 0, xs_bytes = 0;
+    size_t smem = 0;      // dynamic shared memory of the kernel
+    long long bytes = 0;  // slice data
+    int threads = 0;      // CTA size
+    int grid = 0;         // resident CTAs at that footprint
+    DeviceBuffer<int> blk_row, blk_lvl, lvl_bytes, src;
+    DeviceBuffer<long long> blk_off;
+    DeviceBuffer<SliceGather> gat;
+    DeviceBuffer<unsigned char> data;
 
     template <class T>
-    BlockTri<T> view() const;
+    BandTri<T> view() const {
+        BandTri<T> p;
+        p.nblk = nblk;
+        p.stages = stages;
+        p.stage_bytes = stage_bytes;
+        p.xs_bytes = xs_bytes;
+        p.blk_row = blk_row.get();
+        p.blk_lvl = blk_lvl.get();
+        p.blk_off = blk_off.get();
+        p.lvl_bytes = lvl_bytes.get();
+        p.data = data.get();
+        return p;
+    }
 };
-
-template <>
-inline BlockTri<double> TriPack::view<double>() const {
-    BlockTri<double> p;
-    p.nblk = nblk;
-    p.blk_row = blk_row.get();
-    p.blk_lvl = blk_lvl.get();
-    p.lvl_task = lvl_task.get();
-    p.rows = rows.get();
-    p.off = off.get();
-    p.len = len.get();
-    p.codes = codes.get();
-    p.vals = v64.get();
-    p.dvals = d64.get();
-    return p;
-}
-template <>
-inline BlockTri<float> TriPack::view<float>() const {
-    BlockTri<float> p;
-    p.nblk = nblk;
-    p.blk_row = blk_row.get();
-    p.blk_lvl = blk_lvl.get();
-    p.lvl_task = lvl_task.get();
-    p.rows = rows.get();
-    p.off = off.get();
-    p.len = len.get();
-    p.codes = codes.get();
-    p.vals = v32.get();
-    p.dvals = d32.get();
-    return p;
-}
 
 // Host-side results of the pattern analysis (integer output identical to the
 // reference's; see analysis.hpp).
@@ -127,8 +114,11 @@ struct IluSolver::Impl {
     gb300::DeviceBuffer<unsigned> counters;  // ticket counters [0] fact, [1] L, [2] U
     gb300::DeviceBuffer<int> status;         // StatusWord array
     gb300::LevelPack L, U;     // level-ordered warp layout (default)
-    gb300::TriPack LB, UB;     // block-pipelined layout (block_rows > 0)
-    bool block_mode = false;
+    // block-pipelined layout, per value type (used when band64 / band32 is set)
+    gb300::BandPack LB64, UB64, LB32, UB32;
+    bool band64 = false, band32 = false;
+    bool level_packs = false;  // L and U (level-ordered warp layout) are built
+    unsigned setup_gen = 0;    // incremented by every SetupMatrix
     gb300::DeviceBuffer<double> sb64, sy64, sx64;  // Substitute() work vectors
     gb300::DeviceBuffer<float> sy32;               // FP32 forward-sweep intermediate
 
@@ -147,8 +137,8 @@ struct IluSolver::Impl {
     int first_breakdown = -1;
     float last_factor_ms = 0.f;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    int grid_fact = 0, grid_solve = 0, grid_block64 = 0, grid_block32 = 0;
-    int block_rows = 0;  // rows per substitution block (0 = automatic)
+    int grid_fact = 0, grid_solve = 0;
+    int block_rows = 0;  // rows per substitution block (0 = automatic, < 0 = level-ordered kernel)
     long long launches = 0;  // kernels launched by Factorize / Substitute
 
     ~Impl();
@@ -160,6 +150,9 @@ struct IluSolver::Impl {
     void launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const;
     template <class T>
     void launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const;
+    // Identifies the device data the substitution launches of type T read (CUDA graph key).
+    template <class T>
+    const void* subst_key() const;
     // Throws when a dependency wait timed out since the last call.
     void check_status(cudaStream_t s);
 };

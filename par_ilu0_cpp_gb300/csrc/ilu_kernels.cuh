@@ -323,38 +323,6 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
     }
 }
 
-// Packed triangular factor for the substitution kernels (block-pipelined layout).
-//
-// Rows are cut into contiguous blocks of at most S rows; one CTA solves one block at a
-// time and keeps the block's solution in shared memory.  Inside a block rows are grouped
-// by their level in the block-internal dependency DAG (dependencies on rows of other
-// blocks do not count) and a level is solved by the whole CTA between two barriers, so
-// every block-internal dependency is a shared-memory read.  Dependencies on other blocks
-// are read from the global solution with a value-as-flag wait; blocks are taken from a
-// ticket counter in dependency order (ascending for L, descending for U), so a block
-// only waits for blocks whose CTAs are already running: no deadlock, no co-residency
-// assumption.  Only the critical path's block boundaries pay the global handoff.
-//
-// Task t (32 rows of one level, one lane per row) owns slots [off[t], off[t] + 32 len[t]):
-// entry k of lane l sits at off[t] + 32 k + l (coalesced).  Entry codes: >= 0 global
-// column (other block), <= -2 local row -2-code (this block), -1 padding.  L entries are
-// kept in ascending column order and U entries in descending column order — the
-// accumulation order of the reference's substitute_row_L / _U (src/ilu_solver.cpp:687-696,
-// 719-729) — so the result is the same sequence of operations.
-template <class T>
-struct BlockTri {
-    int nblk = 0;
-    const int* blk_row = nullptr;   // [nblk + 1] first row of each block
-    const int* blk_lvl = nullptr;   // [nblk + 1] first level (index into lvl_task) of each block
-    const int* lvl_task = nullptr;  // [levels + 1] first task of each level
-    const int* rows = nullptr;      // [32 * ntask], -1 for padding
-    const int* off = nullptr;       // [ntask]
-    const int* len = nullptr;       // [ntask]
-    const int* codes = nullptr;     // [slots]
-    const T* vals = nullptr;        // [slots]
-    const T* dvals = nullptr;       // [32 * ntask] diagonal (upper factor only)
-};
-
 // Gathers packed values from the CSR factor values: dst[s] = src[s] >= 0 ? lu[src[s]] : 0.
 template <class T>
 __global__ void pack_gather_kernel(long long count, const int* __restrict__ src, const double* __restrict__ lu,
@@ -392,73 +360,289 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
     return *s_slot;
 }
 
+// ---------------------------------------------------------------------------------
+// Block-pipelined substitution (TMA-fed).
+//
+// Rows are cut into contiguous blocks; one CTA solves one block at a time and keeps the
+// block's right-hand side, overwritten in place by its solution, in shared memory.
+// Inside a block rows are grouped by their level in the block-internal dependency DAG
+// (dependencies on rows of other blocks do not count) and a level is solved by the whole
+// CTA between two barriers, one thread per row, so every block-internal dependency is a
+// shared-memory read.  Dependencies on other blocks are read from the global solution
+// with a value-as-flag wait, their loads issued one level ahead.  Blocks are taken from
+// a ticket counter in dependency order (ascending for L, descending for U), so a block
+// only waits for blocks whose CTAs are already running: no deadlock, no co-residency
+// assumption.  When the blocks follow the matrix's planes (a 3-D grid in natural order
+// cut every nx*ny rows) the dependencies between blocks connect equal block-internal
+// levels and the blocks run as a pipeline: the critical path crosses SMs once per
+// block instead of once per level.
+//
+// The per-level data (a "slice") streams into a ring of shared-memory stages by 1-D
+// bulk copies (cp.async.bulk, completed on one mbarrier per stage), `stages` levels
+// ahead, so no level waits on a global load of its own row data.  Slice layout, every
+// piece 16-byte aligned (Wp = W rounded up to 32):
+//   int4 header {W, K, bytes of the slice `stages` levels later (0: none), Wp}
+//   int  rows[Wp]          global row index of each position
+//   int  codes[K * Wp]     entry k of position p at k * Wp + p: >= 0 global column (other
+//                          block), <= -2 block-local row -2 - code, -1 padding (trailing)
+//   T    vals[K * Wp]
+//   T    diag[Wp]          upper factor only; FP32 stores 1 / u_ii
+// L entries are in ascending and U entries in descending column order: the accumulation
+// order of the reference's substitute_row_L / _U (src/ilu_solver.cpp:687-696, 719-729),
+// so each row performs the same operations in the same order as a sequential sweep.
+// ---------------------------------------------------------------------------------
+constexpr int kBandThreadsMax = 512;
+constexpr int kBandMaxStages = 16;
+constexpr int kBandPre = 4;  // cross-block dependencies per row loaded ahead (registers)
+#ifndef GB_BAND_AHEAD
+#define GB_BAND_AHEAD 3
+#endif
+constexpr int kBandAhead = GB_BAND_AHEAD;  // levels between a prefetch and its use
+
+template <class T>
+struct BandTri {
+    int nblk = 0;
+    int stages = 0;           // ring depth (>= 2)
+    unsigned stage_bytes = 0; // capacity of one ring stage (multiple of 128)
+    unsigned xs_bytes = 0;    // shared bytes of the block vector (multiple of 128)
+    const int* blk_row = nullptr;        // [nblk + 1] first row of each block
+    const int* blk_lvl = nullptr;        // [nblk + 1] first level of each block
+    const long long* blk_off = nullptr;  // [nblk] byte offset of each block's first slice
+    const int* lvl_bytes = nullptr;      // [levels] bytes of each slice
+    const unsigned char* data = nullptr; // slices, level order within block order
+};
+
+// Value-gather instructions of one slice of a block-pipelined factor: the slice's
+// values (nvals) and diagonal (ndiag, right after them) take lu[src[src_off + i]]
+// (0 for src < 0); an FP32 diagonal is stored as its reciprocal.
+struct SliceGather {
+    long long src_off;
+    long long val_off;  // byte offset of vals[0] in the slice data
+    int nvals;
+    int ndiag;
+};
+
+// One warp per slice.
+template <class T>
+__global__ void band_gather_kernel(int levels, const SliceGather* __restrict__ gat, const int* __restrict__ src,
+                                   const double* __restrict__ lu, unsigned char* __restrict__ data) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int l = blockIdx.x * wpb + (threadIdx.x >> 5); l < levels; l += gridDim.x * wpb) {
+        const SliceGather gi = gat[l];
+        T* dst = reinterpret_cast<T*>(data + gi.val_off);
+        const int* sp = src + gi.src_off;
+        const int total = gi.nvals + gi.ndiag;
+        for (int i = lane; i < total; i += kWarp) {
+            const int q = sp[i];
+            double v = q >= 0 ? lu[q] : 0.0;
+            if (sizeof(T) == 4 && i >= gi.nvals && q >= 0) v = 1.0 / v;
+            dst[i] = static_cast<T>(v);
+        }
+    }
+}
+
+// The rare slow path (a value not yet published) stays out of line: the hot loop is
+// unrolled several times and must fit the instruction cache.
+template <class T>
+__device__ __noinline__ T band_wait_value(const T* p, int* status) {
+    return wait_value(p, status);
+}
+
+// Issues the loads of this thread's cross-block values of slice `sl` (first position).
+// All shared-memory reads come first: a load with a compiler memory barrier between them
+// would serialise them.
+template <class T>
+__device__ __forceinline__ void band_prefetch(const unsigned char* sl, int p, const T* out, T (&pre)[kBandPre]) {
+    const int4 h = *reinterpret_cast<const int4*>(sl);
+    const int* codes = reinterpret_cast<const int*>(sl + 16) + h.w;
+    int cd[kBandPre];
+#pragma unroll
+    for (int k = 0; k < kBandPre; ++k) cd[k] = (p < h.x && k < h.y) ? codes[k * h.w + p] : -1;
+#pragma unroll
+    for (int k = 0; k < kBandPre; ++k) pre[k] = cd[k] >= 0 ? ld_relaxed_nb(out + cd[k]) : T(0);
+}
+
+// Reloads this thread's prefetched cross-block values of slice `sl` that still hold the
+// sentinel.
+template <class T>
+__device__ __forceinline__ void band_repoll(const unsigned char* sl, int p, const T* out, T (&pre)[kBandPre]) {
+    bool miss = false;
+#pragma unroll
+    for (int k = 0; k < kBandPre; ++k) miss |= Sentinel<T>::is(pre[k]);
+    if (!miss) return;
+    const int4 h = *reinterpret_cast<const int4*>(sl);
+    const int* codes = reinterpret_cast<const int*>(sl + 16) + h.w;
+#pragma unroll
+    for (int k = 0; k < kBandPre; ++k) {
+        if (Sentinel<T>::is(pre[k]) && p < h.x && k < h.y) {
+            const int cd = codes[k * h.w + p];
+            if (cd >= 0) pre[k] = ld_relaxed_nb(out + cd);
+        }
+    }
+}
+
+// Solves the rows of one slice (one block-internal level).  pre: this thread's
+// prefetched cross-block values for its first position (p == threadIdx.x).  The
+// shared-memory operands of a row are loaded together before any global access.
+template <class T, bool UPPER>
+__device__ __forceinline__ void band_solve_slice(const unsigned char* sl, const T (&pre)[kBandPre], T* xs, int base,
+                                                 T* in, bool scaled, T sc, T* out, int* status) {
+    const int4 h = *reinterpret_cast<const int4*>(sl);
+    const int W = h.x, K = h.y, Wp = h.w;
+    const int* rows = reinterpret_cast<const int*>(sl + 16);
+    const int* codes = rows + Wp;
+    const T* vals = reinterpret_cast<const T*>(codes + static_cast<size_t>(K) * Wp);
+    const int tid = threadIdx.x;
+    for (int p = tid; p < W; p += blockDim.x) {
+        const int row = rows[p];
+        int cd[kBandPre];
+        T v[kBandPre], x[kBandPre];
+#pragma unroll
+        for (int k = 0; k < kBandPre; ++k) {
+            cd[k] = k < K ? codes[k * Wp + p] : -1;
+            v[k] = k < K ? vals[k * Wp + p] : T(0);
+        }
+        const T d = UPPER ? vals[static_cast<size_t>(K) * Wp + p] : T(1);
+        T acc = xs[row - base];
+#pragma unroll
+        for (int k = 0; k < kBandPre; ++k) x[k] = cd[k] <= -2 ? xs[-2 - cd[k]] : (p == tid ? pre[k] : T(0));
+        if (!UPPER && scaled) acc = acc * sc;
+        const T acc0 = acc;
+#pragma unroll
+        for (int k = 0; k < kBandPre; ++k) {
+            if (cd[k] >= 0) {
+                if (p != tid) x[k] = ld_relaxed_nb(out + cd[k]);
+                if (Sentinel<T>::is(x[k])) x[k] = band_wait_value(out + cd[k], status);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kBandPre; ++k)
+            if (cd[k] != -1) acc = fma(-v[k], x[k], acc);
+        for (int k = kBandPre; k < K; ++k) {
+            const int c = codes[k * Wp + p];
+            if (c == -1) break;
+            T xv;
+            if (c <= -2) {
+                xv = xs[-2 - c];
+            } else {
+                xv = ld_relaxed(out + c);
+                if (Sentinel<T>::is(xv)) xv = band_wait_value(out + c, status);
+            }
+            acc = fma(-vals[k * Wp + p], xv, acc);
+        }
+        // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
+        if (UPPER) acc = sizeof(T) == 8 ? acc / d : acc * d;
+        acc = Sentinel<T>::canon(acc);
+        xs[row - base] = acc;
+        st_relaxed(out + row, acc);
+        if (!UPPER && scaled) in[row] = acc0;
+    }
+}
+
 // Forward (UPPER = false): out = L^{-1} (scale * in); with `scale`, in is rescaled in
 //   place (GMRES normalises its new Krylov vector in the same pass).
 // Backward (UPPER = true): out = U^{-1} in (in is left as it is).
-// out must hold the sentinel for every row on entry.
+// out must hold the sentinel for every row on entry.  Any block size (a multiple of 32,
+// at most kBandThreadsMax); dynamic shared memory: xs_bytes + stages * stage_bytes, and
+// stages >= kBandAhead + 2.
+//
+// Per level: solve the slice's rows, one CTA barrier, then issue the loads of the
+// cross-block values of the slice kBandAhead levels later.  A block thereby trails the
+// block it depends on by about one L2 round trip, and once the pipeline has filled its
+// levels do not wait on global memory.  Thread 0 alone handles the slice ring: at the
+// start of a level it refills the stage freed by the previous barrier and waits for the
+// slice the next prefetch reads, so the barrier publishes that slice to every thread.
+// The level loop is unrolled kBandAhead times so that every prefetch set stays in its
+// own registers (a register move would wait for the load).
 template <class T, bool UPPER>
-__global__ void __launch_bounds__(kSolveThreads)
-    sptrsv_block_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
-                        const int* gate, int step) {
+__global__ void __launch_bounds__(kBandThreadsMax, 1)
+    sptrsv_band_kernel(BandTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
+                       const int* gate, int step) {
     if (gate_closed(gate, step)) return;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* xs = reinterpret_cast<T*>(smem_raw);
+    extern __shared__ __align__(128) unsigned char band_smem[];
+    __shared__ __align__(8) unsigned long long bars[kBandMaxStages + 1];
     __shared__ int s_ticket;
-    const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const T sc = (!UPPER && scale) ? static_cast<T>(*scale) : T(1);
+    T* xs = reinterpret_cast<T*>(band_smem);
+    unsigned char* ring = band_smem + P.xs_bytes;
+    const unsigned D = static_cast<unsigned>(P.stages);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (unsigned i = 0; i <= D; ++i) mbar_init(&bars[i], 1u);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool scaled = !UPPER && scale != nullptr;
+    const T sc = scaled ? static_cast<T>(*scale) : T(1);
+    unsigned g0 = 0;     // ring slots consumed by this CTA so far (phase bookkeeping)
+    unsigned xpar = 0;   // phase parity of the block-vector barrier
+    auto slice = [&](unsigned g) { return ring + static_cast<size_t>(g % D) * P.stage_bytes; };
+    // thread 0 only
+    auto wait_slice = [&](unsigned g) { mbar_wait(&bars[g % D], (g / D) & 1u, status); };
+    auto issue_slice = [&](unsigned g, unsigned nb, long long& off) {
+        mbar_arrive_expect_tx(&bars[g % D], nb);
+        bulk_copy_g2s(ring + static_cast<size_t>(g % D) * P.stage_bytes, P.data + off, nb, &bars[g % D]);
+        off += nb;
+    };
     for (int tk = draw_block_ticket(counter, P.nblk, &s_ticket); tk < P.nblk;
          tk = draw_block_ticket(counter, P.nblk, &s_ticket)) {
         const int c = UPPER ? P.nblk - 1 - tk : tk;
         const int base = P.blk_row[c];
-        const int l0 = P.blk_lvl[c];
-        const int l1 = P.blk_lvl[c + 1];
-        for (int l = l0; l < l1; ++l) {
-            const int t1 = P.lvl_task[l + 1];
-            for (int t = P.lvl_task[l] + w; t < t1; t += kSolveWarps) {
-                const int q = t * kWarp + lane;
-                const int row = P.rows[q];
-                const int o = P.off[t];
-                const int K = P.len[t];
-                const T d = UPPER ? P.dvals[q] : T(1);
-                T acc = T(0);
-                if (row >= 0) {
-                    acc = in[row];
-                    if (!UPPER && scale) {
-                        acc = acc * sc;
-                        in[row] = acc;
-                    }
-                }
-                for (int k0 = 0; k0 < K; k0 += 8) {
-                    int cd[8];
-                    T v[8], x[8];
+        const int cnt = P.blk_row[c + 1] - base;
+        const int lv0 = P.blk_lvl[c];
+        const int nl = P.blk_lvl[c + 1] - lv0;
+        const T* src = in + base;
+        const unsigned xb =
+            (reinterpret_cast<uintptr_t>(src) & 15u) == 0 ? (static_cast<unsigned>(cnt) * sizeof(T)) & ~15u : 0u;
+        long long issue_off = 0;
+        unsigned nb_prev = 0;  // thread 0: bytes of the slice that refills the stage freed last
+        if (tid == 0) {
+            if (xb) {
+                mbar_arrive_expect_tx(&bars[D], xb);
+                bulk_copy_g2s(xs, src, xb, &bars[D]);
+            }
+            issue_off = P.blk_off[c];
+            const int first = min(static_cast<int>(D), nl);
+            for (int i = 0; i < first; ++i)
+                issue_slice(g0 + static_cast<unsigned>(i), static_cast<unsigned>(P.lvl_bytes[lv0 + i]), issue_off);
+            for (int i = 0; i < kBandAhead && i < nl; ++i) wait_slice(g0 + static_cast<unsigned>(i));
+            if (xb) mbar_wait(&bars[D], xpar, status);
+        }
+        if (xb) xpar ^= 1u;
+        for (int i = static_cast<int>(xb / sizeof(T)) + tid; i < cnt; i += blockDim.x) xs[i] = src[i];
+        __syncthreads();
+        T pre[kBandAhead][kBandPre];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int sidx = o + (k0 + u) * kWarp + lane;
-                        cd[u] = (k0 + u < K) ? P.codes[sidx] : -1;
-                        v[u] = (k0 + u < K) ? P.vals[sidx] : T(0);
-                    }
+        for (int j = 0; j < kBandAhead; ++j)
+            if (j < nl) band_prefetch<T>(slice(g0 + j), tid, out, pre[j]);
+        for (int l = 0; l < nl; l += kBandAhead) {
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        x[u] = cd[u] >= 0 ? ld_relaxed(out + cd[u]) : (cd[u] <= -2 ? xs[-2 - cd[u]] : T(0));
+            for (int j = 0; j < kBandAhead; ++j) {
+                const int lj = l + j;
+                if (lj < nl) {
+                    const unsigned g = g0 + static_cast<unsigned>(lj);
+                    if (tid == 0) {
+                        // the barrier that ended level lj - 1 freed its stage: refill it
+                        if (nb_prev != 0) issue_slice(g + D - 1, nb_prev, issue_off);
+                        // the prefetch after this level's barrier reads slice lj + kBandAhead
+                        if (lj + kBandAhead < nl) wait_slice(g + kBandAhead);
                     }
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        if (cd[u] != -1) {
-                            if (cd[u] >= 0 && Sentinel<T>::is(x[u])) x[u] = wait_value(out + cd[u], status);
-                            acc = fma(-v[u], x[u], acc);
-                        }
-                    }
-                }
-                if (row >= 0) {
-                    if (UPPER) acc = sizeof(T) == 8 ? acc / d : acc * d;
-                    acc = Sentinel<T>::canon(acc);
-                    xs[row - base] = acc;
-                    st_relaxed(out + row, acc);
+                    const unsigned char* sl = slice(g);
+                    band_solve_slice<T, UPPER>(sl, pre[j], xs, base, in, scaled, sc, out, status);
+                    if (tid == 0) nb_prev = static_cast<unsigned>(reinterpret_cast<const int4*>(sl)->z);
+                    __syncthreads();
+                    if (lj + kBandAhead < nl) band_prefetch<T>(slice(g + kBandAhead), tid, out, pre[j]);
+                    // values of the next level that were not yet published when prefetched
+                    // (the producing block runs just ahead): load them again now, a level
+                    // before they are needed, instead of waiting a round trip then
+                    if (kBandAhead > 1 && lj + 1 < nl) band_repoll<T>(slice(g + 1), tid, out, pre[(j + 1) % kBandAhead]);
                 }
             }
-            __syncthreads();
         }
+        g0 += static_cast<unsigned>(nl);
+        // this block's generic writes of xs come before the next block's bulk copy into it
+        // (once per block: a proxy fence waits for the thread's outstanding memory operations)
+        fence_proxy_async_smem();
     }
 }
 

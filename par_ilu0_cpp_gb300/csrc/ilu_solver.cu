@@ -106,146 +106,194 @@ static void gather_level_pack(const LevelPack& P, bool lower, const double* lu, 
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
-// Host construction of a block-pipelined packed factor (see BlockTri).
-// lower: entries [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1])
-// descending plus the diagonal position.
-static void build_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
-                       int block_rows, TriPack& P, cudaStream_t s) {
+// Block-internal levels of rows [lo, hi): dependencies on rows outside the block do
+// not count.  depth[r - lo] receives the level of row r; returns the level count.
+static int block_levels(int lo, int hi, bool lower, const int* rp, const int* ci, const std::vector<int>& diag,
+                        std::vector<int>& depth) {
+    int nlev = 0;
+    for (int s2 = 0; s2 < hi - lo; ++s2) {
+        const int r = lower ? lo + s2 : hi - 1 - s2;
+        int d = 0;
+        const int b0 = lower ? rp[r] : diag[r] + 1;
+        const int b1 = lower ? diag[r] : rp[r + 1];
+        for (int p = b0; p < b1; ++p) {
+            const int col = ci[p];
+            if (col >= lo && col < hi) d = std::max(d, depth[col - lo] + 1);
+        }
+        depth[r - lo] = d;
+        nlev = std::max(nlev, d + 1);
+    }
+    return nlev;
+}
+
+static unsigned round_up(unsigned long long v, unsigned a) { return static_cast<unsigned>((v + a - 1) / a * a); }
+
+// Bytes of one slice of W rows with at most K entries (see BandTri).
+static unsigned long long slice_bytes(int W, int K, int elem, bool lower) {
+    const unsigned long long Wp = round_up(static_cast<unsigned long long>(W), kWarp);
+    return 16 + 4 * Wp * (1 + static_cast<unsigned long long>(K)) +
+           static_cast<unsigned long long>(elem) * (static_cast<unsigned long long>(K) * Wp + (lower ? 0 : Wp));
+}
+
+// Host construction of a block-pipelined packed factor for values of `elem` bytes
+// (see BandTri).  Returns false (and builds nothing) when a ring of kBandAhead + 2 slices does not
+// fit next to the block vector in `smem_budget` bytes of shared memory.
+static bool build_band_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
+                            int block_rows, int elem, size_t smem_budget, BandPack& P, cudaStream_t s) {
     const int S = std::max(1, std::min(block_rows, std::max(n, 1)));
     const int nblk = n > 0 ? ceil_div(n, S) : 0;
-    std::vector<int> blk_row(static_cast<size_t>(nblk) + 1), blk_lvl(static_cast<size_t>(nblk) + 1, 0);
-    std::vector<int> lvl_task(1, 0), rows, off, len, dsrc;
-    std::vector<int> depth(static_cast<size_t>(S)), cnt, ord;
     auto ebeg = [&](int r) { return lower ? rp[r] : diag[r] + 1; };
     auto eend = [&](int r) { return lower ? diag[r] : rp[r + 1]; };
-    long long slots = 0;
-    // pass 1: levels, tasks, lengths
-    std::vector<std::vector<int>> blk_order(static_cast<size_t>(nblk));
+    // pass 1: levels of every block, rows grouped by level, slice sizes
+    std::vector<int> blk_row(static_cast<size_t>(nblk) + 1), blk_lvl(static_cast<size_t>(nblk) + 1, 0);
+    std::vector<int> lvl_start(1, 0), lvl_K, lrows;
+    lrows.reserve(static_cast<size_t>(n));
+    std::vector<int> depth(static_cast<size_t>(S)), cnt;
+    int max_levels = 0;
     for (int c = 0; c < nblk; ++c) {
         const int lo = c * S;
         const int hi = std::min(n, lo + S);
         blk_row[c] = lo;
-        int nlev = 0;
-        for (int s2 = 0; s2 < hi - lo; ++s2) {
-            const int r = lower ? lo + s2 : hi - 1 - s2;
-            int d = 0;
-            for (int p = ebeg(r); p < eend(r); ++p) {
-                const int col = ci[p];
-                if (col >= lo && col < hi) d = std::max(d, depth[col - lo] + 1);
-            }
-            depth[r - lo] = d;
-            nlev = std::max(nlev, d + 1);
-        }
+        const int nlev = block_levels(lo, hi, lower, rp, ci, diag, depth);
+        max_levels = std::max(max_levels, nlev);
         cnt.assign(static_cast<size_t>(nlev) + 1, 0);
         for (int r = lo; r < hi; ++r) ++cnt[depth[r - lo] + 1];
         for (int l = 0; l < nlev; ++l) cnt[l + 1] += cnt[l];
-        ord.assign(static_cast<size_t>(hi - lo), 0);
+        const size_t base = lrows.size();
+        lrows.resize(base + static_cast<size_t>(hi - lo));
         std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-        for (int r = lo; r < hi; ++r) ord[fill[depth[r - lo]]++] = r;
+        for (int r = lo; r < hi; ++r) lrows[base + fill[depth[r - lo]]++] = r;
         for (int l = 0; l < nlev; ++l) {
-            for (int q0 = cnt[l]; q0 < cnt[l + 1]; q0 += kWarp) {
-                int K = 0;
-                for (int u = 0; u < kWarp; ++u) {
-                    const int q = q0 + u;
-                    if (q < cnt[l + 1]) {
-                        const int r = ord[q];
-                        rows.push_back(r);
-                        K = std::max(K, eend(r) - ebeg(r));
-                        if (!lower) dsrc.push_back(diag[r]);
-                    } else {
-                        rows.push_back(-1);
-                        if (!lower) dsrc.push_back(-1);
-                    }
-                }
-                off.push_back(static_cast<int>(slots));
-                len.push_back(K);
-                slots += static_cast<long long>(K) * kWarp;
-                if (slots > INT_MAX) throw std::runtime_error("triangular factor too large for 32-bit slot offsets");
+            int K = 0;
+            for (int q = cnt[l]; q < cnt[l + 1]; ++q) {
+                const int r = lrows[base + q];
+                K = std::max(K, eend(r) - ebeg(r));
             }
-            lvl_task.push_back(static_cast<int>(off.size()));
+            lvl_K.push_back(K);
+            lvl_start.push_back(static_cast<int>(base) + cnt[l + 1]);
         }
         blk_lvl[c + 1] = blk_lvl[c] + nlev;
     }
     blk_row[nblk] = n;
-    const int ntask = static_cast<int>(off.size());
-    // pass 2: entry codes and gather sources
-    std::vector<int> codes(static_cast<size_t>(slots), -1), src(static_cast<size_t>(slots), -1);
-    for (int t = 0; t < ntask; ++t) {
-        for (int l = 0; l < kWarp; ++l) {
-            const int r = rows[static_cast<size_t>(t) * kWarp + l];
-            if (r < 0) continue;
-            const int lo = (r / S) * S;
-            const int hi = std::min(n, lo + S);
-            int k = 0;
-            auto put = [&](int p) {
-                const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
-                const int col = ci[p];
-                codes[sidx] = (col >= lo && col < hi) ? -2 - (col - lo) : col;
-                src[sidx] = p;
-                ++k;
-            };
-            if (lower) {
-                for (int p = rp[r]; p < diag[r]; ++p) put(p);
-            } else {
-                for (int p = rp[r + 1] - 1; p > diag[r]; --p) put(p);
+    const int levels = blk_lvl[nblk];
+    std::vector<int> lvl_bytes(static_cast<size_t>(levels));
+    unsigned long long max_bytes = 16, total = 0;
+    int max_width = 1;
+    for (int l = 0; l < levels; ++l) {
+        max_width = std::max(max_width, lvl_start[l + 1] - lvl_start[l]);
+        const unsigned long long b = slice_bytes(lvl_start[l + 1] - lvl_start[l], lvl_K[l], elem, lower);
+        if (b > (1ull << 30)) return false;
+        lvl_bytes[l] = static_cast<int>(b);
+        max_bytes = std::max(max_bytes, b);
+        total += b;
+    }
+    const unsigned stage_bytes = round_up(max_bytes, 128);
+    const unsigned xs_bytes = round_up(static_cast<unsigned long long>(S) * elem, 128);
+    if (xs_bytes + static_cast<unsigned long long>(kBandAhead + 2) * stage_bytes > smem_budget) return false;
+    const int stages = static_cast<int>(std::min<unsigned long long>(kBandMaxStages, (smem_budget - xs_bytes) / stage_bytes));
+    // pass 2: slice images and gather instructions
+    std::vector<unsigned char> img(static_cast<size_t>(total));
+    std::vector<long long> blk_off(static_cast<size_t>(nblk));
+    std::vector<SliceGather> gat(static_cast<size_t>(levels));
+    std::vector<int> src;
+    long long off = 0;
+    for (int c = 0; c < nblk; ++c) {
+        blk_off[c] = off;
+        const int lo = blk_row[c];
+        const int hi = blk_row[c + 1];
+        const int l0 = blk_lvl[c];
+        const int l1 = blk_lvl[c + 1];
+        for (int L = l0; L < l1; ++L) {
+            const int W = lvl_start[L + 1] - lvl_start[L];
+            const int K = lvl_K[L];
+            const int Wp = static_cast<int>(round_up(static_cast<unsigned long long>(W), kWarp));
+            unsigned char* sl = img.data() + off;
+            const int hdr[4] = {W, K, L + stages < l1 ? lvl_bytes[L + stages] : 0, Wp};
+            std::memcpy(sl, hdr, sizeof(hdr));
+            int* rows = reinterpret_cast<int*>(sl + 16);
+            int* codes = rows + Wp;
+            for (int p = 0; p < Wp; ++p) rows[p] = p < W ? lrows[lvl_start[L] + p] : -1;
+            std::fill(codes, codes + static_cast<size_t>(K) * Wp, -1);
+            SliceGather& gi = gat[L];
+            gi.src_off = static_cast<long long>(src.size());
+            gi.val_off = off + 16 + 4ll * Wp * (1 + K);
+            gi.nvals = K * Wp;
+            gi.ndiag = lower ? 0 : Wp;
+            const size_t s0 = src.size();
+            src.resize(s0 + static_cast<size_t>(gi.nvals + gi.ndiag), -1);
+            for (int p = 0; p < W; ++p) {
+                const int r = rows[p];
+                int k = 0;
+                auto put = [&](int q) {
+                    const int col = ci[q];
+                    codes[static_cast<size_t>(k) * Wp + p] = (col >= lo && col < hi) ? -2 - (col - lo) : col;
+                    src[s0 + static_cast<size_t>(k) * Wp + p] = q;
+                    ++k;
+                };
+                if (lower) {
+                    for (int q = rp[r]; q < diag[r]; ++q) put(q);
+                } else {
+                    for (int q = rp[r + 1] - 1; q > diag[r]; --q) put(q);
+                    src[s0 + static_cast<size_t>(gi.nvals) + p] = diag[r];
+                }
             }
+            off += lvl_bytes[L];
         }
     }
+    if (src.size() > static_cast<size_t>(INT_MAX)) throw std::runtime_error("triangular factor too large");
+    P.elem = elem;
     P.nblk = nblk;
     P.block_rows = S;
-    P.ntask = ntask;
-    P.levels = blk_lvl[nblk];
-    P.slots = slots;
-    P.smem64 = sizeof(double) * static_cast<size_t>(S);
-    P.smem32 = sizeof(float) * static_cast<size_t>(S);
+    P.levels = levels;
+    P.max_levels = max_levels;
+    P.stages = stages;
+    P.stage_bytes = stage_bytes;
+    P.xs_bytes = xs_bytes;
+    P.smem = static_cast<size_t>(xs_bytes) + static_cast<size_t>(stages) * stage_bytes;
+    // one thread per row of the widest level (whole warps, 64 .. kBandThreadsMax)
+    P.threads = std::max(64, std::min(kBandThreadsMax, static_cast<int>(round_up(max_width, kWarp))));
+    P.bytes = static_cast<long long>(total);
     P.blk_row.upload(blk_row.data(), blk_row.size(), s);
     P.blk_lvl.upload(blk_lvl.data(), blk_lvl.size(), s);
-    P.lvl_task.upload(lvl_task.data(), lvl_task.size(), s);
-    P.rows.upload(rows.data(), rows.size(), s);
-    P.off.upload(off.data(), off.size(), s);
-    P.len.upload(len.data(), len.size(), s);
-    P.codes.upload(codes.data(), codes.size(), s);
+    P.blk_off.upload(blk_off.data(), blk_off.size(), s);
+    P.lvl_bytes.upload(lvl_bytes.data(), lvl_bytes.size(), s);
     P.src.upload(src.data(), src.size(), s);
-    if (!lower) P.dsrc.upload(dsrc.data(), dsrc.size(), s);
-    P.v64.reserve(static_cast<size_t>(slots));
-    P.v32.reserve(static_cast<size_t>(slots));
-    if (!lower) {
-        P.d64.reserve(rows.size());
-        P.d32.reserve(rows.size());
-    }
+    P.gat.upload(gat.data(), gat.size(), s);
+    P.data.upload(img.data(), img.size(), s);
     // host vectors must outlive the asynchronous copies
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
+    return true;
 }
 
-static void gather_pack(const TriPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
+static void gather_band(const BandPack& P, const double* lu, cudaStream_t s, int sms) {
+    if (P.levels == 0) return;
     const int threads = 256;
-    auto grid_for = [&](long long count) {
-        long long g = ceil_div<long long>(count, threads);
-        return static_cast<int>(std::max<long long>(1, std::min<long long>(g, 8LL * sms)));
-    };
-    if (P.slots > 0) {
-        pack_gather_kernel<double><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v64.get());
-        pack_gather_kernel<float><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v32.get());
-    }
-    if (!lower && P.ntask > 0) {
-        const long long nd = static_cast<long long>(P.ntask) * kWarp;
-        pack_gather_kernel<double><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d64.get());
-        pack_gather_recip_kernel<<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
-    }
+    const int grid = static_cast<int>(std::max(1, std::min(ceil_div(P.levels, threads / kWarp), 8 * sms)));
+    if (P.elem == 8)
+        band_gather_kernel<double><<<grid, threads, 0, s>>>(P.levels, P.gat.get(), P.src.get(), lu, P.data.get());
+    else
+        band_gather_kernel<float><<<grid, threads, 0, s>>>(P.levels, P.gat.get(), P.src.get(), lu, P.data.get());
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
-// Raises the dynamic shared-memory limit of both substitution kernels of type T to
-// `smem` bytes; returns the persistent grid (CTAs resident at that footprint).
-template <class T>
-static int configure_block_kernels(size_t smem, int sms) {
-    const int bytes = static_cast<int>(std::max<size_t>(smem, 16));
-    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+// Raises the kernel's dynamic shared-memory limit to the pack's footprint and records
+// the number of resident CTAs.
+template <class T, bool UPPER>
+static void configure_band(BandPack& P, int sms) {
+    const int bytes = static_cast<int>(std::max<size_t>(P.smem, 16));
+    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_band_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     int per_sm = 0;
-    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_block_kernel<T, false>, kSolveThreads,
+    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_band_kernel<T, UPPER>, P.threads,
                                                                static_cast<size_t>(bytes)));
-    return std::max(1, per_sm) * sms;
+    P.grid = std::max(1, per_sm) * sms;
+}
+
+template <class T, bool UPPER>
+static void launch_band(const BandPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
+                        int* status, const int* gate, int step) {
+    if (P.nblk == 0) return;
+    sptrsv_band_kernel<T, UPPER><<<std::min(P.grid, P.nblk), P.threads, P.smem, s>>>(
+        P.view<T>(), in, scale, out, counter, status, gate, step);
 }
 
 template <class T>
@@ -271,12 +319,8 @@ IluSolver::Impl::~Impl() {
 
 template <class T>
 void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const {
-    if (block_mode) {
-        if (LB.nblk == 0) return;
-        const int grid = sizeof(T) == 8 ? grid_block64 : grid_block32;
-        const size_t smem = sizeof(T) == 8 ? LB.smem64 : LB.smem32;
-        sptrsv_block_kernel<T, false><<<std::min(grid, LB.nblk), kSolveThreads, smem, s>>>(
-            LB.view<T>(), b, scale, y, counters.get() + 1, status.get(), gate, step);
+    if (sizeof(T) == 8 ? band64 : band32) {
+        launch_band<T, false>(sizeof(T) == 8 ? LB64 : LB32, s, b, scale, y, counters.get() + 1, status.get(), gate, step);
         return;
     }
     if (L.ntask == 0) return;
@@ -286,12 +330,8 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
 
 template <class T>
 void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const {
-    if (block_mode) {
-        if (UB.nblk == 0) return;
-        const int grid = sizeof(T) == 8 ? grid_block64 : grid_block32;
-        const size_t smem = sizeof(T) == 8 ? UB.smem64 : UB.smem32;
-        sptrsv_block_kernel<T, true><<<std::min(grid, UB.nblk), kSolveThreads, smem, s>>>(
-            UB.view<T>(), y, nullptr, x, counters.get() + 2, status.get(), gate, step);
+    if (sizeof(T) == 8 ? band64 : band32) {
+        launch_band<T, true>(sizeof(T) == 8 ? UB64 : UB32, s, y, nullptr, x, counters.get() + 2, status.get(), gate, step);
         return;
     }
     if (U.ntask == 0) return;
@@ -299,6 +339,14 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
                                                                 gate, step);
 }
 
+template <class T>
+const void* IluSolver::Impl::subst_key() const {
+    if (sizeof(T) == 8 ? band64 : band32) return (sizeof(T) == 8 ? LB64 : LB32).data.get();
+    return L.cols.get();
+}
+
+template const void* IluSolver::Impl::subst_key<double>() const;
+template const void* IluSolver::Impl::subst_key<float>() const;
 template void IluSolver::Impl::launch_lower<double>(cudaStream_t, double*, const double*, double*, const int*, int) const;
 template void IluSolver::Impl::launch_lower<float>(cudaStream_t, float*, const double*, float*, const int*, int) const;
 template void IluSolver::Impl::launch_upper<double>(cudaStream_t, double*, double*, const int*, int) const;
@@ -367,11 +415,27 @@ void IluSolver::SetupMatrix() {
     GB_CUDA_CHECK(cudaMemsetAsync(im.counters.get(), 0, sizeof(unsigned) * 8, s));
     im.status.reserve(kStatusWords);
     GB_CUDA_CHECK(cudaMemsetAsync(im.status.get(), 0, sizeof(int) * kStatusWords, s));
-    im.block_mode = im.block_rows > 0;
-    if (im.block_mode) {
-        build_pack(n, rp, ci, im.an.diag, true, im.block_rows, im.LB, s);
-        build_pack(n, rp, ci, im.an.diag, false, im.block_rows, im.UB, s);
-    } else {
+    ++im.setup_gen;
+    im.band64 = im.band32 = false;
+    if (im.block_rows > 0) {
+        // explicit block size; a value type whose block vector and slice ring do not fit
+        // in shared memory keeps the level-ordered kernel
+        const size_t budget = static_cast<size_t>(std::max(0, im.dev.smem_optin - 1024));
+        im.band64 = build_band_pack(n, rp, ci, im.an.diag, true, im.block_rows, 8, budget, im.LB64, s) &&
+                    build_band_pack(n, rp, ci, im.an.diag, false, im.block_rows, 8, budget, im.UB64, s);
+        im.band32 = build_band_pack(n, rp, ci, im.an.diag, true, im.block_rows, 4, budget, im.LB32, s) &&
+                    build_band_pack(n, rp, ci, im.an.diag, false, im.block_rows, 4, budget, im.UB32, s);
+        if (im.band64) {
+            configure_band<double, false>(im.LB64, im.dev.sms);
+            configure_band<double, true>(im.UB64, im.dev.sms);
+        }
+        if (im.band32) {
+            configure_band<float, false>(im.LB32, im.dev.sms);
+            configure_band<float, true>(im.UB32, im.dev.sms);
+        }
+    }
+    im.level_packs = !(im.band64 && im.band32);
+    if (im.level_packs) {
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, im.L, s);
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, im.U, s);
     }
@@ -387,10 +451,6 @@ void IluSolver::SetupMatrix() {
     // L2 and the ready values propagate faster (measured: 1/SM beats full occupancy by
     // 1.8x on the 128^3 7-point factor).
     im.grid_solve = im.dev.sms;
-    if (im.block_mode) {
-        im.grid_block64 = configure_block_kernels<double>(std::max(im.LB.smem64, im.UB.smem64), im.dev.sms);
-        im.grid_block32 = configure_block_kernels<float>(std::max(im.LB.smem32, im.UB.smem32), im.dev.sms);
-    }
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
@@ -430,14 +490,22 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
                 n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(), shift, im.done.get(),
                 im.stamp, im.counters.get(), im.status.get());
             GB_CUDA_CHECK(cudaGetLastError());
-            if (im.block_mode) {
-                gather_pack(im.LB, true, im.lu.get(), s, im.dev.sms);
-                gather_pack(im.UB, false, im.lu.get(), s, im.dev.sms);
-            } else {
+            im.launches += 1;
+            if (im.band64) {
+                gather_band(im.LB64, im.lu.get(), s, im.dev.sms);
+                gather_band(im.UB64, im.lu.get(), s, im.dev.sms);
+                im.launches += 2;
+            }
+            if (im.band32) {
+                gather_band(im.LB32, im.lu.get(), s, im.dev.sms);
+                gather_band(im.UB32, im.lu.get(), s, im.dev.sms);
+                im.launches += 2;
+            }
+            if (im.level_packs) {
                 gather_level_pack(im.L, true, im.lu.get(), s, im.dev.sms);
                 gather_level_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+                im.launches += 6;
             }
-            im.launches += 7;
         }
         GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
         std::array<int, kStatusWords> h{};
@@ -577,13 +645,9 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
     fill_sentinel(y, n, s, im.dev.sms);
     fill_sentinel(d_x, n, s, im.dev.sms);
     double* b = const_cast<double*>(d_b);  // read only: no scale is passed to the forward sweep
-    if (im.block_mode) {
-        if (im.LB.nblk > 0) {
-            sptrsv_block_kernel<double, false><<<std::min(im.grid_block64, im.LB.nblk), kSolveThreads, im.LB.smem64, s>>>(
-                im.LB.view<double>(), b, nullptr, y, counters + 1, status, nullptr, 0);
-            sptrsv_block_kernel<double, true><<<std::min(im.grid_block64, im.UB.nblk), kSolveThreads, im.UB.smem64, s>>>(
-                im.UB.view<double>(), y, nullptr, d_x, counters + 2, status, nullptr, 0);
-        }
+    if (im.band64) {
+        launch_band<double, false>(im.LB64, s, b, nullptr, y, counters + 1, status, nullptr, 0);
+        launch_band<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
     } else if (im.L.ntask > 0) {
         sptrsv_lower_kernel<double><<<im.grid_solve, kSolveThreads, 0, s>>>(im.L.view<double>(), b, nullptr, y,
                                                                             counters + 1, status, nullptr, 0);
