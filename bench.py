@@ -136,14 +136,30 @@ def algorithmic_bytes(kind, a, nnz_l, nnz_u, tsize, steps_hist):
         # packed L entries (col + value), row ids, rhs read, normalised rhs written back, y written
         return S * ((4 + tsize) * nnz_l + 4 * n + 3 * tsize * n)
     if kind == "sptrsv_upper":
-        # packed U entries + diagonal, row ids, y read (and reset), z written
-        return S * ((4 + tsize) * nnz_u + (4 + tsize) * n + 4 * n + 3 * tsize * n)
+        # packed U entries (col + value), row ids, diagonal, y read, z written
+        return S * ((4 + tsize) * nnz_u + 4 * n + 3 * tsize * n)
     if kind == "spmv":
-        return S * ((4 + tsize) * nnz + 4 * (n + 1) + 2 * tsize * n)
+        # CSR (col + value, row pointers), x read, w written, forward-sweep vector reset
+        return S * ((4 + tsize) * nnz + 4 * (n + 1) + 3 * tsize * n)
     if kind == "cgs_dot":
         return sum(tsize * n * (s + 2) for s in steps_hist)
     if kind in ("cgs_axpy_dot", "cgs_axpy_norm"):
         return sum(tsize * n * (s + 3) for s in steps_hist)
+    return None
+
+
+def measured_traffic(kind, size):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the FP32
+    kernel `kind`, from the committed ncu summary of the convdiff3d 128^3 workload
+    (lines "traffic <kind> <bytes>"); None for another size or kernel."""
+    path = os.path.join(ROOT, "profiles", "sptrsv_fp32_convdiff3d_128.md")
+    if size != 128 or not os.path.isfile(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            parts = line.strip().strip("`").split()
+            if len(parts) == 3 and parts[0] == "traffic" and parts[1] == kind:
+                return int(parts[2])
     return None
 
 
@@ -477,11 +493,7 @@ def run_ours(args):
     dom = max((k for k in prof if prof[k]["gbs"] is not None), key=lambda k: prof[k]["ms_total"])
     peak, peak_kind = measured_peaks()
     achieved = prof[dom]["gbs"]
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.isfile(tpath):
-        with open(tpath) as fh:
-            traffic = json.load(fh).get(dom)
+    traffic = measured_traffic(dom, args.size)
 
     batched = None
     others = None
