@@ -59,7 +59,10 @@ enum {
      *        a value type (FP64 / FP32) whose block does not fit keeps the level kernel;
      *   0:   automatic (the level-ordered sync-free kernel);
      *   -1:  the level-ordered sync-free kernel. */
-    LLJBASH_ILU_OPT_BLOCK_ROWS = 2
+    LLJBASH_ILU_OPT_BLOCK_ROWS = 2,
+    /* warps of the level-ordered substitution kernels (0 = automatic: about four levels'
+     * worth of 32-row tasks, at most 8 per SM).  Takes effect at the next IluSolverSetup. */
+    LLJBASH_ILU_OPT_SOLVE_WARPS = 3
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 

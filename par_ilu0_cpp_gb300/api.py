@@ -58,6 +58,7 @@ class GmresReport(ctypes.Structure):
 
 ILU_OPT_COPY_BACK = 1
 ILU_OPT_BLOCK_ROWS = 2
+ILU_OPT_SOLVE_WARPS = 3
 GMRES_OPT_MODE = 1
 GMRES_OPT_TAU = 2
 GMRES_OPT_USE_GRAPH = 3

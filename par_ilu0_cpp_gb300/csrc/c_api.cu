@@ -136,6 +136,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
             case LLJBASH_ILU_OPT_COPY_BACK:
                 s->impl()->copy_back = value != 0.0;
                 return 0;
+            case LLJBASH_ILU_OPT_SOLVE_WARPS:
+                if (value < 0 || value > 1e6) throw std::runtime_error("solve warps must be 0 (automatic) or a warp count");
+                s->impl()->solve_warps = static_cast<int>(value);
+                return 0;
             case LLJBASH_ILU_OPT_BLOCK_ROWS:
                 if (value < -1 || value > 1e8) throw std::runtime_error("block rows must be -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);

@@ -94,6 +94,11 @@ __device__ __forceinline__ int ld_relaxed_int(const int* p) {
     return v;
 }
 
+// Polls made back to back before a wait starts to sleep between polls: a dependency on
+// the critical path is usually published within a few round trips, and a sleep (whose
+// actual length is far above its nominal 32 ns) would delay its detection.
+constexpr int kSpinBeforeSleep = 256;
+
 // Waits until *p is no longer the sentinel; returns the value.  Gives up after
 // kSpinLimit polls (or as soon as another thread has given up), records the timeout in
 // status[kStatusTimeout] and returns 0.
@@ -102,7 +107,7 @@ __device__ __forceinline__ T wait_value(const T* p, int* status) {
     T v = ld_relaxed(p);
     if (!Sentinel<T>::is(v)) return v;
     for (long long it = 0; it < kSpinLimit; ++it) {
-        __nanosleep(32);
+        if (it >= kSpinBeforeSleep) __nanosleep(32);
         v = ld_relaxed(p);
         if (!Sentinel<T>::is(v)) return v;
         if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) return T(0);
@@ -111,11 +116,11 @@ __device__ __forceinline__ T wait_value(const T* p, int* status) {
     return T(0);
 }
 
-// Waits until *flag == stamp (acquire).  Same give-up rule as wait_value.
+// Waits until *flag == stamp (acquire).  Same spin and give-up rules as wait_value.
 __device__ __forceinline__ bool wait_flag(const int* flag, int stamp, int* status) {
     if (ld_acquire(flag) == stamp) return true;
     for (long long it = 0; it < kSpinLimit; ++it) {
-        __nanosleep(32);
+        if (it >= kSpinBeforeSleep) __nanosleep(32);
         if (ld_acquire(flag) == stamp) return true;
         if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) return false;
     }

@@ -137,7 +137,10 @@ struct IluSolver::Impl {
     int first_breakdown = -1;
     float last_factor_ms = 0.f;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    int grid_fact = 0, grid_solve = 0;
+    int grid_fact = 0;
+    // level-ordered substitution launch: grid_solve CTAs of solve_threads threads
+    int grid_solve = 0, solve_threads = 0;
+    int solve_warps = 0;  // requested warps for the level-ordered kernels (0 = automatic)
     int block_rows = 0;  // rows per substitution block (0 = automatic, < 0 = level-ordered kernel)
     long long launches = 0;  // kernels launched by Factorize / Substitute
 

@@ -166,7 +166,10 @@ struct PackedTri {
     const T* dvals = nullptr;    // [32 * ntask] diagonal (upper factor only)
 };
 
-constexpr int kLaneEntries = 8;  // rows with at most this many entries use the per-lane path
+constexpr int kLaneEntries = 8;
+// Automatic size of the level-ordered substitution grid: warps for this many levels of
+// 32-row tasks (averaged over the factor), at most kSolveWarps per SM.
+constexpr double kSolveLevelsAhead = 4.0;  // rows with at most this many entries use the per-lane path
 
 // Per-lane progressive solve of a warp's 32 rows (one per lane), for rows with at most
 // kLaneEntries entries held in registers (c: column or -1, v: value).  Every round a
@@ -215,28 +218,52 @@ __device__ __forceinline__ void progressive_rows(int row, int K, const int (&c)[
     }
 }
 
-// Blocking solve of one row (any number of entries), the reference's entry order.
+// Solve of one long row (more than kLaneEntries entries), the reference's entry order.
+// Entries are taken in chunks of 8, software-pipelined two deep: the columns, values and
+// dependency loads of chunk i + 1 are in flight while chunk i is consumed, so a row pays
+// about two memory round trips in total instead of two per chunk.  A dependency not yet
+// published is waited for (bounded) when its chunk is consumed.
+constexpr int kRowChunk = 8;
+
+template <class T>
+__device__ __forceinline__ void load_row_chunk(int off, int K, int k0, int lane, const int* cols, const T* vals,
+                                               const T* dep, int (&c)[kRowChunk], T (&v)[kRowChunk],
+                                               T (&x)[kRowChunk]) {
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u) {
+        const int s = off + (k0 + u) * kWarp + lane;
+        c[u] = (k0 + u < K) ? cols[s] : -1;
+        v[u] = (k0 + u < K) ? vals[s] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u) x[u] = c[u] >= 0 ? ld_relaxed_nb(dep + c[u]) : T(0);
+}
+
+template <class T>
+__device__ __forceinline__ T consume_row_chunk(const int (&c)[kRowChunk], const T (&v)[kRowChunk], T (&x)[kRowChunk],
+                                               T acc, const T* dep, int* status) {
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u) {
+        if (c[u] >= 0) {
+            if (Sentinel<T>::is(x[u])) x[u] = wait_value(dep + c[u], status);
+            acc = fma(-v[u], x[u], acc);
+        }
+    }
+    return acc;
+}
+
 template <class T>
 __device__ __forceinline__ T blocking_row(int off, int K, int lane, const int* cols, const T* vals, T acc, const T* dep,
                                           int* status) {
-    for (int k0 = 0; k0 < K; k0 += 8) {
-        int c[8];
-        T v[8], x[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int s = off + (k0 + u) * kWarp + lane;
-            c[u] = (k0 + u < K) ? cols[s] : -1;
-            v[u] = (k0 + u < K) ? vals[s] : T(0);
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) x[u] = c[u] >= 0 ? ld_relaxed(dep + c[u]) : T(0);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            if (c[u] >= 0) {
-                if (Sentinel<T>::is(x[u])) x[u] = wait_value(dep + c[u], status);
-                acc = fma(-v[u], x[u], acc);
-            }
-        }
+    int cA[kRowChunk], cB[kRowChunk];
+    T vA[kRowChunk], vB[kRowChunk], xA[kRowChunk], xB[kRowChunk];
+    load_row_chunk(off, K, 0, lane, cols, vals, dep, cA, vA, xA);
+    for (int k0 = 0; k0 < K; k0 += 2 * kRowChunk) {
+        const bool hasB = k0 + kRowChunk < K;
+        if (hasB) load_row_chunk(off, K, k0 + kRowChunk, lane, cols, vals, dep, cB, vB, xB);
+        acc = consume_row_chunk(cA, vA, xA, acc, dep, status);
+        if (k0 + 2 * kRowChunk < K) load_row_chunk(off, K, k0 + 2 * kRowChunk, lane, cols, vals, dep, cA, vA, xA);
+        if (hasB) acc = consume_row_chunk(cB, vB, xB, acc, dep, status);
     }
     return acc;
 }
@@ -246,7 +273,7 @@ __device__ __forceinline__ T blocking_row(int off, int K, int lane, const int* c
 // to b (GMRES uses this to normalise the new Krylov vector in the same pass).
 // y must hold the sentinel everywhere on entry; each row publishes its value once.
 template <class T>
-__global__ void __launch_bounds__(kSolveWarps * kWarp)
+__global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
     sptrsv_lower_kernel(PackedTri<T> L, T* b, const double* scale, T* y, unsigned* counter, int* status,
                         const int* gate, int step) {
     if (gate_closed(gate, step)) return;
@@ -290,7 +317,7 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp)
 // is (the caller resets it to the sentinel before the next forward sweep, off the
 // dependency chain: a store into y here doubles this kernel's time).
 template <class T>
-__global__ void __launch_bounds__(kSolveWarps * kWarp)
+__global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
     sptrsv_upper_kernel(PackedTri<T> U, T* y, T* x, unsigned* counter, int* status, const int* gate, int step) {
     if (gate_closed(gate, step)) return;
     const int lane = threadIdx.x & 31;

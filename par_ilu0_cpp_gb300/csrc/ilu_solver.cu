@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <array>
 #include <climits>
 #include <cstring>
@@ -324,7 +325,7 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
         return;
     }
     if (L.ntask == 0) return;
-    sptrsv_lower_kernel<T><<<grid_solve, kSolveThreads, 0, s>>>(L.view<T>(), b, scale, y, counters.get() + 1,
+    sptrsv_lower_kernel<T><<<grid_solve, solve_threads, 0, s>>>(L.view<T>(), b, scale, y, counters.get() + 1,
                                                                 status.get(), gate, step);
 }
 
@@ -335,7 +336,7 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
         return;
     }
     if (U.ntask == 0) return;
-    sptrsv_upper_kernel<T><<<grid_solve, kSolveThreads, 0, s>>>(U.view<T>(), y, x, counters.get() + 2, status.get(),
+    sptrsv_upper_kernel<T><<<grid_solve, solve_threads, 0, s>>>(U.view<T>(), y, x, counters.get() + 2, status.get(),
                                                                 gate, step);
 }
 
@@ -447,10 +448,23 @@ void IluSolver::SetupMatrix() {
     fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
     fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
     im.grid_fact = persistent_grid(ilu_factor_kernel, kFactWarps * kWarp, im.dev.sms);
-    // One CTA of the level-ordered kernel per SM: fewer spinning warps contend less for
-    // L2 and the ready values propagate faster (measured: 1/SM beats full occupancy by
-    // 1.8x on the 128^3 7-point factor).
-    im.grid_solve = im.dev.sms;
+    // Level-ordered kernels: warps draw 32-row tasks in level order and spin on the rows
+    // they depend on, so warps beyond a few levels' worth of tasks only poll values that
+    // are far from ready, and their traffic slows the L2 handoffs of the critical path
+    // (measured: 1 CTA of 8 warps per SM beats full occupancy by 1.8x on the 128^3
+    // 7-point factor; factors with ~10 tasks per level slow down 5x at 1,216 warps).
+    // Automatic: kSolveLevelsAhead levels' worth of warps, spread over the SMs.
+    {
+        const int levels = std::max(1, std::max(im.an.nlev_l, im.an.nlev_u));
+        const int tasks = std::max(im.L.ntask, im.U.ntask);
+        const int cap = im.dev.sms * kSolveWarps;
+        int warps = im.solve_warps > 0 ? im.solve_warps
+                                       : static_cast<int>(std::ceil(kSolveLevelsAhead * static_cast<double>(tasks) / levels));
+        warps = std::max(1, std::min(cap, warps));
+        const int per_cta = std::max(1, std::min(kSolveWarps, ceil_div(warps, im.dev.sms)));
+        im.solve_threads = per_cta * kWarp;
+        im.grid_solve = std::max(1, ceil_div(warps, per_cta));
+    }
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
@@ -649,9 +663,9 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
         launch_band<double, false>(im.LB64, s, b, nullptr, y, counters + 1, status, nullptr, 0);
         launch_band<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
     } else if (im.L.ntask > 0) {
-        sptrsv_lower_kernel<double><<<im.grid_solve, kSolveThreads, 0, s>>>(im.L.view<double>(), b, nullptr, y,
+        sptrsv_lower_kernel<double><<<im.grid_solve, im.solve_threads, 0, s>>>(im.L.view<double>(), b, nullptr, y,
                                                                             counters + 1, status, nullptr, 0);
-        sptrsv_upper_kernel<double><<<im.grid_solve, kSolveThreads, 0, s>>>(im.U.view<double>(), y, d_x, counters + 2,
+        sptrsv_upper_kernel<double><<<im.grid_solve, im.solve_threads, 0, s>>>(im.U.view<double>(), y, d_x, counters + 2,
                                                                             status, nullptr, 0);
     }
     GB_CUDA_CHECK(cudaGetLastError());
