@@ -19,7 +19,7 @@
 namespace gb300 {
 
 constexpr int kFactWarps = 8;    // warps per block of the factorisation kernel
-constexpr int kFactCap = 256;    // row length staged in shared memory per warp
+constexpr int kFactCap = 128;    // row length staged in shared memory per warp
 constexpr int kSolveWarps = 8;   // warps per block of the substitution kernels
 
 // Binary search of c in the sorted s[lo, hi); returns the position or -1.
@@ -62,16 +62,27 @@ __device__ __forceinline__ bool gate_closed(const int* gate, int step) {
 // part in ascending order: l_jk = a_jk / u_kk, then a_jc -= u_kc * l_jk for every column
 // c of row k's strict-upper part that is also in row j's pattern.  Lanes split row k's
 // entries; every entry of row j therefore receives its updates in ascending k, the same
-// sequence of operations as the reference.  Row j is staged in shared memory (global
-// memory for rows longer than kFactCap).  Row k's values are read at L2 (ld.cg) after an
-// acquire on row k's ready flag; row j publishes with fence + release.
-// `shift` (optional) is added to the diagonal before elimination.
+// sequence of operations as the reference.
+//
+// Row j is staged in shared memory together with, for every pivot k, diag[k], the end
+// of row k and u_kk, all loaded in parallel once the pivots' ready flags are acquired;
+// the strict-upper entries of the next pivot row are loaded into registers while the
+// current pivot is eliminated.  The sequential chain per pivot is then one division
+// (one lane) and a shared-memory search-and-update, instead of three dependent global
+// round trips.  Rows longer than kFactCap are eliminated in global memory.  Row k's
+// values are read at L2 (ld.cg) after an acquire on its ready flag; row j publishes
+// with fence + release.  `shift` (optional) is added to the diagonal before elimination.
+constexpr int kFactPre = 2;  // next-pivot entries per lane held in registers
+
 static __global__ void __launch_bounds__(kFactWarps * kWarp)
     ilu_factor_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const int* __restrict__ diag,
                       const int* __restrict__ order, double* lu, const double* __restrict__ shift, int* done,
                       int stamp, unsigned* counter, int* status) {
     __shared__ int s_col[kFactWarps][kFactCap];
     __shared__ double s_val[kFactWarps][kFactCap];
+    __shared__ int s_kd[kFactWarps][kFactCap];
+    __shared__ int s_ke[kFactWarps][kFactCap];
+    __shared__ double s_ukk[kFactWarps][kFactCap];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     int q = draw_ticket(counter, n, lane);
@@ -86,23 +97,62 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
         if (len <= kFactCap) {
             int* scol = s_col[w];
             double* sval = s_val[w];
+            int* skd = s_kd[w];
+            int* ske = s_ke[w];
+            double* sukk = s_ukk[w];
             for (int t = lane; t < len; t += kWarp) {
-                scol[t] = ci[b + t];
+                const int c = ci[b + t];
+                scol[t] = c;
                 double v = lu[b + t];
                 if (shift != nullptr && t == dloc) v += shift[j];
                 sval[t] = v;
+                if (t < dloc) {
+                    const int kd = diag[c];
+                    skd[t] = kd;
+                    ske[t] = rp[c + 1];
+                    sukk[t] = __ldcg(lu + kd);
+                }
             }
             __syncwarp();
+            // strict-upper entries of pivot row t held by this lane: p = kd + 1 + lane + 32 u
+            int nc[kFactPre];
+            double nv[kFactPre];
+            auto load_pivot = [&](int t) {
+                const int p0 = skd[t] + 1 + lane;
+                const int pe = ske[t];
+#pragma unroll
+                for (int u = 0; u < kFactPre; ++u) {
+                    const int p = p0 + u * kWarp;
+                    nc[u] = p < pe ? ci[p] : -1;
+                    nv[u] = p < pe ? __ldcg(lu + p) : 0.0;
+                }
+            };
+            if (dloc > 0) load_pivot(0);
             for (int t = 0; t < dloc; ++t) {
-                const int k = scol[t];
-                const int kd = diag[k];
-                const int ke = rp[k + 1];
-                const double l = sval[t] / __ldcg(lu + kd);
-                __syncwarp();
-                if (lane == 0) sval[t] = l;
-                for (int p = kd + 1 + lane; p < ke; p += kWarp) {
-                    const int c = ci[p];
-                    const int pos = find_sorted(scol, t + 1, len, c);
+                int cc[kFactPre];
+                double cv[kFactPre];
+#pragma unroll
+                for (int u = 0; u < kFactPre; ++u) {
+                    cc[u] = nc[u];
+                    cv[u] = nv[u];
+                }
+                if (t + 1 < dloc) load_pivot(t + 1);
+                double l = 0.0;
+                if (lane == 0) {
+                    l = sval[t] / sukk[t];
+                    sval[t] = l;
+                }
+                l = __shfl_sync(0xffffffffu, l, 0);
+#pragma unroll
+                for (int u = 0; u < kFactPre; ++u) {
+                    if (cc[u] >= 0) {
+                        const int pos = find_sorted(scol, t + 1, len, cc[u]);
+                        if (pos >= 0) sval[pos] = fma(-cv[u], l, sval[pos]);
+                    }
+                }
+                // strict-upper entries beyond the register window (long pivot rows)
+                for (int p = skd[t] + 1 + lane + kFactPre * kWarp; p < ske[t]; p += kWarp) {
+                    const int pos = find_sorted(scol, t + 1, len, ci[p]);
                     if (pos >= 0) sval[pos] = fma(-__ldcg(lu + p), l, sval[pos]);
                 }
                 __syncwarp();
