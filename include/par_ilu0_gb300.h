@@ -60,8 +60,9 @@ enum {
      *   0:   automatic (the level-ordered sync-free kernel);
      *   -1:  the level-ordered sync-free kernel. */
     LLJBASH_ILU_OPT_BLOCK_ROWS = 2,
-    /* warps of the level-ordered substitution kernels (0 = automatic: about four levels'
-     * worth of 32-row tasks, at most 8 per SM).  Takes effect at the next IluSolverSetup. */
+    /* warps of the level-ordered substitution kernels (0 = automatic: about 48 levels'
+     * worth of 32-row tasks, 4 levels' worth when the factor's rows average more than 8
+     * entries per triangle; at most 8 per SM).  Takes effect at the next IluSolverSetup. */
     LLJBASH_ILU_OPT_SOLVE_WARPS = 3
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);

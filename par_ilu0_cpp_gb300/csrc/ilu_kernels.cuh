@@ -216,10 +216,11 @@ struct PackedTri {
     const T* dvals = nullptr;    // [32 * ntask] diagonal (upper factor only)
 };
 
-constexpr int kLaneEntries = 8;
+constexpr int kLaneEntries = 8;  // rows with at most this many entries use the per-lane path
 // Automatic size of the level-ordered substitution grid: warps for this many levels of
 // 32-row tasks (averaged over the factor), at most kSolveWarps per SM.
-constexpr double kSolveLevelsAhead = 4.0;  // rows with at most this many entries use the per-lane path
+constexpr double kSolveLevelsAhead = 48.0;
+constexpr double kSolveLevelsAheadLong = 4.0;  // factors whose rows average > kLaneEntries
 
 // Per-lane progressive solve of a warp's 32 rows (one per lane), for rows with at most
 // kLaneEntries entries held in registers (c: column or -1, v: value).  Every round a

@@ -449,17 +449,21 @@ void IluSolver::SetupMatrix() {
     fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
     im.grid_fact = persistent_grid(ilu_factor_kernel, kFactWarps * kWarp, im.dev.sms);
     // Level-ordered kernels: warps draw 32-row tasks in level order and spin on the rows
-    // they depend on, so warps beyond a few levels' worth of tasks only poll values that
-    // are far from ready, and their traffic slows the L2 handoffs of the critical path
-    // (measured: 1 CTA of 8 warps per SM beats full occupancy by 1.8x on the 128^3
-    // 7-point factor; factors with ~10 tasks per level slow down 5x at 1,216 warps).
-    // Automatic: kSolveLevelsAhead levels' worth of warps, spread over the SMs.
+    // they depend on.  Rows of up to kLaneEntries entries poll in rounds and want many
+    // warps ahead (1,216 warps best on the 128^3 7-point factor, ~64 levels ahead on the
+    // 256^2 5-point one); longer rows spin in blocking waits, and warps far ahead of the
+    // critical path then slow its L2 handoffs (27-point ILU(1), ~10 tasks per level:
+    // 5.7 ms per sweep at ~40 warps, 8.5 ms at 480 or more).  Automatic:
+    // kSolveLevelsAhead (short rows) or kSolveLevelsAheadLong (long rows) levels' worth
+    // of warps, spread over the SMs.
     {
         const int levels = std::max(1, std::max(im.an.nlev_l, im.an.nlev_u));
         const int tasks = std::max(im.L.ntask, im.U.ntask);
         const int cap = im.dev.sms * kSolveWarps;
+        const bool long_rows = n > 0 && (im.nnz - n) > 2ll * kLaneEntries * n;  // mean entries per triangle
+        const double ahead = long_rows ? kSolveLevelsAheadLong : kSolveLevelsAhead;
         int warps = im.solve_warps > 0 ? im.solve_warps
-                                       : static_cast<int>(std::ceil(kSolveLevelsAhead * static_cast<double>(tasks) / levels));
+                                       : static_cast<int>(std::ceil(ahead * static_cast<double>(tasks) / levels));
         warps = std::max(1, std::min(cap, warps));
         const int per_cta = std::max(1, std::min(kSolveWarps, ceil_div(warps, im.dev.sms)));
         im.solve_threads = per_cta * kWarp;
