@@ -290,13 +290,29 @@ __device__ __forceinline__ void load_row_chunk(int off, int K, int k0, int lane,
     for (int u = 0; u < kRowChunk; ++u) x[u] = c[u] >= 0 ? ld_relaxed_nb(dep + c[u]) : T(0);
 }
 
+// Consumes chunk (c, v, x) in entry order.  Entries of the previous level are usually
+// loaded before they are published, so several of a row's values can still hold the
+// sentinel; after a wait ends, every later value of this chunk and of the other loaded
+// chunk (co, xo; `other` = it is loaded) that still holds it is loaded again, all at
+// once, so the row pays about one round trip per wait instead of one per entry.
 template <class T>
 __device__ __forceinline__ T consume_row_chunk(const int (&c)[kRowChunk], const T (&v)[kRowChunk], T (&x)[kRowChunk],
-                                               T acc, const T* dep, int* status) {
+                                               const int (&co)[kRowChunk], T (&xo)[kRowChunk], bool other, T acc,
+                                               const T* dep, int* status) {
 #pragma unroll
     for (int u = 0; u < kRowChunk; ++u) {
         if (c[u] >= 0) {
-            if (Sentinel<T>::is(x[u])) x[u] = wait_value(dep + c[u], status);
+            if (Sentinel<T>::is(x[u])) {
+                x[u] = wait_value(dep + c[u], status);
+#pragma unroll
+                for (int w = u + 1; w < kRowChunk; ++w)
+                    if (c[w] >= 0 && Sentinel<T>::is(x[w])) x[w] = ld_relaxed_nb(dep + c[w]);
+                if (other) {
+#pragma unroll
+                    for (int w = 0; w < kRowChunk; ++w)
+                        if (co[w] >= 0 && Sentinel<T>::is(xo[w])) xo[w] = ld_relaxed_nb(dep + co[w]);
+                }
+            }
             acc = fma(-v[u], x[u], acc);
         }
     }
@@ -311,10 +327,11 @@ __device__ __forceinline__ T blocking_row(int off, int K, int lane, const int* c
     load_row_chunk(off, K, 0, lane, cols, vals, dep, cA, vA, xA);
     for (int k0 = 0; k0 < K; k0 += 2 * kRowChunk) {
         const bool hasB = k0 + kRowChunk < K;
+        const bool hasA2 = k0 + 2 * kRowChunk < K;
         if (hasB) load_row_chunk(off, K, k0 + kRowChunk, lane, cols, vals, dep, cB, vB, xB);
-        acc = consume_row_chunk(cA, vA, xA, acc, dep, status);
-        if (k0 + 2 * kRowChunk < K) load_row_chunk(off, K, k0 + 2 * kRowChunk, lane, cols, vals, dep, cA, vA, xA);
-        if (hasB) acc = consume_row_chunk(cB, vB, xB, acc, dep, status);
+        acc = consume_row_chunk(cA, vA, xA, cB, xB, hasB, acc, dep, status);
+        if (hasA2) load_row_chunk(off, K, k0 + 2 * kRowChunk, lane, cols, vals, dep, cA, vA, xA);
+        if (hasB) acc = consume_row_chunk(cB, vB, xB, cA, xA, hasA2, acc, dep, status);
     }
     return acc;
 }
