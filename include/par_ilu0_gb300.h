@@ -53,11 +53,16 @@ enum {
     /* 1 (default): copy the factors into GetMatrix()->value after Factorize, as the
      * reference's in-place factorisation leaves them; 0: keep them on the device only. */
     LLJBASH_ILU_OPT_COPY_BACK = 1,
-    /* substitution schedule, taking effect at the next IluSolverSetup:
-     *   > 0: contiguous blocks of that many rows, block-pipelined kernel (each CTA keeps a
-     *        block's solution in shared memory and streams its levels in by bulk copies);
-     *        a value type (FP64 / FP32) whose block does not fit keeps the level kernel;
-     *   0:   automatic (the level-ordered sync-free kernel);
+    /* substitution schedule, taking effect at the next IluSolverSetup (results are the
+     * same for every schedule):
+     *   > 0: contiguous blocks of that many rows, block-local kernel (each CTA keeps a
+     *        block's solution in shared memory; dependencies inside a block are handed
+     *        over in shared memory); a value type (FP64 / FP32) whose block does not fit
+     *        in shared memory keeps the level-ordered kernel;
+     *   0:   automatic (default): per value type, block-local with multiples of the
+     *        matrix's plane size when a cost model expects it to beat the level-ordered
+     *        kernel (factors with at most 8 entries per row and triangle), else the
+     *        level-ordered kernel; LLJBASH_IluInfo reports the choice;
      *   -1:  the level-ordered sync-free kernel. */
     LLJBASH_ILU_OPT_BLOCK_ROWS = 2,
     /* warps of the level-ordered substitution kernels (0 = automatic: about 48 levels'
@@ -112,6 +117,9 @@ typedef struct LLJBASH_IluInfo {
     double factor_ms;     /* device time of the last Factorize (factorisation + packing) */
     long long kernel_launches; /* kernels launched by this solver so far */
     int shift_applied;    /* the last Factorize used a diagonal shift (learned or explicit) */
+    int block_rows_fp64;  /* substitution schedule of the FP64 sweeps: rows per block of the
+                           * block-local kernel, 0 = level-ordered kernel */
+    int block_rows_fp32;  /* the same for the FP32 (mixed-precision) sweeps */
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

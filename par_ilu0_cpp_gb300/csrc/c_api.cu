@@ -306,6 +306,8 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->factor_ms = im->last_factor_ms;
     info->kernel_launches = im->launches;
     info->shift_applied = im->shift_applied ? 1 : 0;
+    info->block_rows_fp64 = im->blk64 ? im->LB64.block_rows : 0;
+    info->block_rows_fp32 = im->blk32 ? im->LB32.block_rows : 0;
     return 0;
 }
 

@@ -128,49 +128,19 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int stamp, int* statu
     return false;
 }
 
-// ---- 1-D bulk asynchronous copies (TMA) global -> shared, completed on mbarriers ----
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-// count: expected arrivals per phase, 1 .. 2^20 - 1.
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-// Makes mbarrier initialisation visible to the async proxy.
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-// Orders this thread's earlier generic-proxy accesses to shared memory before later
-// async-proxy (bulk copy) accesses.
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-// Arrival (count 1) that also expects `bytes` (< 2^20) of bulk-copy data.  Relaxed: the
-// arriving thread publishes nothing through the barrier (a release arrival would wait
-// for the thread's outstanding global stores).
-__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.relaxed.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-// bytes: a multiple of 16; both addresses 16-byte aligned.
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for the completion of the phase with parity `parity`; on time-out records
-// status[kStatusTimeout] and returns false.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int* status) {
-    for (long long it = 0; it < kSpinLimit; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    atomicExch(status + kStatusTimeout, 1);
-    return false;
+// L2 prefetch of a contiguous range (cp.async.bulk.prefetch): no destination, no
+// completion to wait for.  `p` 16-byte aligned; the range is rounded to 16-byte pieces
+// issued in chunks of at most 64 KB, split over the calling warp's lanes.
+__device__ __forceinline__ void prefetch_l2_range(const void* p, long long bytes, int lane) {
+    const unsigned long long a = reinterpret_cast<unsigned long long>(p);
+    const long long n16 = bytes >> 4;
+    constexpr long long kChunk16 = 4096;  // 64 KB
+    for (long long c = static_cast<long long>(lane) * kChunk16; c < n16; c += 32 * kChunk16) {
+        const unsigned sz = static_cast<unsigned>((n16 - c < kChunk16 ? n16 - c : kChunk16) << 4);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a + (static_cast<unsigned long long>(c) << 4)),
+                     "r"(sz)
+                     : "memory");
+    }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -50,37 +50,43 @@ inline PackedTri<float> LevelPack::view<float>() const {
     return p;
 }
 
-// One packed triangular factor in the block-pipelined layout (see BandTri) for one
-// value type: the row partition, the slices and their gather instructions.
-struct BandPack {
-    int elem = 0;         // sizeof(T)
+// One packed triangular factor in the block-local layout (see BlockTri) for one value
+// type (`elem` = sizeof(T)): the row partition, the per-block task lists and the packed
+// values.  `fits`: the largest block's solution fits in shared memory.
+struct BlockPack {
+    int elem = 0;
     int nblk = 0;
     int block_rows = 0;   // rows per block (the last block may be shorter)
-    int levels = 0;       // block-internal levels summed over blocks
-    int max_levels = 0;   // largest block-internal level count
-    int stages = 0;
-    unsigned stage_bytes = 0, xs_bytes = 0;
-    size_t smem = 0;      // dynamic shared memory of the kernel
-    long long bytes = 0;  // slice data
+    int ntask = 0;
+    int kmax = 0;         // most entries of a row
+    long long slots = 0;
     int threads = 0;      // CTA size
-    int grid = 0;         // resident CTAs at that footprint
-    DeviceBuffer<int> blk_row, blk_lvl, lvl_bytes, src;
-    DeviceBuffer<long long> blk_off;
-    DeviceBuffer<SliceGather> gat;
-    DeviceBuffer<unsigned char> data;
+    int grid = 0;         // resident CTAs at the kernel's footprint
+    size_t smem = 0;      // dynamic shared memory of the kernel
+    bool fits = false;
+    DeviceBuffer<int> blk_row, blk_task, rows, off, len, codes, src, dsrc;
+    DeviceBuffer<double> v64, d64;
+    DeviceBuffer<float> v32, d32;
 
     template <class T>
-    BandTri<T> view() const {
-        BandTri<T> p;
+    BlockTri<T> view() const {
+        BlockTri<T> p;
         p.nblk = nblk;
-        p.stages = stages;
-        p.stage_bytes = stage_bytes;
-        p.xs_bytes = xs_bytes;
+        p.ntask = ntask;
+        p.slots = slots;
         p.blk_row = blk_row.get();
-        p.blk_lvl = blk_lvl.get();
-        p.blk_off = blk_off.get();
-        p.lvl_bytes = lvl_bytes.get();
-        p.data = data.get();
+        p.blk_task = blk_task.get();
+        p.rows = rows.get();
+        p.off = off.get();
+        p.len = len.get();
+        p.codes = codes.get();
+        if constexpr (sizeof(T) == 8) {
+            p.vals = v64.get();
+            p.dvals = d64.get();
+        } else {
+            p.vals = v32.get();
+            p.dvals = d32.get();
+        }
         return p;
     }
 };
@@ -114,9 +120,9 @@ struct IluSolver::Impl {
     gb300::DeviceBuffer<unsigned> counters;  // ticket counters [0] fact, [1] L, [2] U
     gb300::DeviceBuffer<int> status;         // StatusWord array
     gb300::LevelPack L, U;     // level-ordered warp layout (default)
-    // block-pipelined layout, per value type (used when band64 / band32 is set)
-    gb300::BandPack LB64, UB64, LB32, UB32;
-    bool band64 = false, band32 = false;
+    // block-local layout per value type (used when blk64 / blk32 is set)
+    gb300::BlockPack LB64, UB64, LB32, UB32;
+    bool blk64 = false, blk32 = false;
     bool level_packs = false;  // L and U (level-ordered warp layout) are built
     unsigned setup_gen = 0;    // incremented by every SetupMatrix
     gb300::DeviceBuffer<double> sb64, sy64, sx64;  // Substitute() work vectors

@@ -456,288 +456,240 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
 }
 
 // ---------------------------------------------------------------------------------
-// Block-pipelined substitution (TMA-fed).
+// Block-local substitution (sync-free inside blocks and between them).
 //
 // Rows are cut into contiguous blocks; one CTA solves one block at a time and keeps the
-// block's right-hand side, overwritten in place by its solution, in shared memory.
-// Inside a block rows are grouped by their level in the block-internal dependency DAG
-// (dependencies on rows of other blocks do not count) and a level is solved by the whole
-// CTA between two barriers, one thread per row, so every block-internal dependency is a
-// shared-memory read.  Dependencies on other blocks are read from the global solution
-// with a value-as-flag wait, their loads issued one level ahead.  Blocks are taken from
-// a ticket counter in dependency order (ascending for L, descending for U), so a block
-// only waits for blocks whose CTAs are already running: no deadlock, no co-residency
-// assumption.  When the blocks follow the matrix's planes (a 3-D grid in natural order
-// cut every nx*ny rows) the dependencies between blocks connect equal block-internal
-// levels and the blocks run as a pipeline: the critical path crosses SMs once per
-// block instead of once per level.
+// block's solution in shared memory, at the sentinel until written.  A block's rows are
+// packed like PackedTri: 32-row tasks (one lane per row), rows in the order of the
+// block-internal dependency DAG's levels, entry k of lane l at off[t] + 32 k + l.  Entry
+// codes: >= 0 global column (a row of another block), <= -2 block-local row -2 - code,
+// -1 padding.  Warp w of the CTA takes the block's tasks w, w + nwarps, ... and each lane
+// solves its row with the per-lane progressive rounds of the level-ordered kernel,
+// polling block-local dependencies in shared memory and the others in L2.  There is no
+// barrier inside a block: a dependency handoff between two warps of the CTA costs one
+// shared-memory round trip instead of an L2 one.  With the blocks cut at the matrix's
+// planes (a 3-D grid in natural order, every nx*ny rows) the critical path crosses SMs
+// once per block instead of once per level.
 //
-// The per-level data (a "slice") streams into a ring of shared-memory stages by 1-D
-// bulk copies (cp.async.bulk, completed on one mbarrier per stage), `stages` levels
-// ahead, so no level waits on a global load of its own row data.  Slice layout, every
-// piece 16-byte aligned (Wp = W rounded up to 32):
-//   int4 header {W, K, bytes of the slice `stages` levels later (0: none), Wp}
-//   int  rows[Wp]          global row index of each position
-//   int  codes[K * Wp]     entry k of position p at k * Wp + p: >= 0 global column (other
-//                          block), <= -2 block-local row -2 - code, -1 padding (trailing)
-//   T    vals[K * Wp]
-//   T    diag[Wp]          upper factor only; FP32 stores 1 / u_ii
-// L entries are in ascending and U entries in descending column order: the accumulation
-// order of the reference's substitute_row_L / _U (src/ilu_solver.cpp:687-696, 719-729),
-// so each row performs the same operations in the same order as a sequential sweep.
+// Deadlock freedom: blocks are taken from a ticket counter in dependency order (ascending
+// for L, descending for U), so a block only waits for blocks whose CTAs hold smaller
+// tickets and are running; inside a block each warp takes its tasks in level order, so
+// the earliest unfinished task always has all its dependencies in finished tasks or in
+// lanes of its own warp, which progress independently.  All waits are bounded.
+//
+// The operations of each row are those of the level-ordered kernel (L ascending, U
+// descending, src/ilu_solver.cpp:687-696, 719-729): results are identical.
 // ---------------------------------------------------------------------------------
-constexpr int kBandThreadsMax = 512;
-constexpr int kBandMaxStages = 16;
-constexpr int kBandPre = 4;  // cross-block dependencies per row loaded ahead (registers)
-#ifndef GB_BAND_AHEAD
-#define GB_BAND_AHEAD 3
-#endif
-constexpr int kBandAhead = GB_BAND_AHEAD;  // levels between a prefetch and its use
+constexpr int kBlockWarpsMax = 16;
 
 template <class T>
-struct BandTri {
+struct BlockTri {
     int nblk = 0;
-    int stages = 0;           // ring depth (>= 2)
-    unsigned stage_bytes = 0; // capacity of one ring stage (multiple of 128)
-    unsigned xs_bytes = 0;    // shared bytes of the block vector (multiple of 128)
-    const int* blk_row = nullptr;        // [nblk + 1] first row of each block
-    const int* blk_lvl = nullptr;        // [nblk + 1] first level of each block
-    const long long* blk_off = nullptr;  // [nblk] byte offset of each block's first slice
-    const int* lvl_bytes = nullptr;      // [levels] bytes of each slice
-    const unsigned char* data = nullptr; // slices, level order within block order
+    int ntask = 0;
+    long long slots = 0;
+    const int* blk_row = nullptr;   // [nblk + 1] first row of each block
+    const int* blk_task = nullptr;  // [nblk + 1] first task of each block
+    const int* rows = nullptr;      // [32 * ntask] global row, -1 for padding
+    const int* off = nullptr;       // [ntask]
+    const int* len = nullptr;       // [ntask]
+    const int* codes = nullptr;     // [slots]
+    const T* vals = nullptr;        // [slots]
+    const T* dvals = nullptr;       // [32 * ntask] diagonal (upper factor only; FP32: 1 / u_ii)
 };
 
-// Value-gather instructions of one slice of a block-pipelined factor: the slice's
-// values (nvals) and diagonal (ndiag, right after them) take lu[src[src_off + i]]
-// (0 for src < 0); an FP32 diagonal is stored as its reciprocal.
-struct SliceGather {
-    long long src_off;
-    long long val_off;  // byte offset of vals[0] in the slice data
-    int nvals;
-    int ndiag;
-};
-
-// One warp per slice.
 template <class T>
-__global__ void band_gather_kernel(int levels, const SliceGather* __restrict__ gat, const int* __restrict__ src,
-                                   const double* __restrict__ lu, unsigned char* __restrict__ data) {
-    const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    for (int l = blockIdx.x * wpb + (threadIdx.x >> 5); l < levels; l += gridDim.x * wpb) {
-        const SliceGather gi = gat[l];
-        T* dst = reinterpret_cast<T*>(data + gi.val_off);
-        const int* sp = src + gi.src_off;
-        const int total = gi.nvals + gi.ndiag;
-        for (int i = lane; i < total; i += kWarp) {
-            const int q = sp[i];
-            double v = q >= 0 ? lu[q] : 0.0;
-            if (sizeof(T) == 4 && i >= gi.nvals && q >= 0) v = 1.0 / v;
-            dst[i] = static_cast<T>(v);
-        }
-    }
+__device__ __forceinline__ T ld_volatile_shared(const T* p) {
+    return *reinterpret_cast<const volatile T*>(p);
+}
+template <class T>
+__device__ __forceinline__ void st_volatile_shared(T* p, T v) {
+    *reinterpret_cast<volatile T*>(p) = v;
 }
 
-// The rare slow path (a value not yet published) stays out of line: the hot loop is
-// unrolled several times and must fit the instruction cache.
+// One dependency value of a block-local solve: block-local rows from shared memory,
+// other rows from L2 (relaxed, GPU scope).
 template <class T>
-__device__ __noinline__ T band_wait_value(const T* p, int* status) {
-    return wait_value(p, status);
+__device__ __forceinline__ T block_dep(int code, const T* xs, const T* out) {
+    return code <= -2 ? ld_volatile_shared(xs + (-2 - code)) : ld_relaxed(out + code);
 }
 
-// Issues the loads of this thread's cross-block values of slice `sl` (first position).
-// All shared-memory reads come first: a load with a compiler memory barrier between them
-// would serialise them.
-template <class T>
-__device__ __forceinline__ void band_prefetch(const unsigned char* sl, int p, const T* out, T (&pre)[kBandPre]) {
-    const int4 h = *reinterpret_cast<const int4*>(sl);
-    const int* codes = reinterpret_cast<const int*>(sl + 16) + h.w;
-    int cd[kBandPre];
+// Per-lane progressive solve of one task's rows (at most KM entries each);
+// publishes each row to shared memory and to `out` the moment its last entry is consumed.
+template <class T, bool UPPER, int KM>
+__device__ __forceinline__ void block_progressive(int row, int K, const int (&c)[KM], const T (&v)[KM], T acc, T d,
+                                                  T* xs, int base, T* out, int* status) {
+    int k = 0;
+    bool done = row < 0;
+    long long rounds = 0;
+    while (!__all_sync(0xffffffffu, done)) {
+        if (!done) {
+            T x[KM];
 #pragma unroll
-    for (int k = 0; k < kBandPre; ++k) cd[k] = (p < h.x && k < h.y) ? codes[k * h.w + p] : -1;
+            for (int u = 0; u < KM; ++u)
+                x[u] = (u >= k && u < K && c[u] != -1) ? block_dep(c[u], xs, out) : T(0);
 #pragma unroll
-    for (int k = 0; k < kBandPre; ++k) pre[k] = cd[k] >= 0 ? ld_relaxed_nb(out + cd[k]) : T(0);
-}
-
-// Reloads this thread's prefetched cross-block values of slice `sl` that still hold the
-// sentinel.
-template <class T>
-__device__ __forceinline__ void band_repoll(const unsigned char* sl, int p, const T* out, T (&pre)[kBandPre]) {
-    bool miss = false;
-#pragma unroll
-    for (int k = 0; k < kBandPre; ++k) miss |= Sentinel<T>::is(pre[k]);
-    if (!miss) return;
-    const int4 h = *reinterpret_cast<const int4*>(sl);
-    const int* codes = reinterpret_cast<const int*>(sl + 16) + h.w;
-#pragma unroll
-    for (int k = 0; k < kBandPre; ++k) {
-        if (Sentinel<T>::is(pre[k]) && p < h.x && k < h.y) {
-            const int cd = codes[k * h.w + p];
-            if (cd >= 0) pre[k] = ld_relaxed_nb(out + cd);
-        }
-    }
-}
-
-// Solves the rows of one slice (one block-internal level).  pre: this thread's
-// prefetched cross-block values for its first position (p == threadIdx.x).  The
-// shared-memory operands of a row are loaded together before any global access.
-template <class T, bool UPPER>
-__device__ __forceinline__ void band_solve_slice(const unsigned char* sl, const T (&pre)[kBandPre], T* xs, int base,
-                                                 T* in, bool scaled, T sc, T* out, int* status) {
-    const int4 h = *reinterpret_cast<const int4*>(sl);
-    const int W = h.x, K = h.y, Wp = h.w;
-    const int* rows = reinterpret_cast<const int*>(sl + 16);
-    const int* codes = rows + Wp;
-    const T* vals = reinterpret_cast<const T*>(codes + static_cast<size_t>(K) * Wp);
-    const int tid = threadIdx.x;
-    for (int p = tid; p < W; p += blockDim.x) {
-        const int row = rows[p];
-        int cd[kBandPre];
-        T v[kBandPre], x[kBandPre];
-#pragma unroll
-        for (int k = 0; k < kBandPre; ++k) {
-            cd[k] = k < K ? codes[k * Wp + p] : -1;
-            v[k] = k < K ? vals[k * Wp + p] : T(0);
-        }
-        const T d = UPPER ? vals[static_cast<size_t>(K) * Wp + p] : T(1);
-        T acc = xs[row - base];
-#pragma unroll
-        for (int k = 0; k < kBandPre; ++k) x[k] = cd[k] <= -2 ? xs[-2 - cd[k]] : (p == tid ? pre[k] : T(0));
-        if (!UPPER && scaled) acc = acc * sc;
-        const T acc0 = acc;
-#pragma unroll
-        for (int k = 0; k < kBandPre; ++k) {
-            if (cd[k] >= 0) {
-                if (p != tid) x[k] = ld_relaxed_nb(out + cd[k]);
-                if (Sentinel<T>::is(x[k])) x[k] = band_wait_value(out + cd[k], status);
+            for (int u = 0; u < KM; ++u) {
+                if (k == u && u < K) {
+                    if (c[u] == -1) {
+                        ++k;
+                    } else if (!Sentinel<T>::is(x[u])) {
+                        acc = fma(-v[u], x[u], acc);
+                        ++k;
+                    }
+                }
+            }
+            if (k >= K) {
+                // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
+                const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / d : acc * d) : acc);
+                st_volatile_shared(xs + (row - base), r);
+                st_relaxed(out + row, r);
+                done = true;
             }
         }
-#pragma unroll
-        for (int k = 0; k < kBandPre; ++k)
-            if (cd[k] != -1) acc = fma(-v[k], x[k], acc);
-        for (int k = kBandPre; k < K; ++k) {
-            const int c = codes[k * Wp + p];
-            if (c == -1) break;
-            T xv;
-            if (c <= -2) {
-                xv = xs[-2 - c];
+        if (++rounds >= kSpinLimit) {
+            if (!done) atomicExch(status + kStatusTimeout, 1);
+            break;
+        }
+        if ((rounds & 1023) == 0 && ld_relaxed_int(status + kStatusTimeout) != 0) break;
+    }
+}
+
+// Solve of one long row (more than kLaneEntries entries) of a block-local task, entry by
+// entry in order, each dependency waited for (bounded) when it is reached.
+template <class T>
+__device__ __noinline__ T block_long_row(int off, int K, int lane, const int* codes, const T* vals, T acc,
+                                         const T* xs, const T* out, int* status) {
+    for (int k = 0; k < K; ++k) {
+        const int s = off + k * kWarp + lane;
+        const int c = codes[s];
+        if (c == -1) continue;
+        T x = block_dep(c, xs, out);
+        if (Sentinel<T>::is(x)) {
+            if (c >= 0) {
+                x = wait_value(out + c, status);
             } else {
-                xv = ld_relaxed(out + c);
-                if (Sentinel<T>::is(xv)) xv = band_wait_value(out + c, status);
+                for (long long it = 0; it < kSpinLimit && Sentinel<T>::is(x); ++it) {
+                    x = ld_volatile_shared(xs + (-2 - c));
+                    if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) break;
+                }
+                if (Sentinel<T>::is(x)) {
+                    atomicExch(status + kStatusTimeout, 1);
+                    x = T(0);
+                }
             }
-            acc = fma(-vals[k * Wp + p], xv, acc);
         }
-        // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
-        if (UPPER) acc = sizeof(T) == 8 ? acc / d : acc * d;
-        acc = Sentinel<T>::canon(acc);
-        xs[row - base] = acc;
-        st_relaxed(out + row, acc);
-        if (!UPPER && scaled) in[row] = acc0;
+        acc = fma(-vals[s], x, acc);
     }
+    return acc;
+}
+
+// One lane's share of a block-local task: its row, entries (registers), right-hand side
+// and diagonal.
+template <class T, int KM>
+struct BlockTask {
+    int row, off, K;
+    int c[KM];
+    T v[KM];
+    T b, d;
+};
+
+template <class T, bool UPPER, int KM>
+__device__ __forceinline__ void load_block_task(const BlockTri<T>& P, int t, int lane, const T* in,
+                                                BlockTask<T, KM>& s) {
+    s.row = P.rows[t * kWarp + lane];
+    s.off = P.off[t];
+    s.K = P.len[t];
+#pragma unroll
+    for (int u = 0; u < KM; ++u) {
+        const int sidx = s.off + u * kWarp + lane;
+        s.c[u] = (u < s.K) ? P.codes[sidx] : -1;
+        s.v[u] = (u < s.K) ? P.vals[sidx] : T(0);
+    }
+    s.b = s.row >= 0 ? in[s.row] : T(0);
+    s.d = UPPER ? P.dvals[t * kWarp + lane] : T(1);
+}
+
+template <class T, bool UPPER, int KM>
+__device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const BlockTask<T, KM>& s, int lane,
+                                                 bool scaled, T sc, T* in, T* xs, int base, T* out, int* status) {
+    T acc = scaled ? s.b * sc : s.b;
+    const T acc0 = acc;
+    if (s.K <= KM) {
+        block_progressive<T, UPPER, KM>(s.row, s.K, s.c, s.v, acc, s.d, xs, base, out, status);
+    } else {
+        acc = block_long_row(s.off, s.K, lane, P.codes, P.vals, acc, xs, out, status);
+        if (s.row >= 0) {
+            const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / s.d : acc * s.d) : acc);
+            st_volatile_shared(xs + (s.row - base), r);
+            st_relaxed(out + s.row, r);
+        }
+    }
+    // the normalised Krylov vector is written back after the row is published
+    if (scaled && s.row >= 0) in[s.row] = acc0;
 }
 
 // Forward (UPPER = false): out = L^{-1} (scale * in); with `scale`, in is rescaled in
 //   place (GMRES normalises its new Krylov vector in the same pass).
 // Backward (UPPER = true): out = U^{-1} in (in is left as it is).
-// out must hold the sentinel for every row on entry.  Any block size (a multiple of 32,
-// at most kBandThreadsMax); dynamic shared memory: xs_bytes + stages * stage_bytes, and
-// stages >= kBandAhead + 2.
-//
-// Per level: solve the slice's rows, one CTA barrier, then issue the loads of the
-// cross-block values of the slice kBandAhead levels later.  A block thereby trails the
-// block it depends on by about one L2 round trip, and once the pipeline has filled its
-// levels do not wait on global memory.  Thread 0 alone handles the slice ring: at the
-// start of a level it refills the stage freed by the previous barrier and waits for the
-// slice the next prefetch reads, so the barrier publishes that slice to every thread.
-// The level loop is unrolled kBandAhead times so that every prefetch set stays in its
-// own registers (a register move would wait for the load).
-template <class T, bool UPPER>
-__global__ void __launch_bounds__(kBandThreadsMax, 1)
-    sptrsv_band_kernel(BandTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
-                       const int* gate, int step) {
+// out must hold the sentinel for every row on entry.  Dynamic shared memory: the
+// largest block's rows x sizeof(T).
+// KM: entries per row held in registers (4 when no row of the factor has more, else
+// kLaneEntries); longer rows take the entry-by-entry path.
+template <class T, bool UPPER, int KM>
+__global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
+    sptrsv_block_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
+                        const int* gate, int step) {
     if (gate_closed(gate, step)) return;
-    extern __shared__ __align__(128) unsigned char band_smem[];
-    __shared__ __align__(8) unsigned long long bars[kBandMaxStages + 1];
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    T* xs = reinterpret_cast<T*>(blk_smem);
     __shared__ int s_ticket;
-    T* xs = reinterpret_cast<T*>(band_smem);
-    unsigned char* ring = band_smem + P.xs_bytes;
-    const unsigned D = static_cast<unsigned>(P.stages);
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        for (unsigned i = 0; i <= D; ++i) mbar_init(&bars[i], 1u);
-        fence_mbar_init();
-    }
-    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
     const bool scaled = !UPPER && scale != nullptr;
     const T sc = scaled ? static_cast<T>(*scale) : T(1);
-    unsigned g0 = 0;     // ring slots consumed by this CTA so far (phase bookkeeping)
-    unsigned xpar = 0;   // phase parity of the block-vector barrier
-    auto slice = [&](unsigned g) { return ring + static_cast<size_t>(g % D) * P.stage_bytes; };
-    // thread 0 only
-    auto wait_slice = [&](unsigned g) { mbar_wait(&bars[g % D], (g / D) & 1u, status); };
-    auto issue_slice = [&](unsigned g, unsigned nb, long long& off) {
-        mbar_arrive_expect_tx(&bars[g % D], nb);
-        bulk_copy_g2s(ring + static_cast<size_t>(g % D) * P.stage_bytes, P.data + off, nb, &bars[g % D]);
-        off += nb;
-    };
     for (int tk = draw_block_ticket(counter, P.nblk, &s_ticket); tk < P.nblk;
          tk = draw_block_ticket(counter, P.nblk, &s_ticket)) {
-        const int c = UPPER ? P.nblk - 1 - tk : tk;
-        const int base = P.blk_row[c];
-        const int cnt = P.blk_row[c + 1] - base;
-        const int lv0 = P.blk_lvl[c];
-        const int nl = P.blk_lvl[c + 1] - lv0;
-        const T* src = in + base;
-        const unsigned xb =
-            (reinterpret_cast<uintptr_t>(src) & 15u) == 0 ? (static_cast<unsigned>(cnt) * sizeof(T)) & ~15u : 0u;
-        long long issue_off = 0;
-        unsigned nb_prev = 0;  // thread 0: bytes of the slice that refills the stage freed last
-        if (tid == 0) {
-            if (xb) {
-                mbar_arrive_expect_tx(&bars[D], xb);
-                bulk_copy_g2s(xs, src, xb, &bars[D]);
-            }
-            issue_off = P.blk_off[c];
-            const int first = min(static_cast<int>(D), nl);
-            for (int i = 0; i < first; ++i)
-                issue_slice(g0 + static_cast<unsigned>(i), static_cast<unsigned>(P.lvl_bytes[lv0 + i]), issue_off);
-            for (int i = 0; i < kBandAhead && i < nl; ++i) wait_slice(g0 + static_cast<unsigned>(i));
-            if (xb) mbar_wait(&bars[D], xpar, status);
+        const int blk = UPPER ? P.nblk - 1 - tk : tk;
+        const int base = P.blk_row[blk];
+        const int cnt = P.blk_row[blk + 1] - base;
+        const int t1 = P.blk_task[blk + 1];
+        if (threadIdx.x < kWarp) {
+            // the block's packed task data and right-hand side are streamed into L2 now:
+            // between sweeps the Krylov vectors evict them, and the warps' own loads run
+            // only two tasks ahead
+            const int t0 = P.blk_task[blk];
+            const long long s0 = P.off[t0];
+            const long long s1 = t1 < P.ntask ? P.off[t1] : P.slots;
+            prefetch_l2_range(P.codes + s0, (s1 - s0) * 4, lane);
+            prefetch_l2_range(P.vals + s0, (s1 - s0) * static_cast<long long>(sizeof(T)), lane);
+            prefetch_l2_range(P.rows + static_cast<long long>(t0) * kWarp, (t1 - t0) * 128ll, lane);
+            if (UPPER)
+                prefetch_l2_range(P.dvals + static_cast<long long>(t0) * kWarp,
+                                  (t1 - t0) * static_cast<long long>(kWarp * sizeof(T)), lane);
+            // right-hand side rows [base, base + cnt): whole 16-byte pieces inside the range
+            const unsigned long long ib = reinterpret_cast<unsigned long long>(in + base);
+            const unsigned long long ie = reinterpret_cast<unsigned long long>(in + base + cnt);
+            const unsigned long long a16 = (ib + 15) & ~15ull;
+            if (ie > a16) prefetch_l2_range(reinterpret_cast<const void*>(a16), static_cast<long long>((ie - a16) & ~15ull), lane);
         }
-        if (xb) xpar ^= 1u;
-        for (int i = static_cast<int>(xb / sizeof(T)) + tid; i < cnt; i += blockDim.x) xs[i] = src[i];
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
         __syncthreads();
-        T pre[kBandAhead][kBandPre];
-#pragma unroll
-        for (int j = 0; j < kBandAhead; ++j)
-            if (j < nl) band_prefetch<T>(slice(g0 + j), tid, out, pre[j]);
-        for (int l = 0; l < nl; l += kBandAhead) {
-#pragma unroll
-            for (int j = 0; j < kBandAhead; ++j) {
-                const int lj = l + j;
-                if (lj < nl) {
-                    const unsigned g = g0 + static_cast<unsigned>(lj);
-                    if (tid == 0) {
-                        // the barrier that ended level lj - 1 freed its stage: refill it
-                        if (nb_prev != 0) issue_slice(g + D - 1, nb_prev, issue_off);
-                        // the prefetch after this level's barrier reads slice lj + kBandAhead
-                        if (lj + kBandAhead < nl) wait_slice(g + kBandAhead);
-                    }
-                    const unsigned char* sl = slice(g);
-                    band_solve_slice<T, UPPER>(sl, pre[j], xs, base, in, scaled, sc, out, status);
-                    if (tid == 0) nb_prev = static_cast<unsigned>(reinterpret_cast<const int4*>(sl)->z);
-                    __syncthreads();
-                    if (lj + kBandAhead < nl) band_prefetch<T>(slice(g + kBandAhead), tid, out, pre[j]);
-                    // values of the next level that were not yet published when prefetched
-                    // (the producing block runs just ahead): load them again now, a level
-                    // before they are needed, instead of waiting a round trip then
-                    if (kBandAhead > 1 && lj + 1 < nl) band_repoll<T>(slice(g + 1), tid, out, pre[(j + 1) % kBandAhead]);
-                }
+        // Task data is loaded two tasks ahead (into two register sets, the loop unrolled by
+        // two so that neither set is ever moved): the packed factor comes from HBM, a
+        // round trip longer than the two levels one task ahead would cover.
+        BlockTask<T, KM> A, B2;
+        int t = P.blk_task[blk] + w;
+        if (t < t1) load_block_task<T, UPPER, KM>(P, t, lane, in, A);
+        if (t + nw < t1) load_block_task<T, UPPER, KM>(P, t + nw, lane, in, B2);
+        for (; t < t1; t += 2 * nw) {
+            solve_block_task<T, UPPER, KM>(P, A, lane, scaled, sc, in, xs, base, out, status);
+            if (t + 2 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 2 * nw, lane, in, A);
+            if (t + nw < t1) {
+                solve_block_task<T, UPPER, KM>(P, B2, lane, scaled, sc, in, xs, base, out, status);
+                if (t + 3 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 3 * nw, lane, in, B2);
             }
         }
-        g0 += static_cast<unsigned>(nl);
-        // this block's generic writes of xs come before the next block's bulk copy into it
-        // (once per block: a proxy fence waits for the thread's outstanding memory operations)
-        fence_proxy_async_smem();
     }
 }
 

@@ -127,174 +127,251 @@ static int block_levels(int lo, int hi, bool lower, const int* rp, const int* ci
     return nlev;
 }
 
-static unsigned round_up(unsigned long long v, unsigned a) { return static_cast<unsigned>((v + a - 1) / a * a); }
+// ---- choice of the substitution schedule ----------------------------------------
+// Model constants, measured on GB300 with the 128^3 7-point and 256^2 5-point factors:
+// one block-internal level of the block-local kernel, one cross-block handoff, and the
+// level-ordered kernel's cost per level (a fixed handoff plus a term per row).
+constexpr double kModelBlockLevelUs = 0.35;
+constexpr double kModelBlockHopUs = 2.0;
+constexpr double kModelLevelUs = 0.6;
+constexpr double kModelLevelRowUs = 9e-5;
 
-// Bytes of one slice of W rows with at most K entries (see BandTri).
-static unsigned long long slice_bytes(int W, int K, int elem, bool lower) {
-    const unsigned long long Wp = round_up(static_cast<unsigned long long>(W), kWarp);
-    return 16 + 4 * Wp * (1 + static_cast<unsigned long long>(K)) +
-           static_cast<unsigned long long>(elem) * (static_cast<unsigned long long>(K) * Wp + (lower ? 0 : Wp));
+// Plane size of a matrix from a structured grid in natural order: the most frequent
+// offset r - c of the strict-lower entries among those at least half the largest one
+// (nx * ny for a 3-D grid, nx for a 2-D one), provided it occurs in a quarter of the
+// rows; 0 otherwise.
+static int plane_offset(int n, const int* rp, const int* ci, const std::vector<int>& diag) {
+    int max_off = 0;
+    for (int r = 0; r < n; ++r)
+        if (diag[r] > rp[r]) max_off = std::max(max_off, r - ci[rp[r]]);
+    if (max_off <= 0) return 0;
+    const int lo = (max_off + 1) / 2;
+    std::vector<int> count(static_cast<size_t>(max_off - lo) + 1, 0);
+    for (int r = 0; r < n; ++r)
+        for (int p = rp[r]; p < diag[r]; ++p)
+            if (r - ci[p] >= lo) ++count[r - ci[p] - lo];
+    int best = 0, best_cnt = 0;
+    for (int o = lo; o <= max_off; ++o) {
+        if (count[o - lo] > best_cnt) {
+            best_cnt = count[o - lo];
+            best = o;
+        }
+    }
+    return 4ll * best_cnt >= n ? best : 0;
 }
 
-// Host construction of a block-pipelined packed factor for values of `elem` bytes
-// (see BandTri).  Returns false (and builds nothing) when a ring of kBandAhead + 2 slices does not
-// fit next to the block vector in `smem_budget` bytes of shared memory.
-static bool build_band_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
-                            int block_rows, int elem, size_t smem_budget, BandPack& P, cudaStream_t s) {
+// Modelled critical path (us) of the forward sweep with the block-local kernel and
+// blocks of B rows: every row finishes one block-level after its latest dependency,
+// plus a handoff when that dependency lies in another block.
+static double block_schedule_model(int n, const int* rp, const int* ci, const std::vector<int>& diag, int B) {
+    std::vector<double> t(static_cast<size_t>(n));
+    double T = 0.0;
+    for (int r = 0; r < n; ++r) {
+        double m = 0.0;
+        const int br = r / B;
+        for (int p = rp[r]; p < diag[r]; ++p) {
+            const int c = ci[p];
+            m = std::max(m, t[c] + (c / B == br ? 0.0 : kModelBlockHopUs));
+        }
+        t[r] = m + kModelBlockLevelUs;
+        T = std::max(T, t[r]);
+    }
+    return T;
+}
+
+// Block size of the block-local schedule for values of `elem` bytes, or 0 when the
+// level-ordered kernel is expected to be faster.  Candidates are multiples of the plane
+// size that fit in shared memory; rows with more than kLaneEntries entries take the
+// block kernel's slow path, so such factors keep the level kernel.
+static int choose_block_rows(int n, const int* rp, const int* ci, const std::vector<int>& diag, int nlev, int elem,
+                             size_t smem_budget) {
+    if (n <= 0) return 0;
+    int kmax = 0;
+    for (int r = 0; r < n; ++r) kmax = std::max({kmax, diag[r] - rp[r], rp[r + 1] - diag[r] - 1});
+    if (kmax > kLaneEntries) return 0;
+    const long long max_rows = static_cast<long long>(smem_budget / static_cast<size_t>(elem));
+    const double level_us =
+        std::max(1, nlev) * (kModelLevelUs + kModelLevelRowUs * static_cast<double>(n) / std::max(1, nlev));
+    if (n <= max_rows) return block_schedule_model(n, rp, ci, diag, n) < level_us ? n : 0;
+    const int P = plane_offset(n, rp, ci, diag);
+    if (P <= 0) return 0;
+    int best = 0;
+    double best_us = level_us;
+    for (long long B = P; B <= max_rows && B < n; B *= 2) {
+        const double us = block_schedule_model(n, rp, ci, diag, static_cast<int>(B));
+        if (us < best_us) {
+            best_us = us;
+            best = static_cast<int>(B);
+        }
+    }
+    return best;
+}
+
+// Host construction of a block-local packed factor (see BlockTri): contiguous blocks of
+// `block_rows` rows; inside a block the rows in block-internal level order (ascending row
+// index inside a level), 32 to a task, tasks never crossing a block.  lower: entries
+// [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1]) descending plus the
+// diagonal position.  A value type is marked as fitting when the largest block's
+// solution fits in `smem_budget` bytes of shared memory.
+static void build_block_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
+                             int block_rows, int elem, size_t smem_budget, BlockPack& P, cudaStream_t s) {
     const int S = std::max(1, std::min(block_rows, std::max(n, 1)));
     const int nblk = n > 0 ? ceil_div(n, S) : 0;
     auto ebeg = [&](int r) { return lower ? rp[r] : diag[r] + 1; };
     auto eend = [&](int r) { return lower ? diag[r] : rp[r + 1]; };
-    // pass 1: levels of every block, rows grouped by level, slice sizes
-    std::vector<int> blk_row(static_cast<size_t>(nblk) + 1), blk_lvl(static_cast<size_t>(nblk) + 1, 0);
-    std::vector<int> lvl_start(1, 0), lvl_K, lrows;
-    lrows.reserve(static_cast<size_t>(n));
-    std::vector<int> depth(static_cast<size_t>(S)), cnt;
-    int max_levels = 0;
+    std::vector<int> blk_row(static_cast<size_t>(nblk) + 1), blk_task(static_cast<size_t>(nblk) + 1, 0);
+    std::vector<int> rows, off, len, dsrc;
+    std::vector<int> depth(static_cast<size_t>(S)), cnt, ord;
+    long long slots = 0;
+    int max_level_tasks = 1;
     for (int c = 0; c < nblk; ++c) {
         const int lo = c * S;
         const int hi = std::min(n, lo + S);
         blk_row[c] = lo;
+        blk_task[c] = static_cast<int>(off.size());
         const int nlev = block_levels(lo, hi, lower, rp, ci, diag, depth);
-        max_levels = std::max(max_levels, nlev);
         cnt.assign(static_cast<size_t>(nlev) + 1, 0);
         for (int r = lo; r < hi; ++r) ++cnt[depth[r - lo] + 1];
-        for (int l = 0; l < nlev; ++l) cnt[l + 1] += cnt[l];
-        const size_t base = lrows.size();
-        lrows.resize(base + static_cast<size_t>(hi - lo));
-        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-        for (int r = lo; r < hi; ++r) lrows[base + fill[depth[r - lo]]++] = r;
         for (int l = 0; l < nlev; ++l) {
-            int K = 0;
-            for (int q = cnt[l]; q < cnt[l + 1]; ++q) {
-                const int r = lrows[base + q];
-                K = std::max(K, eend(r) - ebeg(r));
-            }
-            lvl_K.push_back(K);
-            lvl_start.push_back(static_cast<int>(base) + cnt[l + 1]);
+            max_level_tasks = std::max(max_level_tasks, ceil_div(cnt[l + 1], kWarp));
+            cnt[l + 1] += cnt[l];
         }
-        blk_lvl[c + 1] = blk_lvl[c] + nlev;
+        ord.assign(static_cast<size_t>(hi - lo), 0);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int r = lo; r < hi; ++r) ord[fill[depth[r - lo]]++] = r;
+        // tasks never straddle two levels: a task's rows are independent of each other,
+        // so a warp finishes its task in one level-time
+        for (int l = 0; l < nlev; ++l) {
+            for (int q0 = cnt[l]; q0 < cnt[l + 1]; q0 += kWarp) {
+                int K = 0;
+                for (int u = 0; u < kWarp; ++u) {
+                    const int q = q0 + u;
+                    if (q < cnt[l + 1]) {
+                        const int r = ord[q];
+                        rows.push_back(r);
+                        K = std::max(K, eend(r) - ebeg(r));
+                        if (!lower) dsrc.push_back(diag[r]);
+                    } else {
+                        rows.push_back(-1);
+                        if (!lower) dsrc.push_back(-1);
+                    }
+                }
+                off.push_back(static_cast<int>(slots));
+                len.push_back(K);
+                slots += static_cast<long long>(K) * kWarp;
+                if (slots > INT_MAX) throw std::runtime_error("triangular factor too large for 32-bit slot offsets");
+            }
+        }
     }
     blk_row[nblk] = n;
-    const int levels = blk_lvl[nblk];
-    std::vector<int> lvl_bytes(static_cast<size_t>(levels));
-    unsigned long long max_bytes = 16, total = 0;
-    int max_width = 1;
-    for (int l = 0; l < levels; ++l) {
-        max_width = std::max(max_width, lvl_start[l + 1] - lvl_start[l]);
-        const unsigned long long b = slice_bytes(lvl_start[l + 1] - lvl_start[l], lvl_K[l], elem, lower);
-        if (b > (1ull << 30)) return false;
-        lvl_bytes[l] = static_cast<int>(b);
-        max_bytes = std::max(max_bytes, b);
-        total += b;
-    }
-    const unsigned stage_bytes = round_up(max_bytes, 128);
-    const unsigned xs_bytes = round_up(static_cast<unsigned long long>(S) * elem, 128);
-    if (xs_bytes + static_cast<unsigned long long>(kBandAhead + 2) * stage_bytes > smem_budget) return false;
-    const int stages = static_cast<int>(std::min<unsigned long long>(kBandMaxStages, (smem_budget - xs_bytes) / stage_bytes));
-    // pass 2: slice images and gather instructions
-    std::vector<unsigned char> img(static_cast<size_t>(total));
-    std::vector<long long> blk_off(static_cast<size_t>(nblk));
-    std::vector<SliceGather> gat(static_cast<size_t>(levels));
-    std::vector<int> src;
-    long long off = 0;
-    for (int c = 0; c < nblk; ++c) {
-        blk_off[c] = off;
-        const int lo = blk_row[c];
-        const int hi = blk_row[c + 1];
-        const int l0 = blk_lvl[c];
-        const int l1 = blk_lvl[c + 1];
-        for (int L = l0; L < l1; ++L) {
-            const int W = lvl_start[L + 1] - lvl_start[L];
-            const int K = lvl_K[L];
-            const int Wp = static_cast<int>(round_up(static_cast<unsigned long long>(W), kWarp));
-            unsigned char* sl = img.data() + off;
-            const int hdr[4] = {W, K, L + stages < l1 ? lvl_bytes[L + stages] : 0, Wp};
-            std::memcpy(sl, hdr, sizeof(hdr));
-            int* rows = reinterpret_cast<int*>(sl + 16);
-            int* codes = rows + Wp;
-            for (int p = 0; p < Wp; ++p) rows[p] = p < W ? lrows[lvl_start[L] + p] : -1;
-            std::fill(codes, codes + static_cast<size_t>(K) * Wp, -1);
-            SliceGather& gi = gat[L];
-            gi.src_off = static_cast<long long>(src.size());
-            gi.val_off = off + 16 + 4ll * Wp * (1 + K);
-            gi.nvals = K * Wp;
-            gi.ndiag = lower ? 0 : Wp;
-            const size_t s0 = src.size();
-            src.resize(s0 + static_cast<size_t>(gi.nvals + gi.ndiag), -1);
-            for (int p = 0; p < W; ++p) {
-                const int r = rows[p];
-                int k = 0;
-                auto put = [&](int q) {
-                    const int col = ci[q];
-                    codes[static_cast<size_t>(k) * Wp + p] = (col >= lo && col < hi) ? -2 - (col - lo) : col;
-                    src[s0 + static_cast<size_t>(k) * Wp + p] = q;
-                    ++k;
-                };
-                if (lower) {
-                    for (int q = rp[r]; q < diag[r]; ++q) put(q);
-                } else {
-                    for (int q = rp[r + 1] - 1; q > diag[r]; --q) put(q);
-                    src[s0 + static_cast<size_t>(gi.nvals) + p] = diag[r];
-                }
+    blk_task[nblk] = static_cast<int>(off.size());
+    const int ntask = static_cast<int>(off.size());
+    std::vector<int> codes(static_cast<size_t>(slots), -1), src(static_cast<size_t>(slots), -1);
+    for (int t = 0; t < ntask; ++t) {
+        for (int l = 0; l < kWarp; ++l) {
+            const int r = rows[static_cast<size_t>(t) * kWarp + l];
+            if (r < 0) continue;
+            const int lo = (r / S) * S;
+            const int hi = std::min(n, lo + S);
+            int k = 0;
+            auto put = [&](int p) {
+                const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
+                const int col = ci[p];
+                codes[sidx] = (col >= lo && col < hi) ? -2 - (col - lo) : col;
+                src[sidx] = p;
+                ++k;
+            };
+            if (lower) {
+                for (int p = rp[r]; p < diag[r]; ++p) put(p);
+            } else {
+                for (int p = rp[r + 1] - 1; p > diag[r]; --p) put(p);
             }
-            off += lvl_bytes[L];
         }
     }
-    if (src.size() > static_cast<size_t>(INT_MAX)) throw std::runtime_error("triangular factor too large");
-    P.elem = elem;
     P.nblk = nblk;
     P.block_rows = S;
-    P.levels = levels;
-    P.max_levels = max_levels;
-    P.stages = stages;
-    P.stage_bytes = stage_bytes;
-    P.xs_bytes = xs_bytes;
-    P.smem = static_cast<size_t>(xs_bytes) + static_cast<size_t>(stages) * stage_bytes;
-    // one thread per row of the widest level (whole warps, 64 .. kBandThreadsMax)
-    P.threads = std::max(64, std::min(kBandThreadsMax, static_cast<int>(round_up(max_width, kWarp))));
-    P.bytes = static_cast<long long>(total);
+    P.ntask = ntask;
+    P.kmax = len.empty() ? 0 : *std::max_element(len.begin(), len.end());
+    P.slots = slots;
+    // two tasks in flight per level of the widest block level, 4 .. kBlockWarpsMax warps
+    P.threads = kWarp * std::max(4, std::min(kBlockWarpsMax, 2 * max_level_tasks));
+    P.elem = elem;
+    P.smem = static_cast<size_t>(elem) * static_cast<size_t>(S);
+    P.fits = P.smem <= smem_budget;
     P.blk_row.upload(blk_row.data(), blk_row.size(), s);
-    P.blk_lvl.upload(blk_lvl.data(), blk_lvl.size(), s);
-    P.blk_off.upload(blk_off.data(), blk_off.size(), s);
-    P.lvl_bytes.upload(lvl_bytes.data(), lvl_bytes.size(), s);
+    P.blk_task.upload(blk_task.data(), blk_task.size(), s);
+    P.rows.upload(rows.data(), rows.size(), s);
+    P.off.upload(off.data(), off.size(), s);
+    P.len.upload(len.data(), len.size(), s);
+    P.codes.upload(codes.data(), codes.size(), s);
     P.src.upload(src.data(), src.size(), s);
-    P.gat.upload(gat.data(), gat.size(), s);
-    P.data.upload(img.data(), img.size(), s);
+    if (!lower) P.dsrc.upload(dsrc.data(), dsrc.size(), s);
+    if (elem == 8) {
+        P.v64.reserve(static_cast<size_t>(slots));
+        if (!lower) P.d64.reserve(rows.size());
+    } else {
+        P.v32.reserve(static_cast<size_t>(slots));
+        if (!lower) P.d32.reserve(rows.size());
+    }
     // host vectors must outlive the asynchronous copies
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
-    return true;
 }
 
-static void gather_band(const BandPack& P, const double* lu, cudaStream_t s, int sms) {
-    if (P.levels == 0) return;
+static void gather_block(const BlockPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
     const int threads = 256;
-    const int grid = static_cast<int>(std::max(1, std::min(ceil_div(P.levels, threads / kWarp), 8 * sms)));
-    if (P.elem == 8)
-        band_gather_kernel<double><<<grid, threads, 0, s>>>(P.levels, P.gat.get(), P.src.get(), lu, P.data.get());
-    else
-        band_gather_kernel<float><<<grid, threads, 0, s>>>(P.levels, P.gat.get(), P.src.get(), lu, P.data.get());
+    auto grid_for = [&](long long count) {
+        long long g = ceil_div<long long>(count, threads);
+        return static_cast<int>(std::max<long long>(1, std::min<long long>(g, 8LL * sms)));
+    };
+    if (P.slots > 0) {
+        if (P.elem == 8)
+            pack_gather_kernel<double><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v64.get());
+        else
+            pack_gather_kernel<float><<<grid_for(P.slots), threads, 0, s>>>(P.slots, P.src.get(), lu, P.v32.get());
+    }
+    if (!lower && P.ntask > 0) {
+        const long long nd = static_cast<long long>(P.ntask) * kWarp;
+        if (P.elem == 8)
+            pack_gather_kernel<double><<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d64.get());
+        else
+            pack_gather_recip_kernel<<<grid_for(nd), threads, 0, s>>>(nd, P.dsrc.get(), lu, P.d32.get());
+    }
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
-// Raises the kernel's dynamic shared-memory limit to the pack's footprint and records
-// the number of resident CTAs.
-template <class T, bool UPPER>
-static void configure_band(BandPack& P, int sms) {
+// Raises the kernel's dynamic shared-memory limit to the pack's footprint for type T and
+// records the number of resident CTAs.
+template <class T, bool UPPER, int KM>
+static void configure_block_km(BlockPack& P, int sms) {
     const int bytes = static_cast<int>(std::max<size_t>(P.smem, 16));
-    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_band_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, UPPER, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       bytes));
     int per_sm = 0;
-    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_band_kernel<T, UPPER>, P.threads,
+    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_block_kernel<T, UPPER, KM>, P.threads,
                                                                static_cast<size_t>(bytes)));
     P.grid = std::max(1, per_sm) * sms;
 }
 
 template <class T, bool UPPER>
-static void launch_band(const BandPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
-                        int* status, const int* gate, int step) {
+static void configure_block(BlockPack& P, int sms) {
+    if (P.kmax <= 4)
+        configure_block_km<T, UPPER, 4>(P, sms);
+    else
+        configure_block_km<T, UPPER, kLaneEntries>(P, sms);
+}
+
+template <class T, bool UPPER>
+static void launch_block(const BlockPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
+                         int* status, const int* gate, int step) {
     if (P.nblk == 0) return;
-    sptrsv_band_kernel<T, UPPER><<<std::min(P.grid, P.nblk), P.threads, P.smem, s>>>(
-        P.view<T>(), in, scale, out, counter, status, gate, step);
+    const int grid = std::min(P.grid, P.nblk);
+    const size_t smem = P.smem;
+    if (P.kmax <= 4)
+        sptrsv_block_kernel<T, UPPER, 4><<<grid, P.threads, smem, s>>>(P.view<T>(), in, scale, out, counter, status,
+                                                                       gate, step);
+    else
+        sptrsv_block_kernel<T, UPPER, kLaneEntries><<<grid, P.threads, smem, s>>>(P.view<T>(), in, scale, out, counter,
+                                                                                  status, gate, step);
 }
 
 template <class T>
@@ -320,8 +397,9 @@ IluSolver::Impl::~Impl() {
 
 template <class T>
 void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const {
-    if (sizeof(T) == 8 ? band64 : band32) {
-        launch_band<T, false>(sizeof(T) == 8 ? LB64 : LB32, s, b, scale, y, counters.get() + 1, status.get(), gate, step);
+    if (sizeof(T) == 8 ? blk64 : blk32) {
+        launch_block<T, false>(sizeof(T) == 8 ? LB64 : LB32, s, b, scale, y, counters.get() + 1, status.get(), gate,
+                               step);
         return;
     }
     if (L.ntask == 0) return;
@@ -331,8 +409,9 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
 
 template <class T>
 void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const {
-    if (sizeof(T) == 8 ? band64 : band32) {
-        launch_band<T, true>(sizeof(T) == 8 ? UB64 : UB32, s, y, nullptr, x, counters.get() + 2, status.get(), gate, step);
+    if (sizeof(T) == 8 ? blk64 : blk32) {
+        launch_block<T, true>(sizeof(T) == 8 ? UB64 : UB32, s, y, nullptr, x, counters.get() + 2, status.get(), gate,
+                              step);
         return;
     }
     if (U.ntask == 0) return;
@@ -342,7 +421,7 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
 
 template <class T>
 const void* IluSolver::Impl::subst_key() const {
-    if (sizeof(T) == 8 ? band64 : band32) return (sizeof(T) == 8 ? LB64 : LB32).data.get();
+    if (sizeof(T) == 8 ? blk64 : blk32) return (sizeof(T) == 8 ? LB64 : LB32).codes.get();
     return L.cols.get();
 }
 
@@ -417,25 +496,33 @@ void IluSolver::SetupMatrix() {
     im.status.reserve(kStatusWords);
     GB_CUDA_CHECK(cudaMemsetAsync(im.status.get(), 0, sizeof(int) * kStatusWords, s));
     ++im.setup_gen;
-    im.band64 = im.band32 = false;
-    if (im.block_rows > 0) {
-        // explicit block size; a value type whose block vector and slice ring do not fit
-        // in shared memory keeps the level-ordered kernel
+    im.blk64 = im.blk32 = false;
+    if (im.block_rows >= 0) {
+        // block-local schedule: an explicit block size, or (0) the one the cost model
+        // picks per value type; a type whose block does not fit in shared memory, or for
+        // which the model prefers the level-ordered kernel, keeps the level kernel
         const size_t budget = static_cast<size_t>(std::max(0, im.dev.smem_optin - 1024));
-        im.band64 = build_band_pack(n, rp, ci, im.an.diag, true, im.block_rows, 8, budget, im.LB64, s) &&
-                    build_band_pack(n, rp, ci, im.an.diag, false, im.block_rows, 8, budget, im.UB64, s);
-        im.band32 = build_band_pack(n, rp, ci, im.an.diag, true, im.block_rows, 4, budget, im.LB32, s) &&
-                    build_band_pack(n, rp, ci, im.an.diag, false, im.block_rows, 4, budget, im.UB32, s);
-        if (im.band64) {
-            configure_band<double, false>(im.LB64, im.dev.sms);
-            configure_band<double, true>(im.UB64, im.dev.sms);
-        }
-        if (im.band32) {
-            configure_band<float, false>(im.LB32, im.dev.sms);
-            configure_band<float, true>(im.UB32, im.dev.sms);
+        for (int elem : {8, 4}) {
+            const int B = im.block_rows > 0 ? im.block_rows
+                                            : choose_block_rows(n, rp, ci, im.an.diag, im.an.nlev_l, elem, budget);
+            if (B <= 0) continue;
+            BlockPack& lb = elem == 8 ? im.LB64 : im.LB32;
+            BlockPack& ub = elem == 8 ? im.UB64 : im.UB32;
+            build_block_pack(n, rp, ci, im.an.diag, true, B, elem, budget, lb, s);
+            build_block_pack(n, rp, ci, im.an.diag, false, B, elem, budget, ub, s);
+            if (!(lb.fits && ub.fits)) continue;
+            if (elem == 8) {
+                configure_block<double, false>(lb, im.dev.sms);
+                configure_block<double, true>(ub, im.dev.sms);
+                im.blk64 = true;
+            } else {
+                configure_block<float, false>(lb, im.dev.sms);
+                configure_block<float, true>(ub, im.dev.sms);
+                im.blk32 = true;
+            }
         }
     }
-    im.level_packs = !(im.band64 && im.band32);
+    im.level_packs = !(im.blk64 && im.blk32);
     if (im.level_packs) {
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, im.L, s);
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, im.U, s);
@@ -509,14 +596,14 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
                 im.stamp, im.counters.get(), im.status.get());
             GB_CUDA_CHECK(cudaGetLastError());
             im.launches += 1;
-            if (im.band64) {
-                gather_band(im.LB64, im.lu.get(), s, im.dev.sms);
-                gather_band(im.UB64, im.lu.get(), s, im.dev.sms);
+            if (im.blk64) {
+                gather_block(im.LB64, true, im.lu.get(), s, im.dev.sms);
+                gather_block(im.UB64, false, im.lu.get(), s, im.dev.sms);
                 im.launches += 2;
             }
-            if (im.band32) {
-                gather_band(im.LB32, im.lu.get(), s, im.dev.sms);
-                gather_band(im.UB32, im.lu.get(), s, im.dev.sms);
+            if (im.blk32) {
+                gather_block(im.LB32, true, im.lu.get(), s, im.dev.sms);
+                gather_block(im.UB32, false, im.lu.get(), s, im.dev.sms);
                 im.launches += 2;
             }
             if (im.level_packs) {
@@ -663,9 +750,9 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
     fill_sentinel(y, n, s, im.dev.sms);
     fill_sentinel(d_x, n, s, im.dev.sms);
     double* b = const_cast<double*>(d_b);  // read only: no scale is passed to the forward sweep
-    if (im.band64) {
-        launch_band<double, false>(im.LB64, s, b, nullptr, y, counters + 1, status, nullptr, 0);
-        launch_band<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
+    if (im.blk64) {
+        launch_block<double, false>(im.LB64, s, b, nullptr, y, counters + 1, status, nullptr, 0);
+        launch_block<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
     } else if (im.L.ntask > 0) {
         sptrsv_lower_kernel<double><<<im.grid_solve, im.solve_threads, 0, s>>>(im.L.view<double>(), b, nullptr, y,
                                                                             counters + 1, status, nullptr, 0);
