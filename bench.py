@@ -148,11 +148,13 @@ def algorithmic_bytes(kind, a, nnz_l, nnz_u, tsize, steps_hist):
     return None
 
 
-def measured_traffic(kind, size):
+def measured_traffic(kind, size, block_rows):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the FP32
-    kernel `kind`, from the committed ncu summary of the convdiff3d 128^3 workload
-    (lines "traffic <kind> <bytes>"); None for another size or kernel."""
-    path = os.path.join(ROOT, "profiles", "sptrsv_fp32_convdiff3d_128.md")
+    sweep `kind`, from the committed ncu summary of the convdiff3d 128^3 workload for the
+    schedule in use (block-local with `block_rows` rows per block, or level-ordered when
+    0; lines "traffic <kind> <bytes>"); None for another size or kernel."""
+    name = "sptrsv_block_fp32_convdiff3d_128.md" if block_rows else "sptrsv_fp32_convdiff3d_128.md"
+    path = os.path.join(ROOT, "profiles", name)
     if size != 128 or not os.path.isfile(path):
         return None
     with open(path) as fh:
@@ -493,7 +495,9 @@ def run_ours(args):
     dom = max((k for k in prof if prof[k]["gbs"] is not None), key=lambda k: prof[k]["ms_total"])
     peak, peak_kind = measured_peaks()
     achieved = prof[dom]["gbs"]
-    traffic = measured_traffic(dom, args.size)
+    info_m = solvers["mixed"][0].info()
+    schedule = {"fp64_block_rows": int(info_m.block_rows_fp64), "fp32_block_rows": int(info_m.block_rows_fp32)}
+    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"])
 
     batched = None
     others = None
@@ -512,7 +516,8 @@ def run_ours(args):
             "metric": METRIC, "value": round(ms["mixed"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms["mixed"], 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 Krylov/ILU + f64 refinement", "data": "synthetic (seeded generator)",
-            "config": config_of(a, args.size, "mixed (FP32 cycles in FP64 refinement) + learned shift policy"),
+            "config": dict(config_of(a, args.size, "mixed (FP32 cycles in FP64 refinement) + learned shift policy"),
+                           substitution_schedule=schedule),
             "learned_shift": {k: v for k, v in learned.items() if k != "params"},
             "plain_fp64_ms": round(ms["plain"], 3),
             "speedup_vs_plain": round(ms["plain"] / ms["mixed"], 3),
