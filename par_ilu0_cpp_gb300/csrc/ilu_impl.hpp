@@ -61,10 +61,12 @@ struct BlockPack {
     int kmax = 0;         // most entries of a row
     long long slots = 0;
     int threads = 0;      // CTA size
-    int grid = 0;         // resident CTAs at the kernel's footprint
+    int cl = 0;           // cluster size of the cluster variant (0: plain variant)
+    int halo = 0;         // halo rows per CTA (cluster variant)
+    int grid = 0;         // CTAs to launch: resident CTAs (plain) or resident clusters x cl
     size_t smem = 0;      // dynamic shared memory of the kernel
     bool fits = false;
-    DeviceBuffer<int> blk_row, blk_task, rows, off, len, codes, src, dsrc;
+    DeviceBuffer<int> blk_row, blk_task, rows, off, len, codes, src, dsrc, exps;
     DeviceBuffer<double> v64, d64;
     DeviceBuffer<float> v32, d32;
 
@@ -74,6 +76,10 @@ struct BlockPack {
         p.nblk = nblk;
         p.ntask = ntask;
         p.slots = slots;
+        p.block_rows = block_rows;
+        p.halo = halo;
+        p.cl = cl;
+        p.exps = cl ? exps.get() : nullptr;
         p.blk_row = blk_row.get();
         p.blk_task = blk_task.get();
         p.rows = rows.get();

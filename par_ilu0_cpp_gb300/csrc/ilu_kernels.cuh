@@ -481,6 +481,7 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
 // descending, src/ilu_solver.cpp:687-696, 719-729): results are identical.
 // ---------------------------------------------------------------------------------
 constexpr int kBlockWarpsMax = 16;
+constexpr int kBlockCluster = 8;  // CTAs per cluster of the cluster variant (portable maximum)
 
 template <class T>
 struct BlockTri {
@@ -495,7 +496,47 @@ struct BlockTri {
     const int* codes = nullptr;     // [slots]
     const T* vals = nullptr;        // [slots]
     const T* dvals = nullptr;       // [32 * ntask] diagonal (upper factor only; FP32: 1 / u_ii)
+    // cluster variant: blocks at processing positions q*cl .. q*cl + cl - 1 run on one
+    // cluster; the rows of a block that the next position's block reads are pushed into
+    // that CTA's shared-memory halo xs[block_rows + slot] (slot = exps[...], -1 none)
+    int block_rows = 0;
+    int halo = 0;
+    int cl = 0;
+    const int* exps = nullptr;      // [32 * ntask]
 };
+
+// ---- thread-block cluster helpers (distributed shared memory) ----
+__device__ __forceinline__ unsigned cluster_rank_u32() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_size_u32() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+// Address of `p` (this CTA's shared memory) in the shared memory of cluster CTA `rank`.
+__device__ __forceinline__ unsigned map_shared_rank(const void* p, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(r)
+                 : "r"(static_cast<unsigned>(__cvta_generic_to_shared(p))), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void st_cluster(unsigned addr, float v) {
+    asm volatile("st.relaxed.cluster.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(unsigned addr, double v) {
+    asm volatile("st.relaxed.cluster.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(unsigned addr, int v) {
+    asm volatile("st.relaxed.cluster.shared::cluster.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+// All threads of all CTAs of the cluster; release / acquire ordering of shared memory.
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 template <class T>
 __device__ __forceinline__ T ld_volatile_shared(const T* p) {
@@ -517,7 +558,7 @@ __device__ __forceinline__ T block_dep(int code, const T* xs, const T* out) {
 // publishes each row to shared memory and to `out` the moment its last entry is consumed.
 template <class T, bool UPPER, int KM>
 __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)[KM], const T (&v)[KM], T acc, T d,
-                                                  T* xs, int base, T* out, int* status) {
+                                                  T* xs, int base, T* out, unsigned remote, int ex, int* status) {
     int k = 0;
     bool done = row < 0;
     long long rounds = 0;
@@ -542,6 +583,7 @@ __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)
                 // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
                 const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / d : acc * d) : acc);
                 st_volatile_shared(xs + (row - base), r);
+                if (remote != 0u && ex >= 0) st_cluster(remote + static_cast<unsigned>(ex) * sizeof(T), r);
                 st_relaxed(out + row, r);
                 done = true;
             }
@@ -587,7 +629,7 @@ __device__ __noinline__ T block_long_row(int off, int K, int lane, const int* co
 // and diagonal.
 template <class T, int KM>
 struct BlockTask {
-    int row, off, K;
+    int row, off, K, ex;
     int c[KM];
     T v[KM];
     T b, d;
@@ -607,25 +649,81 @@ __device__ __forceinline__ void load_block_task(const BlockTri<T>& P, int t, int
     }
     s.b = s.row >= 0 ? in[s.row] : T(0);
     s.d = UPPER ? P.dvals[t * kWarp + lane] : T(1);
+    s.ex = P.exps != nullptr ? P.exps[t * kWarp + lane] : -1;
 }
 
 template <class T, bool UPPER, int KM>
 __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const BlockTask<T, KM>& s, int lane,
-                                                 bool scaled, T sc, T* in, T* xs, int base, T* out, int* status) {
+                                                 bool scaled, T sc, T* in, T* xs, int base, T* out, unsigned remote,
+                                                 int* status) {
     T acc = scaled ? s.b * sc : s.b;
     const T acc0 = acc;
     if (s.K <= KM) {
-        block_progressive<T, UPPER, KM>(s.row, s.K, s.c, s.v, acc, s.d, xs, base, out, status);
+        block_progressive<T, UPPER, KM>(s.row, s.K, s.c, s.v, acc, s.d, xs, base, out, remote, s.ex, status);
     } else {
         acc = block_long_row(s.off, s.K, lane, P.codes, P.vals, acc, xs, out, status);
         if (s.row >= 0) {
             const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / s.d : acc * s.d) : acc);
             st_volatile_shared(xs + (s.row - base), r);
+            if (remote != 0u && s.ex >= 0) st_cluster(remote + static_cast<unsigned>(s.ex) * sizeof(T), r);
             st_relaxed(out + s.row, r);
         }
     }
     // the normalised Krylov vector is written back after the row is published
     if (scaled && s.row >= 0) in[s.row] = acc0;
+}
+
+// Solves block `blk` (its solution xs[0 .. rows) already at the sentinel).
+template <class T, bool UPPER, int KM>
+__device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in, bool scaled, T sc, T* xs, T* out,
+                                            unsigned remote, int* status) {
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const int base = P.blk_row[blk];
+    const int t1 = P.blk_task[blk + 1];
+    // Task data is loaded two tasks ahead (into two register sets, the loop unrolled by
+    // two so that neither set is ever moved): the packed factor comes from HBM, a round
+    // trip longer than the two levels one task ahead would cover.
+    BlockTask<T, KM> A, B2;
+    int t = P.blk_task[blk] + w;
+    if (t < t1) load_block_task<T, UPPER, KM>(P, t, lane, in, A);
+    if (t + nw < t1) load_block_task<T, UPPER, KM>(P, t + nw, lane, in, B2);
+    for (; t < t1; t += 2 * nw) {
+        solve_block_task<T, UPPER, KM>(P, A, lane, scaled, sc, in, xs, base, out, remote, status);
+        if (t + 2 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 2 * nw, lane, in, A);
+        if (t + nw < t1) {
+            solve_block_task<T, UPPER, KM>(P, B2, lane, scaled, sc, in, xs, base, out, remote, status);
+            if (t + 3 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 3 * nw, lane, in, B2);
+        }
+    }
+}
+
+// Streams block `blk`'s packed task data and right-hand side into L2 (first warp):
+// between sweeps the Krylov vectors evict them, and the warps' own loads run only two
+// tasks ahead.
+template <class T, bool UPPER>
+__device__ __forceinline__ void prefetch_block(const BlockTri<T>& P, int blk, const T* in) {
+    if (threadIdx.x >= kWarp) return;
+    const int lane = threadIdx.x;
+    const int base = P.blk_row[blk];
+    const int cnt = P.blk_row[blk + 1] - base;
+    const int t0 = P.blk_task[blk];
+    const int t1 = P.blk_task[blk + 1];
+    const long long s0 = P.off[t0];
+    const long long s1 = t1 < P.ntask ? P.off[t1] : P.slots;
+    prefetch_l2_range(P.codes + s0, (s1 - s0) * 4, lane);
+    prefetch_l2_range(P.vals + s0, (s1 - s0) * static_cast<long long>(sizeof(T)), lane);
+    prefetch_l2_range(P.rows + static_cast<long long>(t0) * kWarp, (t1 - t0) * 128ll, lane);
+    if (UPPER)
+        prefetch_l2_range(P.dvals + static_cast<long long>(t0) * kWarp,
+                          (t1 - t0) * static_cast<long long>(kWarp * sizeof(T)), lane);
+    // right-hand side rows [base, base + cnt): whole 16-byte pieces inside the range
+    const unsigned long long ib = reinterpret_cast<unsigned long long>(in + base);
+    const unsigned long long ie = reinterpret_cast<unsigned long long>(in + base + cnt);
+    const unsigned long long a16 = (ib + 15) & ~15ull;
+    if (ie > a16)
+        prefetch_l2_range(reinterpret_cast<const void*>(a16), static_cast<long long>((ie - a16) & ~15ull), lane);
 }
 
 // Forward (UPPER = false): out = L^{-1} (scale * in); with `scale`, in is rescaled in
@@ -643,53 +741,71 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
     extern __shared__ __align__(16) unsigned char blk_smem[];
     T* xs = reinterpret_cast<T*>(blk_smem);
     __shared__ int s_ticket;
-    const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const int nw = blockDim.x >> 5;
     const bool scaled = !UPPER && scale != nullptr;
     const T sc = scaled ? static_cast<T>(*scale) : T(1);
     for (int tk = draw_block_ticket(counter, P.nblk, &s_ticket); tk < P.nblk;
          tk = draw_block_ticket(counter, P.nblk, &s_ticket)) {
         const int blk = UPPER ? P.nblk - 1 - tk : tk;
-        const int base = P.blk_row[blk];
-        const int cnt = P.blk_row[blk + 1] - base;
-        const int t1 = P.blk_task[blk + 1];
-        if (threadIdx.x < kWarp) {
-            // the block's packed task data and right-hand side are streamed into L2 now:
-            // between sweeps the Krylov vectors evict them, and the warps' own loads run
-            // only two tasks ahead
-            const int t0 = P.blk_task[blk];
-            const long long s0 = P.off[t0];
-            const long long s1 = t1 < P.ntask ? P.off[t1] : P.slots;
-            prefetch_l2_range(P.codes + s0, (s1 - s0) * 4, lane);
-            prefetch_l2_range(P.vals + s0, (s1 - s0) * static_cast<long long>(sizeof(T)), lane);
-            prefetch_l2_range(P.rows + static_cast<long long>(t0) * kWarp, (t1 - t0) * 128ll, lane);
-            if (UPPER)
-                prefetch_l2_range(P.dvals + static_cast<long long>(t0) * kWarp,
-                                  (t1 - t0) * static_cast<long long>(kWarp * sizeof(T)), lane);
-            // right-hand side rows [base, base + cnt): whole 16-byte pieces inside the range
-            const unsigned long long ib = reinterpret_cast<unsigned long long>(in + base);
-            const unsigned long long ie = reinterpret_cast<unsigned long long>(in + base + cnt);
-            const unsigned long long a16 = (ib + 15) & ~15ull;
-            if (ie > a16) prefetch_l2_range(reinterpret_cast<const void*>(a16), static_cast<long long>((ie - a16) & ~15ull), lane);
-        }
+        const int cnt = P.blk_row[blk + 1] - P.blk_row[blk];
+        prefetch_block<T, UPPER>(P, blk, in);
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
         __syncthreads();
-        // Task data is loaded two tasks ahead (into two register sets, the loop unrolled by
-        // two so that neither set is ever moved): the packed factor comes from HBM, a
-        // round trip longer than the two levels one task ahead would cover.
-        BlockTask<T, KM> A, B2;
-        int t = P.blk_task[blk] + w;
-        if (t < t1) load_block_task<T, UPPER, KM>(P, t, lane, in, A);
-        if (t + nw < t1) load_block_task<T, UPPER, KM>(P, t + nw, lane, in, B2);
-        for (; t < t1; t += 2 * nw) {
-            solve_block_task<T, UPPER, KM>(P, A, lane, scaled, sc, in, xs, base, out, status);
-            if (t + 2 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 2 * nw, lane, in, A);
-            if (t + nw < t1) {
-                solve_block_task<T, UPPER, KM>(P, B2, lane, scaled, sc, in, xs, base, out, status);
-                if (t + 3 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 3 * nw, lane, in, B2);
-            }
+        solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, 0u, status);
+    }
+}
+
+// Cluster variant: launched with clusters of P.cl CTAs.  The cluster's CTA of rank r takes
+// processing position q * cl + r of the cluster's ticket q (tickets in dependency order:
+// no co-residency assumption between clusters; the CTAs of one cluster are co-scheduled
+// by the hardware).  Each CTA pushes the rows that the next position's block reads into
+// that CTA's shared-memory halo (xs[block_rows + slot], distributed shared memory), where
+// the consumer's entry codes point: in-cluster handoffs never touch L2.  Rank 0 reads its
+// cross-block values from L2 as in the plain variant.  Dynamic shared memory:
+// (block_rows + halo) x sizeof(T).
+template <class T, bool UPPER, int KM>
+__global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
+    sptrsv_block_cluster_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
+                                const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    T* xs = reinterpret_cast<T*>(blk_smem);
+    __shared__ int s_ticket;
+    const bool scaled = !UPPER && scale != nullptr;
+    const T sc = scaled ? static_cast<T>(*scale) : T(1);
+    const unsigned rank = cluster_rank_u32();
+    const unsigned CL = cluster_size_u32();
+    const int nq = (P.nblk + static_cast<int>(CL) - 1) / static_cast<int>(CL);
+    const int nclusters = static_cast<int>(gridDim.x / CL);
+    for (;;) {
+        // the previous round is complete in every CTA of the cluster (no remote store in
+        // flight) before the ticket and the halos are reset
+        cluster_sync_all();
+        if (rank == 0 && threadIdx.x == 0) {
+            const int q = static_cast<int>(atomicAdd(counter, 1u));
+            if (q == nq + nclusters - 1) atomicExch(counter, 0u);
+            for (unsigned r = 0; r < CL; ++r) st_cluster(map_shared_rank(&s_ticket, r), q);
         }
+        cluster_sync_all();
+        const int q = *reinterpret_cast<volatile int*>(&s_ticket);
+        if (q >= nq) break;
+        const int pos = q * static_cast<int>(CL) + static_cast<int>(rank);
+        const bool active = pos < P.nblk;
+        const int blk = UPPER ? P.nblk - 1 - pos : pos;
+        if (active) {
+            const int cnt = P.blk_row[blk + 1] - P.blk_row[blk];
+            prefetch_block<T, UPPER>(P, blk, in);
+            for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
+            for (int i = threadIdx.x; i < P.halo; i += blockDim.x) xs[P.block_rows + i] = Sentinel<T>::value();
+        }
+        __syncthreads();
+        // every halo is at the sentinel before any CTA of the cluster pushes into it
+        cluster_sync_all();
+        if (active) {
+            const bool push = rank + 1 < CL && pos + 1 < P.nblk;
+            const unsigned remote = push ? map_shared_rank(xs + P.block_rows, rank + 1) : 0u;
+            solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, remote, status);
+        }
+        __syncthreads();
     }
 }
 

@@ -214,7 +214,7 @@ static int choose_block_rows(int n, const int* rp, const int* ci, const std::vec
 // diagonal position.  A value type is marked as fitting when the largest block's
 // solution fits in `smem_budget` bytes of shared memory.
 static void build_block_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
-                             int block_rows, int elem, size_t smem_budget, BlockPack& P, cudaStream_t s) {
+                             int block_rows, int elem, size_t smem_budget, int cl, BlockPack& P, cudaStream_t s) {
     const int S = std::max(1, std::min(block_rows, std::max(n, 1)));
     const int nblk = n > 0 ? ceil_div(n, S) : 0;
     auto ebeg = [&](int r) { return lower ? rp[r] : diag[r] + 1; };
@@ -295,9 +295,51 @@ static void build_block_pack(int n, const int* rp, const int* ci, const std::vec
     P.slots = slots;
     // two tasks in flight per level of the widest block level, 4 .. kBlockWarpsMax warps
     P.threads = kWarp * std::max(4, std::min(kBlockWarpsMax, 2 * max_level_tasks));
+    // Cluster halos (cl > 0): the block at processing position p (ascending blocks for L,
+    // descending for U) reads the rows of position p - 1 that it depends on from its
+    // shared-memory halo when both positions are in one cluster (p % cl != 0).  Halo
+    // slots follow ascending row order; the producer's rows carry their slot in `exps`.
+    std::vector<int> exps;
+    int H = 0;
+    if (cl > 1) {
+        exps.assign(rows.size(), -1);
+        std::vector<int> slot_of(static_cast<size_t>(S), -1), used;
+        for (int pos = 1; pos < nblk; ++pos) {
+            if (pos % cl == 0) continue;
+            const int cb = lower ? pos : nblk - 1 - pos;
+            const int pb = lower ? pos - 1 : nblk - pos;
+            const int plo = blk_row[pb], phi = blk_row[pb + 1];
+            used.clear();
+            for (int t = blk_task[cb]; t < blk_task[cb + 1]; ++t)
+                for (long long q = off[t]; q < off[t] + static_cast<long long>(len[t]) * kWarp; ++q) {
+                    const int col = codes[static_cast<size_t>(q)];
+                    if (col >= plo && col < phi && slot_of[col - plo] < 0) {
+                        slot_of[col - plo] = 0;
+                        used.push_back(col);
+                    }
+                }
+            std::sort(used.begin(), used.end());
+            for (size_t k = 0; k < used.size(); ++k) slot_of[used[k] - plo] = static_cast<int>(k);
+            H = std::max(H, static_cast<int>(used.size()));
+            for (int t = blk_task[cb]; t < blk_task[cb + 1]; ++t)
+                for (long long q = off[t]; q < off[t] + static_cast<long long>(len[t]) * kWarp; ++q) {
+                    int& code = codes[static_cast<size_t>(q)];
+                    if (code >= plo && code < phi) code = -2 - (S + slot_of[code - plo]);
+                }
+            for (int t = blk_task[pb]; t < blk_task[pb + 1]; ++t)
+                for (int l = 0; l < kWarp; ++l) {
+                    const int r = rows[static_cast<size_t>(t) * kWarp + l];
+                    if (r >= 0) exps[static_cast<size_t>(t) * kWarp + l] = slot_of[r - plo];
+                }
+            for (int col : used) slot_of[col - plo] = -1;
+        }
+    }
+    P.cl = cl > 1 ? cl : 0;
+    P.halo = H;
     P.elem = elem;
-    P.smem = static_cast<size_t>(elem) * static_cast<size_t>(S);
+    P.smem = static_cast<size_t>(elem) * (static_cast<size_t>(S) + static_cast<size_t>(H));
     P.fits = P.smem <= smem_budget;
+    if (P.cl) P.exps.upload(exps.data(), exps.size(), s);
     P.blk_row.upload(blk_row.data(), blk_row.size(), s);
     P.blk_task.upload(blk_task.data(), blk_task.size(), s);
     P.rows.upload(rows.data(), rows.size(), s);
@@ -341,9 +383,43 @@ static void gather_block(const BlockPack& P, bool lower, const double* lu, cudaS
 
 // Raises the kernel's dynamic shared-memory limit to the pack's footprint for type T and
 // records the number of resident CTAs.
+// Launch configuration of the cluster variant (clusters of P.cl CTAs along x).
+static cudaLaunchConfig_t cluster_launch_config(const BlockPack& P, int grid, size_t smem, cudaStream_t s,
+                                                cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(grid));
+    cfg.blockDim = dim3(static_cast<unsigned>(P.threads));
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(P.cl);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+// Raises the kernel's dynamic shared-memory limit to the pack's footprint and records how
+// many CTAs to launch: the resident CTAs (plain variant) or the resident clusters times
+// the cluster size (cluster variant; 0 when a cluster cannot be scheduled).
 template <class T, bool UPPER, int KM>
 static void configure_block_km(BlockPack& P, int sms) {
     const int bytes = static_cast<int>(std::max<size_t>(P.smem, 16));
+    if (P.cl) {
+        auto* kern = sptrsv_block_cluster_kernel<T, UPPER, KM>;
+        GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        const int nq = ceil_div(P.nblk, P.cl);
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = cluster_launch_config(P, nq * P.cl, static_cast<size_t>(bytes), nullptr, attr);
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            nclusters = 0;
+        }
+        P.grid = std::min(nclusters, nq) * P.cl;
+        return;
+    }
     GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, UPPER, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        bytes));
     int per_sm = 0;
@@ -360,18 +436,28 @@ static void configure_block(BlockPack& P, int sms) {
         configure_block_km<T, UPPER, kLaneEntries>(P, sms);
 }
 
+template <class T, bool UPPER, int KM>
+static void launch_block_km(const BlockPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
+                            int* status, const int* gate, int step) {
+    if (P.cl) {
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = cluster_launch_config(P, P.grid, P.smem, s, attr);
+        GB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, sptrsv_block_cluster_kernel<T, UPPER, KM>, P.view<T>(), in, scale, out,
+                                         counter, status, gate, step));
+        return;
+    }
+    sptrsv_block_kernel<T, UPPER, KM><<<std::min(P.grid, P.nblk), P.threads, P.smem, s>>>(P.view<T>(), in, scale, out,
+                                                                                        counter, status, gate, step);
+}
+
 template <class T, bool UPPER>
 static void launch_block(const BlockPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
                          int* status, const int* gate, int step) {
     if (P.nblk == 0) return;
-    const int grid = std::min(P.grid, P.nblk);
-    const size_t smem = P.smem;
     if (P.kmax <= 4)
-        sptrsv_block_kernel<T, UPPER, 4><<<grid, P.threads, smem, s>>>(P.view<T>(), in, scale, out, counter, status,
-                                                                       gate, step);
+        launch_block_km<T, UPPER, 4>(P, s, in, scale, out, counter, status, gate, step);
     else
-        sptrsv_block_kernel<T, UPPER, kLaneEntries><<<grid, P.threads, smem, s>>>(P.view<T>(), in, scale, out, counter,
-                                                                                  status, gate, step);
+        launch_block_km<T, UPPER, kLaneEntries>(P, s, in, scale, out, counter, status, gate, step);
 }
 
 template <class T>
@@ -508,18 +594,28 @@ void IluSolver::SetupMatrix() {
             if (B <= 0) continue;
             BlockPack& lb = elem == 8 ? im.LB64 : im.LB32;
             BlockPack& ub = elem == 8 ? im.UB64 : im.UB32;
-            build_block_pack(n, rp, ci, im.an.diag, true, B, elem, budget, lb, s);
-            build_block_pack(n, rp, ci, im.an.diag, false, B, elem, budget, ub, s);
-            if (!(lb.fits && ub.fits)) continue;
-            if (elem == 8) {
-                configure_block<double, false>(lb, im.dev.sms);
-                configure_block<double, true>(ub, im.dev.sms);
-                im.blk64 = true;
-            } else {
-                configure_block<float, false>(lb, im.dev.sms);
-                configure_block<float, true>(ub, im.dev.sms);
-                im.blk32 = true;
+            // cluster variant first (block + halo must fit and a cluster be schedulable),
+            // else the plain variant
+            bool ok = false;
+            for (int cl : {kBlockCluster, 0}) {
+                if (cl > 0 && n <= B) continue;  // a single block has no handoffs
+                build_block_pack(n, rp, ci, im.an.diag, true, B, elem, budget, cl, lb, s);
+                build_block_pack(n, rp, ci, im.an.diag, false, B, elem, budget, cl, ub, s);
+                if (!(lb.fits && ub.fits)) continue;
+                if (elem == 8) {
+                    configure_block<double, false>(lb, im.dev.sms);
+                    configure_block<double, true>(ub, im.dev.sms);
+                } else {
+                    configure_block<float, false>(lb, im.dev.sms);
+                    configure_block<float, true>(ub, im.dev.sms);
+                }
+                if (lb.grid > 0 && ub.grid > 0) {
+                    ok = true;
+                    break;
+                }
             }
+            if (!ok) continue;
+            (elem == 8 ? im.blk64 : im.blk32) = true;
         }
     }
     im.level_packs = !(im.blk64 && im.blk32);
