@@ -148,12 +148,18 @@ def algorithmic_bytes(kind, a, nnz_l, nnz_u, tsize, steps_hist):
     return None
 
 
-def measured_traffic(kind, size, block_rows):
+def measured_traffic(kind, size, block_rows, cluster):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the FP32
     sweep `kind`, from the committed ncu summary of the convdiff3d 128^3 workload for the
-    schedule in use (block-local with `block_rows` rows per block, or level-ordered when
-    0; lines "traffic <kind> <bytes>"); None for another size or kernel."""
-    name = "sptrsv_block_fp32_convdiff3d_128.md" if block_rows else "sptrsv_fp32_convdiff3d_128.md"
+    schedule in use (block-local with `block_rows` rows per block and clusters of
+    `cluster` CTAs, or level-ordered when block_rows is 0; lines "traffic <kind> <bytes>");
+    None for another size or kernel."""
+    if not block_rows:
+        name = "sptrsv_fp32_convdiff3d_128.md"
+    elif cluster:
+        name = "sptrsv_block_cluster_fp32_convdiff3d_128.md"
+    else:
+        name = "sptrsv_block_fp32_convdiff3d_128.md"
     path = os.path.join(ROOT, "profiles", name)
     if size != 128 or not os.path.isfile(path):
         return None
@@ -496,8 +502,9 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = prof[dom]["gbs"]
     info_m = solvers["mixed"][0].info()
-    schedule = {"fp64_block_rows": int(info_m.block_rows_fp64), "fp32_block_rows": int(info_m.block_rows_fp32)}
-    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"])
+    schedule = {"fp64_block_rows": int(info_m.block_rows_fp64), "fp32_block_rows": int(info_m.block_rows_fp32),
+                "fp64_cluster": int(info_m.block_cluster_fp64), "fp32_cluster": int(info_m.block_cluster_fp32)}
+    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"], schedule["fp32_cluster"])
 
     batched = None
     others = None

@@ -120,6 +120,10 @@ typedef struct LLJBASH_IluInfo {
     int block_rows_fp64;  /* substitution schedule of the FP64 sweeps: rows per block of the
                            * block-local kernel, 0 = level-ordered kernel */
     int block_rows_fp32;  /* the same for the FP32 (mixed-precision) sweeps */
+    int block_cluster_fp64; /* CTAs per thread-block cluster of the block-local FP64 sweeps
+                             * (boundary rows handed over in distributed shared memory),
+                             * 0 = no clusters */
+    int block_cluster_fp32; /* the same for the FP32 sweeps */
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

@@ -48,7 +48,8 @@ class IluInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("nnz", ctypes.c_int), ("levels_lower", ctypes.c_int),
                 ("levels_upper", ctypes.c_int), ("breakdowns", ctypes.c_int), ("first_breakdown", ctypes.c_int),
                 ("factor_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong), ("shift_applied", ctypes.c_int),
-                ("block_rows_fp64", ctypes.c_int), ("block_rows_fp32", ctypes.c_int)]
+                ("block_rows_fp64", ctypes.c_int), ("block_rows_fp32", ctypes.c_int),
+                ("block_cluster_fp64", ctypes.c_int), ("block_cluster_fp32", ctypes.c_int)]
 
 
 class GmresReport(ctypes.Structure):

@@ -308,6 +308,8 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->shift_applied = im->shift_applied ? 1 : 0;
     info->block_rows_fp64 = im->blk64 ? im->LB64.block_rows : 0;
     info->block_rows_fp32 = im->blk32 ? im->LB32.block_rows : 0;
+    info->block_cluster_fp64 = im->blk64 ? im->LB64.cl : 0;
+    info->block_cluster_fp32 = im->blk32 ? im->LB32.cl : 0;
     return 0;
 }
 
