@@ -294,7 +294,7 @@ __device__ __forceinline__ void chunk_dots_rows(const T* __restrict__ V, long lo
     using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     const int lane = threadIdx.x & 31;
-#pragma unroll 2
+#pragma unroll 4
     for (int j = 0; j < nv; ++j) {
         T v[RPL];
         load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
