@@ -657,7 +657,6 @@ __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const Blo
                                                  bool scaled, T sc, T* in, T* xs, int base, T* out, unsigned remote,
                                                  int* status) {
     T acc = scaled ? s.b * sc : s.b;
-    const T acc0 = acc;
     if (s.K <= KM) {
         block_progressive<T, UPPER, KM>(s.row, s.K, s.c, s.v, acc, s.d, xs, base, out, remote, s.ex, status);
     } else {
@@ -669,8 +668,6 @@ __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const Blo
             st_relaxed(out + s.row, r);
         }
     }
-    // the normalised Krylov vector is written back after the row is published
-    if (scaled && s.row >= 0) in[s.row] = acc0;
 }
 
 // Solves block `blk` (its solution xs[0 .. rows) already at the sentinel).
@@ -697,6 +694,17 @@ __device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in
             if (t + 3 * nw < t1) load_block_task<T, UPPER, KM>(P, t + 3 * nw, lane, in, B2);
         }
     }
+}
+
+// GMRES normalises its new Krylov vector in the forward sweep: once every row of the
+// block is solved, the block's slice of `in` is rescaled in one coalesced pass (the same
+// product b * scale the rows used), off the dependency chain.
+template <class T>
+__device__ __forceinline__ void rescale_block_rhs(const BlockTri<T>& P, int blk, T* in, T sc) {
+    __syncthreads();
+    const int base = P.blk_row[blk];
+    const int cnt = P.blk_row[blk + 1] - base;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) in[base + i] = in[base + i] * sc;
 }
 
 // Streams block `blk`'s packed task data and right-hand side into L2 (first warp):
@@ -751,6 +759,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
         __syncthreads();
         solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, 0u, status);
+        if (scaled) rescale_block_rhs(P, blk, in, sc);
     }
 }
 
@@ -805,6 +814,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
             const unsigned remote = push ? map_shared_rank(xs + P.block_rows, rank + 1) : 0u;
             solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, remote, status);
         }
+        if (scaled && active) rescale_block_rhs(P, blk, in, sc);
         __syncthreads();
     }
 }
