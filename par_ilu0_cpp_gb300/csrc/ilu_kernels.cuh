@@ -739,7 +739,7 @@ __device__ __forceinline__ void prefetch_block(const BlockTri<T>& P, int blk, co
 // Backward (UPPER = true): out = U^{-1} in (in is left as it is).
 // out must hold the sentinel for every row on entry.  Dynamic shared memory: the
 // largest block's rows x sizeof(T).
-// KM: entries per row held in registers (4 when no row of the factor has more, else
+// KM: entries per row held in registers (3 or 4 when no row of the factor has more, else
 // kLaneEntries); longer rows take the entry-by-entry path.
 template <class T, bool UPPER, int KM>
 __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)

@@ -430,7 +430,9 @@ static void configure_block_km(BlockPack& P, int sms) {
 
 template <class T, bool UPPER>
 static void configure_block(BlockPack& P, int sms) {
-    if (P.kmax <= 4)
+    if (P.kmax <= 3)
+        configure_block_km<T, UPPER, 3>(P, sms);
+    else if (P.kmax <= 4)
         configure_block_km<T, UPPER, 4>(P, sms);
     else
         configure_block_km<T, UPPER, kLaneEntries>(P, sms);
@@ -454,7 +456,9 @@ template <class T, bool UPPER>
 static void launch_block(const BlockPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
                          int* status, const int* gate, int step) {
     if (P.nblk == 0) return;
-    if (P.kmax <= 4)
+    if (P.kmax <= 3)
+        launch_block_km<T, UPPER, 3>(P, s, in, scale, out, counter, status, gate, step);
+    else if (P.kmax <= 4)
         launch_block_km<T, UPPER, 4>(P, s, in, scale, out, counter, status, gate, step);
     else
         launch_block_km<T, UPPER, kLaneEntries>(P, s, in, scale, out, counter, status, gate, step);
