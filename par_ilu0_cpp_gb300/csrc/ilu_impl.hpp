@@ -79,7 +79,7 @@ struct BlockPack {
         p.block_rows = block_rows;
         p.halo = halo;
         p.cl = cl;
-        p.exps = cl ? exps.get() : nullptr;
+        p.exps = exps.get();
         p.blk_row = blk_row.get();
         p.blk_task = blk_task.get();
         p.rows = rows.get();

@@ -482,6 +482,7 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
 // ---------------------------------------------------------------------------------
 constexpr int kBlockWarpsMax = 16;
 constexpr int kBlockCluster = 8;  // CTAs per cluster of the cluster variant (portable maximum)
+constexpr int kPubGlobal = 1 << 30;
 
 template <class T>
 struct BlockTri {
@@ -496,9 +497,11 @@ struct BlockTri {
     const int* codes = nullptr;     // [slots]
     const T* vals = nullptr;        // [slots]
     const T* dvals = nullptr;       // [32 * ntask] diagonal (upper factor only; FP32: 1 / u_ii)
-    // cluster variant: blocks at processing positions q*cl .. q*cl + cl - 1 run on one
-    // cluster; the rows of a block that the next position's block reads are pushed into
-    // that CTA's shared-memory halo xs[block_rows + slot] (slot = exps[...], -1 none)
+    // Per-row publication words: bit kPubGlobal = another block reads the row through L2
+    // (store it to `out` as soon as it is computed; the others reach `out` in a coalesced
+    // copy when their block is done); bits 0-29 = halo slot + 1 (cluster variant: blocks
+    // at processing positions q*cl .. q*cl + cl - 1 run on one cluster and the rows the
+    // next position's block reads are pushed into that CTA's halo xs[block_rows + slot]).
     int block_rows = 0;
     int halo = 0;
     int cl = 0;
@@ -583,8 +586,9 @@ __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)
                 // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
                 const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / d : acc * d) : acc);
                 st_volatile_shared(xs + (row - base), r);
-                if (remote != 0u && ex >= 0) st_cluster(remote + static_cast<unsigned>(ex) * sizeof(T), r);
-                st_relaxed(out + row, r);
+                const int slot = (ex & (kPubGlobal - 1)) - 1;
+                if (remote != 0u && slot >= 0) st_cluster(remote + static_cast<unsigned>(slot) * sizeof(T), r);
+                if (ex & kPubGlobal) st_relaxed(out + row, r);
                 done = true;
             }
         }
@@ -649,7 +653,7 @@ __device__ __forceinline__ void load_block_task(const BlockTri<T>& P, int t, int
     }
     s.b = s.row >= 0 ? in[s.row] : T(0);
     s.d = UPPER ? P.dvals[t * kWarp + lane] : T(1);
-    s.ex = P.exps != nullptr ? P.exps[t * kWarp + lane] : -1;
+    s.ex = P.exps[t * kWarp + lane];
 }
 
 template <class T, bool UPPER, int KM>
@@ -664,8 +668,9 @@ __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const Blo
         if (s.row >= 0) {
             const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / s.d : acc * s.d) : acc);
             st_volatile_shared(xs + (s.row - base), r);
-            if (remote != 0u && s.ex >= 0) st_cluster(remote + static_cast<unsigned>(s.ex) * sizeof(T), r);
-            st_relaxed(out + s.row, r);
+            const int slot = (s.ex & (kPubGlobal - 1)) - 1;
+            if (remote != 0u && slot >= 0) st_cluster(remote + static_cast<unsigned>(slot) * sizeof(T), r);
+            if (s.ex & kPubGlobal) st_relaxed(out + s.row, r);
         }
     }
 }
@@ -696,15 +701,21 @@ __device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in
     }
 }
 
-// GMRES normalises its new Krylov vector in the forward sweep: once every row of the
-// block is solved, the block's slice of `in` is rescaled in one coalesced pass (the same
+// Once every row of the block is solved: GMRES normalises its new Krylov vector in the
+// forward sweep, so the block's slice of `in` is rescaled in one coalesced pass (the same
 // product b * scale the rows used), off the dependency chain.
+// Also the block's solution reaches `out` here, copied from shared memory (rows that
+// other blocks read were stored when computed and are stored again, unchanged).
 template <class T>
-__device__ __forceinline__ void rescale_block_rhs(const BlockTri<T>& P, int blk, T* in, T sc) {
+__device__ __forceinline__ void finish_block(const BlockTri<T>& P, int blk, T* in, bool scaled, T sc, const T* xs,
+                                             T* out) {
     __syncthreads();
     const int base = P.blk_row[blk];
     const int cnt = P.blk_row[blk + 1] - base;
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) in[base + i] = in[base + i] * sc;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        out[base + i] = xs[i];
+        if (scaled) in[base + i] = in[base + i] * sc;
+    }
 }
 
 // Streams block `blk`'s packed task data and right-hand side into L2 (first warp):
@@ -759,7 +770,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
         __syncthreads();
         solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, 0u, status);
-        if (scaled) rescale_block_rhs(P, blk, in, sc);
+        finish_block(P, blk, in, scaled, sc, xs, out);
     }
 }
 
@@ -814,7 +825,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
             const unsigned remote = push ? map_shared_rank(xs + P.block_rows, rank + 1) : 0u;
             solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, remote, status);
         }
-        if (scaled && active) rescale_block_rhs(P, blk, in, sc);
+        if (active) finish_block(P, blk, in, scaled, sc, xs, out);
         __syncthreads();
     }
 }

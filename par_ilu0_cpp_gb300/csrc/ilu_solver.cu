@@ -334,12 +334,27 @@ static void build_block_pack(int n, const int* rp, const int* ci, const std::vec
             for (int col : used) slot_of[col - plo] = -1;
         }
     }
+    // Per-row publication word (`pub`): bit 30 = some block reads the row through L2
+    // (a code >= 0 names it), so its value is stored to `out` the moment it is computed;
+    // bits 0-29 = halo slot + 1 (0: none).  Rows without bit 30 reach `out` in one
+    // coalesced copy when their block is done.
+    {
+        std::vector<unsigned char> global_read(static_cast<size_t>(n), 0);
+        for (int code : codes)
+            if (code >= 0) global_read[static_cast<size_t>(code)] = 1;
+        if (exps.empty()) exps.assign(rows.size(), -1);
+        for (size_t q = 0; q < rows.size(); ++q) {
+            const int r = rows[q];
+            const int slot = exps[q];
+            exps[q] = (r >= 0 && global_read[static_cast<size_t>(r)] ? (1 << 30) : 0) | (slot + 1);
+        }
+    }
     P.cl = cl > 1 ? cl : 0;
     P.halo = H;
     P.elem = elem;
     P.smem = static_cast<size_t>(elem) * (static_cast<size_t>(S) + static_cast<size_t>(H));
     P.fits = P.smem <= smem_budget;
-    if (P.cl) P.exps.upload(exps.data(), exps.size(), s);
+    P.exps.upload(exps.data(), exps.size(), s);
     P.blk_row.upload(blk_row.data(), blk_row.size(), s);
     P.blk_task.upload(blk_task.data(), blk_task.size(), s);
     P.rows.upload(rows.data(), rows.size(), s);
