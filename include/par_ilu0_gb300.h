@@ -66,9 +66,24 @@ enum {
      *   -1:  the level-ordered sync-free kernel. */
     LLJBASH_ILU_OPT_BLOCK_ROWS = 2,
     /* warps of the level-ordered substitution kernels (0 = automatic: about 48 levels'
-     * worth of 32-row tasks, 4 levels' worth when the factor's rows average more than 8
-     * entries per triangle; at most 8 per SM).  Takes effect at the next IluSolverSetup. */
-    LLJBASH_ILU_OPT_SOLVE_WARPS = 3
+     * worth of tasks, 4 levels' worth when a triangle has rows too long for a lane group
+     * and its rows average more than 8 entries; at most 8 per SM).  Takes effect at the
+     * next IluSolverSetup. */
+    LLJBASH_ILU_OPT_SOLVE_WARPS = 3,
+    /* lanes per row of the level-ordered substitution kernels (results are the same for
+     * every value):
+     *   0:  automatic (default): per triangle, one lane while rows have at most 8
+     *       entries, else the smallest group of 2, 4, .. 32 lanes holding the longest
+     *       row in 8 entries per lane; one lane (blocking waits) past 256 entries;
+     *   1:  one lane per row;
+     *   2, 4, 8, 16, 32: at least that many lanes per row (rows of up to 256 entries).
+     * Takes effect at the next IluSolverSetup. */
+    LLJBASH_ILU_OPT_ROW_LANES = 4,
+    /* limit of one device-side dependency wait, in microseconds of device time (0 =
+     * default, 4 s).  A wait that reaches it gives up: the call that launched it returns
+     * -1 ("dependency wait timed out on the device") and the solver stays usable.  Takes
+     * effect at the next launch. */
+    LLJBASH_ILU_OPT_WAIT_LIMIT_US = 5
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 
@@ -124,6 +139,8 @@ typedef struct LLJBASH_IluInfo {
                              * (boundary rows handed over in distributed shared memory),
                              * 0 = no clusters */
     int block_cluster_fp32; /* the same for the FP32 sweeps */
+    int row_lanes_lower;  /* lanes per row of the level-ordered lower / upper sweeps */
+    int row_lanes_upper;
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

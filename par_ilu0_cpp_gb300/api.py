@@ -49,7 +49,8 @@ class IluInfo(ctypes.Structure):
                 ("levels_upper", ctypes.c_int), ("breakdowns", ctypes.c_int), ("first_breakdown", ctypes.c_int),
                 ("factor_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong), ("shift_applied", ctypes.c_int),
                 ("block_rows_fp64", ctypes.c_int), ("block_rows_fp32", ctypes.c_int),
-                ("block_cluster_fp64", ctypes.c_int), ("block_cluster_fp32", ctypes.c_int)]
+                ("block_cluster_fp64", ctypes.c_int), ("block_cluster_fp32", ctypes.c_int),
+                ("row_lanes_lower", ctypes.c_int), ("row_lanes_upper", ctypes.c_int)]
 
 
 class GmresReport(ctypes.Structure):
@@ -61,6 +62,8 @@ class GmresReport(ctypes.Structure):
 ILU_OPT_COPY_BACK = 1
 ILU_OPT_BLOCK_ROWS = 2
 ILU_OPT_SOLVE_WARPS = 3
+ILU_OPT_ROW_LANES = 4
+ILU_OPT_WAIT_LIMIT_US = 5
 GMRES_OPT_MODE = 1
 GMRES_OPT_TAU = 2
 GMRES_OPT_USE_GRAPH = 3

@@ -140,6 +140,19 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 if (value < 0 || value > 1e6) throw std::runtime_error("solve warps must be 0 (automatic) or a warp count");
                 s->impl()->solve_warps = static_cast<int>(value);
                 return 0;
+            case LLJBASH_ILU_OPT_ROW_LANES: {
+                const int v = static_cast<int>(value);
+                if (value != v || (v != 0 && (v & (v - 1)) != 0) || v < 0 || v > 32)
+                    throw std::runtime_error("row lanes must be 0 (automatic), 1, 2, 4, 8, 16 or 32");
+                s->impl()->row_lanes = v;
+                return 0;
+            }
+            case LLJBASH_ILU_OPT_WAIT_LIMIT_US:
+                if (value < 0 || value > 2147483647.0 || value != static_cast<int>(value))
+                    throw std::runtime_error("wait limit must be 0 (default) or a number of microseconds");
+                s->impl()->wait_limit_us = static_cast<int>(value);
+                s->impl()->push_wait_limit();
+                return 0;
             case LLJBASH_ILU_OPT_BLOCK_ROWS:
                 if (value < -1 || value > 1e8) throw std::runtime_error("block rows must be -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);
@@ -310,6 +323,8 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->block_rows_fp32 = im->blk32 ? im->LB32.block_rows : 0;
     info->block_cluster_fp64 = im->blk64 ? im->LB64.cl : 0;
     info->block_cluster_fp32 = im->blk32 ? im->LB32.cl : 0;
+    info->row_lanes_lower = im->level_packs ? im->L.group : 0;
+    info->row_lanes_upper = im->level_packs ? im->U.group : 0;
     return 0;
 }
 

@@ -22,13 +22,23 @@ namespace gb300 {
 constexpr int kWarp = 32;
 
 // Device status words (one int array per solver):
-//   [0] a dependency wait gave up (iteration cap reached)
+//   [0] a dependency wait gave up
 //   [1] number of zero / non-finite pivots met in the last factorisation
 //   [2] smallest row index with such a pivot (INT_MAX when none)
-enum StatusWord { kStatusTimeout = 0, kStatusBreakdowns = 1, kStatusFirstBreakdown = 2, kStatusWords = 4 };
+//   [3] wait limit in microseconds, written by the host (0: kWaitLimitUsDefault)
+enum StatusWord {
+    kStatusTimeout = 0,
+    kStatusBreakdowns = 1,
+    kStatusFirstBreakdown = 2,
+    kStatusWaitLimitUs = 3,
+    kStatusWords = 4
+};
 
-// Upper bound on polls of one dependency before a wait gives up (about a second).
-constexpr long long kSpinLimit = 1ll << 21;
+// A dependency wait gives up when the awaited value has not arrived within the wait
+// limit (default 4 s of device time: every wait on the critical path of a correct
+// computation ends far sooner), or after kPollLimit polls whatever the clock says.
+constexpr int kWaitLimitUsDefault = 4000000;
+constexpr long long kPollLimit = 1ll << 28;
 
 // "Not yet written" markers for value-as-flag waits.  A computed value is never equal to
 // them: results that are NaN are stored as the canonical quiet NaN instead.
@@ -94,35 +104,66 @@ __device__ __forceinline__ int ld_relaxed_int(const int* p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bookkeeping of one bounded wait (or one bounded polling loop), called once per poll.
+// expired() turns true once the wait limit has passed since the wait began (the clock
+// is read every 64 polls), once another thread has given up (status checked every 1024
+// polls), or after kPollLimit polls.  Every lane of a warp that polls in lockstep gets
+// the same answer, so a warp leaves such a loop as a whole.
+struct WaitBudget {
+    unsigned long long t0 = 0;
+    unsigned long long limit_ns = 0;
+    long long polls = 0;
+
+    __device__ __forceinline__ bool expired(const int* status) {
+        ++polls;
+        if ((polls & 63) != 0) return false;
+        if (polls >= kPollLimit) return true;
+        if ((polls & 1023) == 0 && ld_relaxed_int(status + kStatusTimeout) != 0) return true;
+        const unsigned long long now = global_ns();
+        if (t0 == 0) {
+            const int us = status[kStatusWaitLimitUs];
+            limit_ns = 1000ull * static_cast<unsigned long long>(us > 0 ? us : kWaitLimitUsDefault);
+            t0 = now;
+            return false;
+        }
+        return now - t0 > limit_ns;
+    }
+};
+
 // Polls made back to back before a wait starts to sleep between polls: a dependency on
 // the critical path is usually published within a few round trips, and a sleep (whose
 // actual length is far above its nominal 32 ns) would delay its detection.
 constexpr int kSpinBeforeSleep = 256;
 
-// Waits until *p is no longer the sentinel; returns the value.  Gives up after
-// kSpinLimit polls (or as soon as another thread has given up), records the timeout in
-// status[kStatusTimeout] and returns 0.
+// Waits until *p is no longer the sentinel; returns the value.  When the wait expires
+// (WaitBudget) the timeout is recorded in status[kStatusTimeout] and 0 is returned.
 template <class T>
 __device__ __forceinline__ T wait_value(const T* p, int* status) {
     T v = ld_relaxed(p);
     if (!Sentinel<T>::is(v)) return v;
-    for (long long it = 0; it < kSpinLimit; ++it) {
-        if (it >= kSpinBeforeSleep) __nanosleep(32);
+    WaitBudget wb;
+    while (!wb.expired(status)) {
+        if (wb.polls > kSpinBeforeSleep) __nanosleep(32);
         v = ld_relaxed(p);
         if (!Sentinel<T>::is(v)) return v;
-        if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) return T(0);
     }
     atomicExch(status + kStatusTimeout, 1);
     return T(0);
 }
 
-// Waits until *flag == stamp (acquire).  Same spin and give-up rules as wait_value.
+// Waits until *flag == stamp (acquire).  Same give-up rules as wait_value.
 __device__ __forceinline__ bool wait_flag(const int* flag, int stamp, int* status) {
     if (ld_acquire(flag) == stamp) return true;
-    for (long long it = 0; it < kSpinLimit; ++it) {
-        if (it >= kSpinBeforeSleep) __nanosleep(32);
+    WaitBudget wb;
+    while (!wb.expired(status)) {
+        if (wb.polls > kSpinBeforeSleep) __nanosleep(32);
         if (ld_acquire(flag) == stamp) return true;
-        if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) return false;
     }
     atomicExch(status + kStatusTimeout, 1);
     return false;

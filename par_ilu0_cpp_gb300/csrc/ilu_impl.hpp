@@ -16,6 +16,7 @@ namespace gb300 {
 // schedule arrays plus packed values in FP64 and FP32.
 struct LevelPack {
     int ntask = 0;
+    int group = 1;  // lanes per row
     long long slots = 0;
     DeviceBuffer<int> rows, off, len, cols, src, dsrc;
     DeviceBuffer<double> v64, d64;
@@ -150,9 +151,15 @@ struct IluSolver::Impl {
     float last_factor_ms = 0.f;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int grid_fact = 0;
+    // factorisation launch: staged entries per warp, warps per block, pivot-row register
+    // window per lane, dynamic shared memory per block
+    int fact_cap = 0, fact_warps = 0, fact_pre = 2;
+    size_t fact_smem = 0;
     // level-ordered substitution launch: grid_solve CTAs of solve_threads threads
     int grid_solve = 0, solve_threads = 0;
     int solve_warps = 0;  // requested warps for the level-ordered kernels (0 = automatic)
+    int row_lanes = 0;    // requested lanes per row of the level-ordered kernels (0 = automatic)
+    int wait_limit_us = 0;  // device wait limit in microseconds (0 = kWaitLimitUsDefault)
     int block_rows = 0;  // rows per substitution block (0 = automatic, < 0 = level-ordered kernel)
     long long launches = 0;  // kernels launched by Factorize / Substitute
 
@@ -170,6 +177,8 @@ struct IluSolver::Impl {
     const void* subst_key() const;
     // Throws when a dependency wait timed out since the last call.
     void check_status(cudaStream_t s);
+    // Writes wait_limit_us into the device status words (when they exist).
+    void push_wait_limit();
 };
 
 }  // namespace lljbash

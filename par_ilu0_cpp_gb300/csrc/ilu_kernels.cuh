@@ -18,8 +18,10 @@
 
 namespace gb300 {
 
-constexpr int kFactWarps = 8;    // warps per block of the factorisation kernel
-constexpr int kFactCap = 128;    // row length staged in shared memory per warp
+constexpr int kFactWarps = 8;    // most warps per block of the factorisation kernel
+constexpr int kFactCap = 128;    // least row length staged in shared memory per warp
+constexpr int kFactEntryBytes = 2 * sizeof(double) + 3 * sizeof(int);  // staged bytes per entry
+constexpr int kFactSmemMax = 200 * 1024;  // dynamic shared memory of one factorisation block
 constexpr int kSolveWarps = 8;   // warps per block of the substitution kernels
 
 // Binary search of c in the sorted s[lo, hi); returns the position or -1.
@@ -66,25 +68,30 @@ __device__ __forceinline__ bool gate_closed(const int* gate, int step) {
 //
 // Row j is staged in shared memory together with, for every pivot k, diag[k], the end
 // of row k and u_kk, all loaded in parallel once the pivots' ready flags are acquired;
-// the strict-upper entries of the next pivot row are loaded into registers while the
-// current pivot is eliminated.  The sequential chain per pivot is then one division
-// (one lane) and a shared-memory search-and-update, instead of three dependent global
-// round trips.  Rows longer than kFactCap are eliminated in global memory.  Row k's
-// values are read at L2 (ld.cg) after an acquire on its ready flag; row j publishes
-// with fence + release.  `shift` (optional) is added to the diagonal before elimination.
-constexpr int kFactPre = 2;  // next-pivot entries per lane held in registers
-
-static __global__ void __launch_bounds__(kFactWarps * kWarp)
+// the strict-upper entries of the next pivot row (PRE per lane: 2, or 8 for matrices
+// whose rows have more than 64 entries above the diagonal) are loaded into registers
+// while the current pivot is eliminated.  The sequential chain per pivot is then one
+// division (one lane) and a shared-memory search-and-update, instead of three dependent
+// global round trips.  Each warp stages up to `cap` entries (dynamic shared memory,
+// kFactEntryBytes per entry and warp, sized by the host to the longest row where it
+// fits); longer rows are eliminated in global memory.  Row k's values are read at L2
+// (ld.cg) after an acquire on its ready flag; row j publishes with fence + release.
+// `shift` (optional) is added to the diagonal before elimination.
+template <int PRE>
+__global__ void __launch_bounds__(kFactWarps * kWarp)
     ilu_factor_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const int* __restrict__ diag,
                       const int* __restrict__ order, double* lu, const double* __restrict__ shift, int* done,
-                      int stamp, unsigned* counter, int* status) {
-    __shared__ int s_col[kFactWarps][kFactCap];
-    __shared__ double s_val[kFactWarps][kFactCap];
-    __shared__ int s_kd[kFactWarps][kFactCap];
-    __shared__ int s_ke[kFactWarps][kFactCap];
-    __shared__ double s_ukk[kFactWarps][kFactCap];
+                      int stamp, unsigned* counter, int* status, int cap) {
+    extern __shared__ double fact_smem[];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const size_t wc = static_cast<size_t>(w) * cap, nc_ = static_cast<size_t>(nw) * cap;
+    double* sval = fact_smem + wc;
+    double* sukk = fact_smem + nc_ + wc;
+    int* scol = reinterpret_cast<int*>(fact_smem + 2 * nc_) + wc;
+    int* skd = reinterpret_cast<int*>(fact_smem + 2 * nc_) + nc_ + wc;
+    int* ske = reinterpret_cast<int*>(fact_smem + 2 * nc_) + 2 * nc_ + wc;
     int q = draw_ticket(counter, n, lane);
     while (q < n) {
         const int qn = draw_ticket(counter, n, lane);
@@ -94,12 +101,7 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
         const int dloc = diag[j] - b;
         for (int t = lane; t < dloc; t += kWarp) wait_flag(done + ci[b + t], stamp, status);
         __syncwarp();
-        if (len <= kFactCap) {
-            int* scol = s_col[w];
-            double* sval = s_val[w];
-            int* skd = s_kd[w];
-            int* ske = s_ke[w];
-            double* sukk = s_ukk[w];
+        if (len <= cap) {
             for (int t = lane; t < len; t += kWarp) {
                 const int c = ci[b + t];
                 scol[t] = c;
@@ -115,13 +117,13 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
             }
             __syncwarp();
             // strict-upper entries of pivot row t held by this lane: p = kd + 1 + lane + 32 u
-            int nc[kFactPre];
-            double nv[kFactPre];
+            int nc[PRE];
+            double nv[PRE];
             auto load_pivot = [&](int t) {
                 const int p0 = skd[t] + 1 + lane;
                 const int pe = ske[t];
 #pragma unroll
-                for (int u = 0; u < kFactPre; ++u) {
+                for (int u = 0; u < PRE; ++u) {
                     const int p = p0 + u * kWarp;
                     nc[u] = p < pe ? ci[p] : -1;
                     nv[u] = p < pe ? __ldcg(lu + p) : 0.0;
@@ -129,10 +131,10 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
             };
             if (dloc > 0) load_pivot(0);
             for (int t = 0; t < dloc; ++t) {
-                int cc[kFactPre];
-                double cv[kFactPre];
+                int cc[PRE];
+                double cv[PRE];
 #pragma unroll
-                for (int u = 0; u < kFactPre; ++u) {
+                for (int u = 0; u < PRE; ++u) {
                     cc[u] = nc[u];
                     cv[u] = nv[u];
                 }
@@ -144,14 +146,14 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
                 }
                 l = __shfl_sync(0xffffffffu, l, 0);
 #pragma unroll
-                for (int u = 0; u < kFactPre; ++u) {
+                for (int u = 0; u < PRE; ++u) {
                     if (cc[u] >= 0) {
                         const int pos = find_sorted(scol, t + 1, len, cc[u]);
                         if (pos >= 0) sval[pos] = fma(-cv[u], l, sval[pos]);
                     }
                 }
                 // strict-upper entries beyond the register window (long pivot rows)
-                for (int p = skd[t] + 1 + lane + kFactPre * kWarp; p < ske[t]; p += kWarp) {
+                for (int p = skd[t] + 1 + lane + PRE * kWarp; p < ske[t]; p += kWarp) {
                     const int pos = find_sorted(scol, t + 1, len, ci[p]);
                     if (pos >= 0) sval[pos] = fma(-__ldcg(lu + p), l, sval[pos]);
                 }
@@ -199,28 +201,30 @@ static __global__ void __launch_bounds__(kFactWarps * kWarp)
 }
 
 // Level-ordered packed triangular factor (default substitution layout).  Rows are taken in the
-// schedule order and grouped 32 to a task (one lane per row).  Task t owns slots
-// [off[t], off[t] + 32 * len[t]); entry k of lane l sits at off[t] + 32 k + l, so a
-// warp's loads of entry k are one coalesced 128/256-byte access.  Pad slots have
-// col = -1.  L entries are stored in ascending column order and U entries in descending
-// column order: the accumulation order of the reference's substitute_row_L / _U
-// (src/ilu_solver.cpp:687-696, 719-729).
+// schedule order, G lanes per row (G = 1, 2, 4 .. 32, one value per factor), 32 / G rows
+// to a task.  Task t owns slots [off[t], off[t] + 32 * len[t]); lane l = i G + j holds
+// entries [j len[t], (j + 1) len[t]) of the task's row i, entry j len[t] + u at
+// off[t] + 32 u + l, so a warp's loads of entry slot u are one coalesced 128/256-byte
+// access.  Pad slots have col = -1.  L entries are stored in ascending column order and
+// U entries in descending column order: the accumulation order of the reference's
+// substitute_row_L / _U (src/ilu_solver.cpp:687-696, 719-729).
 template <class T>
 struct PackedTri {
     int ntask = 0;
-    const int* rows = nullptr;   // [32 * ntask], -1 for padding
+    const int* rows = nullptr;   // [32 * ntask] row of each lane, -1 for padding
     const int* off = nullptr;    // [ntask]
-    const int* len = nullptr;    // [ntask]
+    const int* len = nullptr;    // [ntask] entries per lane
     const int* cols = nullptr;   // [slots]
     const T* vals = nullptr;     // [slots]
-    const T* dvals = nullptr;    // [32 * ntask] diagonal (upper factor only)
+    const T* dvals = nullptr;    // [32 * ntask] diagonal of each lane's row (upper factor only)
 };
 
-constexpr int kLaneEntries = 8;  // rows with at most this many entries use the per-lane path
+constexpr int kLaneEntries = 8;  // entries a lane holds in registers
+constexpr int kRowLanesMax = 32;  // largest lane group per row (rows of up to 256 entries)
 // Automatic size of the level-ordered substitution grid: warps for this many levels of
-// 32-row tasks (averaged over the factor), at most kSolveWarps per SM.
+// tasks (averaged over the factor), at most kSolveWarps per SM.
 constexpr double kSolveLevelsAhead = 48.0;
-constexpr double kSolveLevelsAheadLong = 4.0;  // factors whose rows average > kLaneEntries
+constexpr double kSolveLevelsAheadLong = 4.0;  // rows longer than kRowLanesMax * kLaneEntries
 
 // Per-lane progressive solve of a warp's 32 rows (one per lane), for rows with at most
 // kLaneEntries entries held in registers (c: column or -1, v: value).  Every round a
@@ -228,15 +232,15 @@ constexpr double kSolveLevelsAheadLong = 4.0;  // factors whose rows average > k
 // prefix in entry order (the reference's accumulation order, so the operations are the
 // same as a sequential sweep) and publishes its row the moment its last entry is
 // consumed.  A row therefore never waits for the slowest row of its warp; the warp
-// leaves the loop when all 32 rows are published.  Rounds are bounded: past kSpinLimit
-// (or once another wait has given up) the status word is set and the loop ends.
+// leaves the loop when all 32 rows are published.  Rounds are bounded (WaitBudget): when
+// the wait expires the status word is set and the loop ends.
 template <class T, bool UPPER>
 __device__ __forceinline__ void progressive_rows(int row, int K, const int (&c)[kLaneEntries],
                                                  const T (&v)[kLaneEntries], T acc, T d, const T* dep, T* out,
                                                  int* status) {
     int k = 0;
     bool done = row < 0;
-    long long rounds = 0;
+    WaitBudget wb;
     while (!__all_sync(0xffffffffu, done)) {
         if (!done) {
             T xs[kLaneEntries];
@@ -261,11 +265,83 @@ __device__ __forceinline__ void progressive_rows(int row, int K, const int (&c)[
                 done = true;
             }
         }
-        if (++rounds >= kSpinLimit) {
+        if (wb.expired(status)) {
             if (!done) atomicExch(status + kStatusTimeout, 1);
             break;
         }
-        if ((rounds & 1023) == 0 && ld_relaxed_int(status + kStatusTimeout) != 0) break;
+    }
+}
+
+// Progressive solve of rows of up to G * kLaneEntries entries with G lanes per row
+// (G = 2 .. 32, a warp holds 32 / G rows).  Lane j of a row's group holds entries
+// [j K, j K + K) of the row in registers (K = the task's entries per lane; columns -1
+// pad the row's tail).  Every round each lane loads, all at once, the dependencies it
+// holds that are still unconsumed and still read as the sentinel (published values
+// never change, so a value once read is kept).  The running sum then travels along the
+// group: the lane holding the first unconsumed entry (the owner) consumes its ready
+// prefix in entry order and, once all its entries are consumed, hands the sum to the
+// next lane by a shuffle; that lane goes on in the same round with the values it
+// already holds.  So each entry is consumed in the reference's order (the operations of
+// a sequential sweep), while a row waits about one round trip per wait instead of one
+// per chunk of entries.  Lane 0 of the group publishes the row.  Rounds are bounded as
+// in progressive_rows.
+template <class T, bool UPPER, int G>
+__device__ __forceinline__ void group_rows(int row, int K, int lane, const int (&c)[kLaneEntries],
+                                           const T (&v)[kLaneEntries], T acc, T d, const T* dep, T* out,
+                                           int* status) {
+    const int j = lane & (G - 1);
+    const int gb = lane - j;
+    T x[kLaneEntries];
+#pragma unroll
+    for (int u = 0; u < kLaneEntries; ++u) x[u] = Sentinel<T>::value();
+    int o = 0;  // owner: group position of the first unconsumed entry (G = row done)
+    int k = 0;  // next entry of this lane to consume (meaningful in the owner)
+    bool done = row < 0;
+    WaitBudget wb;
+    while (!__all_sync(0xffffffffu, done)) {
+        if (!done && j >= o) {
+            const int k0 = j == o ? k : 0;
+#pragma unroll
+            for (int u = 0; u < kLaneEntries; ++u)
+                if (u >= k0 && u < K && c[u] >= 0 && Sentinel<T>::is(x[u])) x[u] = ld_relaxed_nb(dep + c[u]);
+        }
+#pragma unroll 1
+        for (int step = 0; step < G; ++step) {
+            bool fin = false;
+            if (!done && j == o) {
+#pragma unroll
+                for (int u = 0; u < kLaneEntries; ++u) {
+                    if (k == u && u < K) {
+                        if (c[u] < 0) {
+                            ++k;
+                        } else if (!Sentinel<T>::is(x[u])) {
+                            acc = fma(-v[u], x[u], acc);
+                            ++k;
+                        }
+                    }
+                }
+                fin = k >= K;
+            }
+            const int src = gb + (o < G ? o : G - 1);
+            const bool moved = __shfl_sync(0xffffffffu, fin, src);
+            acc = __shfl_sync(0xffffffffu, acc, src);
+            if (moved) {
+                ++o;
+                if (o == G) {
+                    if (j == 0) {
+                        // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
+                        const T r = UPPER ? (sizeof(T) == 8 ? acc / d : acc * d) : acc;
+                        st_relaxed(out + row, Sentinel<T>::canon(r));
+                    }
+                    done = true;
+                }
+            }
+            if (!__any_sync(0xffffffffu, moved)) break;
+        }
+        if (wb.expired(status)) {
+            if (!done) atomicExch(status + kStatusTimeout, 1);
+            break;
+        }
     }
 }
 
@@ -336,16 +412,31 @@ __device__ __forceinline__ T blocking_row(int off, int K, int lane, const int* c
     return acc;
 }
 
+// Loads lane `lane`'s packed entries of task (off, K): columns (-1 past K) and values.
+template <class T>
+__device__ __forceinline__ void load_lane_entries(const PackedTri<T>& P, int off, int K, int lane,
+                                                  int (&c)[kLaneEntries], T (&v)[kLaneEntries]) {
+#pragma unroll
+    for (int u = 0; u < kLaneEntries; ++u) {
+        const int s = off + u * kWarp + lane;
+        c[u] = (u < K) ? P.cols[s] : -1;
+        v[u] = (u < K) ? P.vals[s] : T(0);
+    }
+}
+
 // Forward substitution with the unit lower factor: y = L^{-1} (scale * b).
 // With `scale` non-null, b is rescaled on the fly and the rescaled value is written back
 // to b (GMRES uses this to normalise the new Krylov vector in the same pass).
 // y must hold the sentinel everywhere on entry; each row publishes its value once.
-template <class T>
+// G lanes per row: 1 (rows of up to kLaneEntries entries progressive, longer rows
+// blocking) or 2 .. 32 (group_rows; the packing guarantees K <= kLaneEntries).
+template <class T, int G>
 __global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
     sptrsv_lower_kernel(PackedTri<T> L, T* b, const double* scale, T* y, unsigned* counter, int* status,
                         const int* gate, int step) {
     if (gate_closed(gate, step)) return;
     const int lane = threadIdx.x & 31;
+    const bool lead = (lane & (G - 1)) == 0;  // the lane that owns the row's right-hand side
     const T sc = scale ? static_cast<T>(*scale) : T(1);
     int t = draw_ticket(counter, L.ntask, lane);
     while (t < L.ntask) {
@@ -354,28 +445,26 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
         const int off = L.off[t];
         const int K = L.len[t];
         T acc = T(0);
-        if (row >= 0) {
+        if (row >= 0 && lead) {
             acc = b[row];
             if (scale) acc = acc * sc;
         }
         const T acc0 = acc;
-        if (K <= kLaneEntries) {
+        if (G > 1 || K <= kLaneEntries) {
             int c[kLaneEntries];
             T v[kLaneEntries];
-#pragma unroll
-            for (int u = 0; u < kLaneEntries; ++u) {
-                const int s = off + u * kWarp + lane;
-                c[u] = (u < K) ? L.cols[s] : -1;
-                v[u] = (u < K) ? L.vals[s] : T(0);
-            }
-            progressive_rows<T, false>(row, K, c, v, acc, T(1), y, y, status);
+            load_lane_entries(L, off, K, lane, c, v);
+            if (G > 1)
+                group_rows<T, false, G>(row, K, lane, c, v, acc, T(1), y, y, status);
+            else
+                progressive_rows<T, false>(row, K, c, v, acc, T(1), y, y, status);
         } else {
             acc = blocking_row(off, K, lane, L.cols, L.vals, acc, y, status);
             if (row >= 0) st_relaxed(y + row, Sentinel<T>::canon(acc));
         }
         // the normalised Krylov vector is written back after the row is published: a
         // plain store ahead of the waits would delay them
-        if (scale && row >= 0) b[row] = acc0;
+        if (scale && row >= 0 && lead) b[row] = acc0;
         t = tn;
     }
 }
@@ -384,11 +473,12 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
 // rows it depends on.  x must hold the sentinel everywhere on entry.  y is left as it
 // is (the caller resets it to the sentinel before the next forward sweep, off the
 // dependency chain: a store into y here doubles this kernel's time).
-template <class T>
+template <class T, int G>
 __global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
     sptrsv_upper_kernel(PackedTri<T> U, T* y, T* x, unsigned* counter, int* status, const int* gate, int step) {
     if (gate_closed(gate, step)) return;
     const int lane = threadIdx.x & 31;
+    const bool lead = (lane & (G - 1)) == 0;
     int t = draw_ticket(counter, U.ntask, lane);
     while (t < U.ntask) {
         const int tn = draw_ticket(counter, U.ntask, lane);
@@ -399,17 +489,15 @@ __global__ void __launch_bounds__(kSolveWarps * kWarp, 1)
         // the diagonal is loaded before the dependency waits: the waits are ordered
         // memory operations, so a load after them would add a full round trip per level
         const T d = U.dvals[q];
-        const T acc = row >= 0 ? y[row] : T(0);
-        if (K <= kLaneEntries) {
+        const T acc = (row >= 0 && lead) ? y[row] : T(0);
+        if (G > 1 || K <= kLaneEntries) {
             int c[kLaneEntries];
             T v[kLaneEntries];
-#pragma unroll
-            for (int u = 0; u < kLaneEntries; ++u) {
-                const int s = off + u * kWarp + lane;
-                c[u] = (u < K) ? U.cols[s] : -1;
-                v[u] = (u < K) ? U.vals[s] : T(0);
-            }
-            progressive_rows<T, true>(row, K, c, v, acc, d, x, x, status);
+            load_lane_entries(U, off, K, lane, c, v);
+            if (G > 1)
+                group_rows<T, true, G>(row, K, lane, c, v, acc, d, x, x, status);
+            else
+                progressive_rows<T, true>(row, K, c, v, acc, d, x, x, status);
         } else {
             const T r = blocking_row(off, K, lane, U.cols, U.vals, acc, x, status);
             if (row >= 0) st_relaxed(x + row, Sentinel<T>::canon(sizeof(T) == 8 ? r / d : r * d));
@@ -564,7 +652,7 @@ __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)
                                                   T* xs, int base, T* out, unsigned remote, int ex, int* status) {
     int k = 0;
     bool done = row < 0;
-    long long rounds = 0;
+    WaitBudget wb;
     while (!__all_sync(0xffffffffu, done)) {
         if (!done) {
             T x[KM];
@@ -592,11 +680,10 @@ __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)
                 done = true;
             }
         }
-        if (++rounds >= kSpinLimit) {
+        if (wb.expired(status)) {
             if (!done) atomicExch(status + kStatusTimeout, 1);
             break;
         }
-        if ((rounds & 1023) == 0 && ld_relaxed_int(status + kStatusTimeout) != 0) break;
     }
 }
 
@@ -614,10 +701,8 @@ __device__ __noinline__ T block_long_row(int off, int K, int lane, const int* co
             if (c >= 0) {
                 x = wait_value(out + c, status);
             } else {
-                for (long long it = 0; it < kSpinLimit && Sentinel<T>::is(x); ++it) {
-                    x = ld_volatile_shared(xs + (-2 - c));
-                    if ((it & 1023) == 1023 && ld_relaxed_int(status + kStatusTimeout) != 0) break;
-                }
+                WaitBudget wb;
+                while (Sentinel<T>::is(x) && !wb.expired(status)) x = ld_volatile_shared(xs + (-2 - c));
                 if (Sentinel<T>::is(x)) {
                     atomicExch(status + kStatusTimeout, 1);
                     x = T(0);

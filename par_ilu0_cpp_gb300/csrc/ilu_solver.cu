@@ -23,55 +23,73 @@
 
 namespace gb300 {
 
-// Host construction of a packed factor from a schedule `order` (rows in level order).
-// lower: entries [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1])
-// descending plus the diagonal position.
+// Lanes per row of the level-ordered kernels for a triangle whose rows have at most
+// `kmax` entries: 1 while a row fits one lane's registers, else the smallest group that
+// holds kmax entries in kLaneEntries per lane; rows too long for kRowLanesMax lanes keep
+// one lane per row (blocking path).  `requested`: 1 forces one lane per row, > 1 raises
+// the group to at least that many lanes.
+static int row_lanes_for(int kmax, int requested) {
+    if (requested == 1) return 1;
+    int g = 1;
+    while (g < kRowLanesMax && ceil_div(kmax, g) > kLaneEntries) g *= 2;
+    if (ceil_div(kmax, g) > kLaneEntries) return 1;
+    while (g < requested && g < kRowLanesMax) g *= 2;
+    return g;
+}
+
+// Host construction of a packed factor from a schedule `order` (rows in level order),
+// `group` lanes per row (PackedTri layout).  lower: entries [rp[r], diag[r]) ascending;
+// upper: entries (diag[r], rp[r+1]) descending plus the diagonal position.
 static void build_level_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag,
-                       const std::vector<int>& order, bool lower, LevelPack& P, cudaStream_t s) {
-    const int ntask = ceil_div(n, kWarp);
+                             const std::vector<int>& order, bool lower, int group, LevelPack& P, cudaStream_t s) {
+    const int per_task = kWarp / group;  // rows per task
+    const int ntask = ceil_div(n, per_task);
     std::vector<int> rows(static_cast<size_t>(ntask) * kWarp, -1);
     std::vector<int> off(ntask), len(ntask);
     std::vector<int> dsrc(lower ? 0 : static_cast<size_t>(ntask) * kWarp, -1);
+    auto count = [&](int r) { return lower ? diag[r] - rp[r] : rp[r + 1] - diag[r] - 1; };
     long long slots = 0;
     for (int t = 0; t < ntask; ++t) {
         int k = 0;
-        for (int l = 0; l < kWarp; ++l) {
-            const int q = t * kWarp + l;
+        for (int i = 0; i < per_task; ++i) {
+            const long long q = static_cast<long long>(t) * per_task + i;
             if (q >= n) break;
             const int r = order[q];
-            rows[q] = r;
-            const int cnt = lower ? diag[r] - rp[r] : rp[r + 1] - diag[r] - 1;
-            k = std::max(k, cnt);
-            if (!lower) dsrc[q] = diag[r];
+            k = std::max(k, count(r));
+            for (int j = 0; j < group; ++j) {
+                rows[static_cast<size_t>(t) * kWarp + i * group + j] = r;
+                if (!lower) dsrc[static_cast<size_t>(t) * kWarp + i * group + j] = diag[r];
+            }
         }
         off[t] = static_cast<int>(slots);
-        len[t] = k;
-        slots += static_cast<long long>(k) * kWarp;
+        len[t] = ceil_div(k, group);
+        if (group > 1 && len[t] > kLaneEntries) throw std::runtime_error("lane group too small for the row length");
+        slots += static_cast<long long>(len[t]) * kWarp;
         if (slots > INT_MAX) throw std::runtime_error("triangular factor too large for 32-bit slot offsets");
     }
     std::vector<int> cols(static_cast<size_t>(slots), -1), src(static_cast<size_t>(slots), -1);
     for (int t = 0; t < ntask; ++t) {
-        for (int l = 0; l < kWarp; ++l) {
-            const int q = t * kWarp + l;
+        for (int i = 0; i < per_task; ++i) {
+            const long long q = static_cast<long long>(t) * per_task + i;
             if (q >= n) break;
             const int r = order[q];
-            int k = 0;
+            int e = 0;  // entry index within the row, in accumulation order
+            auto put = [&](int p) {
+                const int l = i * group + e / len[t];
+                const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(e % len[t]) * kWarp + l;
+                cols[sidx] = ci[p];
+                src[sidx] = p;
+                ++e;
+            };
             if (lower) {
-                for (int p = rp[r]; p < diag[r]; ++p, ++k) {
-                    const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
-                    cols[sidx] = ci[p];
-                    src[sidx] = p;
-                }
+                for (int p = rp[r]; p < diag[r]; ++p) put(p);
             } else {
-                for (int p = rp[r + 1] - 1; p > diag[r]; --p, ++k) {
-                    const size_t sidx = static_cast<size_t>(off[t]) + static_cast<size_t>(k) * kWarp + l;
-                    cols[sidx] = ci[p];
-                    src[sidx] = p;
-                }
+                for (int p = rp[r + 1] - 1; p > diag[r]; --p) put(p);
             }
         }
     }
     P.ntask = ntask;
+    P.group = group;
     P.slots = slots;
     P.rows.upload(rows.data(), rows.size(), s);
     P.off.upload(off.data(), off.size(), s);
@@ -87,6 +105,37 @@ static void build_level_pack(int n, const int* rp, const int* ci, const std::vec
     }
     // host vectors must outlive the asynchronous copies
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
+}
+
+// Level-ordered sweeps, dispatched on the factor's lanes per row.
+template <class T>
+static void launch_level_lower(const LevelPack& L, int grid, int threads, cudaStream_t s, T* b, const double* scale,
+                               T* y, unsigned* counter, int* status, const int* gate, int step) {
+    const PackedTri<T> P = L.view<T>();
+    switch (L.group) {
+        case 1: sptrsv_lower_kernel<T, 1><<<grid, threads, 0, s>>>(P, b, scale, y, counter, status, gate, step); break;
+        case 2: sptrsv_lower_kernel<T, 2><<<grid, threads, 0, s>>>(P, b, scale, y, counter, status, gate, step); break;
+        case 4: sptrsv_lower_kernel<T, 4><<<grid, threads, 0, s>>>(P, b, scale, y, counter, status, gate, step); break;
+        case 8: sptrsv_lower_kernel<T, 8><<<grid, threads, 0, s>>>(P, b, scale, y, counter, status, gate, step); break;
+        case 16: sptrsv_lower_kernel<T, 16><<<grid, threads, 0, s>>>(P, b, scale, y, counter, status, gate, step); break;
+        case 32: sptrsv_lower_kernel<T, 32><<<grid, threads, 0, s>>>(P, b, scale, y, counter, status, gate, step); break;
+        default: throw std::runtime_error("unsupported lanes per row");
+    }
+}
+
+template <class T>
+static void launch_level_upper(const LevelPack& U, int grid, int threads, cudaStream_t s, T* y, T* x,
+                               unsigned* counter, int* status, const int* gate, int step) {
+    const PackedTri<T> P = U.view<T>();
+    switch (U.group) {
+        case 1: sptrsv_upper_kernel<T, 1><<<grid, threads, 0, s>>>(P, y, x, counter, status, gate, step); break;
+        case 2: sptrsv_upper_kernel<T, 2><<<grid, threads, 0, s>>>(P, y, x, counter, status, gate, step); break;
+        case 4: sptrsv_upper_kernel<T, 4><<<grid, threads, 0, s>>>(P, y, x, counter, status, gate, step); break;
+        case 8: sptrsv_upper_kernel<T, 8><<<grid, threads, 0, s>>>(P, y, x, counter, status, gate, step); break;
+        case 16: sptrsv_upper_kernel<T, 16><<<grid, threads, 0, s>>>(P, y, x, counter, status, gate, step); break;
+        case 32: sptrsv_upper_kernel<T, 32><<<grid, threads, 0, s>>>(P, y, x, counter, status, gate, step); break;
+        default: throw std::runtime_error("unsupported lanes per row");
+    }
 }
 
 static void gather_level_pack(const LevelPack& P, bool lower, const double* lu, cudaStream_t s, int sms) {
@@ -508,8 +557,7 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
         return;
     }
     if (L.ntask == 0) return;
-    sptrsv_lower_kernel<T><<<grid_solve, solve_threads, 0, s>>>(L.view<T>(), b, scale, y, counters.get() + 1,
-                                                                status.get(), gate, step);
+    launch_level_lower<T>(L, grid_solve, solve_threads, s, b, scale, y, counters.get() + 1, status.get(), gate, step);
 }
 
 template <class T>
@@ -520,8 +568,7 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
         return;
     }
     if (U.ntask == 0) return;
-    sptrsv_upper_kernel<T><<<grid_solve, solve_threads, 0, s>>>(U.view<T>(), y, x, counters.get() + 2, status.get(),
-                                                                gate, step);
+    launch_level_upper<T>(U, grid_solve, solve_threads, s, y, x, counters.get() + 2, status.get(), gate, step);
 }
 
 template <class T>
@@ -536,6 +583,13 @@ template void IluSolver::Impl::launch_lower<double>(cudaStream_t, double*, const
 template void IluSolver::Impl::launch_lower<float>(cudaStream_t, float*, const double*, float*, const int*, int) const;
 template void IluSolver::Impl::launch_upper<double>(cudaStream_t, double*, double*, const int*, int) const;
 template void IluSolver::Impl::launch_upper<float>(cudaStream_t, float*, float*, const int*, int) const;
+
+void IluSolver::Impl::push_wait_limit() {
+    if (!status.get()) return;
+    GB_CUDA_CHECK(cudaMemcpyAsync(status.get() + kStatusWaitLimitUs, &wait_limit_us, sizeof(int),
+                                  cudaMemcpyHostToDevice, stream));
+    GB_CUDA_CHECK(cudaStreamSynchronize(stream));
+}
 
 void IluSolver::Impl::check_status(cudaStream_t s) {
     int h[kStatusWords];
@@ -600,6 +654,7 @@ void IluSolver::SetupMatrix() {
     GB_CUDA_CHECK(cudaMemsetAsync(im.counters.get(), 0, sizeof(unsigned) * 8, s));
     im.status.reserve(kStatusWords);
     GB_CUDA_CHECK(cudaMemsetAsync(im.status.get(), 0, sizeof(int) * kStatusWords, s));
+    im.push_wait_limit();
     ++im.setup_gen;
     im.blk64 = im.blk32 = false;
     if (im.block_rows >= 0) {
@@ -639,8 +694,13 @@ void IluSolver::SetupMatrix() {
     }
     im.level_packs = !(im.blk64 && im.blk32);
     if (im.level_packs) {
-        build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, im.L, s);
-        build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, im.U, s);
+        int kl = 0, ku = 0;
+        for (int r = 0; r < n; ++r) {
+            kl = std::max(kl, im.an.diag[r] - rp[r]);
+            ku = std::max(ku, rp[r + 1] - im.an.diag[r] - 1);
+        }
+        build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, row_lanes_for(kl, im.row_lanes), im.L, s);
+        build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, row_lanes_for(ku, im.row_lanes), im.U, s);
     }
     const size_t nv = static_cast<size_t>(std::max(n, 1));
     im.sb64.reserve(nv);
@@ -649,20 +709,44 @@ void IluSolver::SetupMatrix() {
     im.sy32.reserve(nv);
     fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
     fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
-    im.grid_fact = persistent_grid(ilu_factor_kernel, kFactWarps * kWarp, im.dev.sms);
-    // Level-ordered kernels: warps draw 32-row tasks in level order and spin on the rows
-    // they depend on.  Rows of up to kLaneEntries entries poll in rounds and want many
-    // warps ahead (1,216 warps best on the 128^3 7-point factor, ~64 levels ahead on the
-    // 256^2 5-point one); longer rows spin in blocking waits, and warps far ahead of the
-    // critical path then slow its L2 handoffs (27-point ILU(1), ~10 tasks per level:
-    // 5.7 ms per sweep at ~40 warps, 8.5 ms at 480 or more).  Automatic:
-    // kSolveLevelsAhead (short rows) or kSolveLevelsAheadLong (long rows) levels' worth
-    // of warps, spread over the SMs.
+    // Factorisation launch: rows staged in shared memory up to the longest row where a
+    // warp's share fits (fewer warps per block for long rows), a wider register window
+    // of the next pivot row when pivot rows are long.
+    {
+        int maxlen = 0, maxup = 0;
+        for (int r = 0; r < n; ++r) {
+            maxlen = std::max(maxlen, rp[r + 1] - rp[r]);
+            maxup = std::max(maxup, rp[r + 1] - im.an.diag[r] - 1);
+        }
+        int cap = std::max(kFactCap, ceil_div(maxlen, kWarp) * kWarp);
+        const int cap_max = kFactSmemMax / kFactEntryBytes / kWarp * kWarp;
+        if (cap > cap_max) cap = cap_max;  // longer rows: global-memory elimination
+        int warps = kFactWarps;
+        while (warps > 1 && static_cast<long long>(warps) * cap * kFactEntryBytes > kFactSmemMax) --warps;
+        im.fact_cap = cap;
+        im.fact_warps = warps;
+        im.fact_pre = maxup > 2 * kWarp ? 8 : 2;
+        im.fact_smem = static_cast<size_t>(warps) * cap * kFactEntryBytes;
+        auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
+        GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(im.fact_smem)));
+        int per_sm = 0;
+        GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * kWarp, im.fact_smem));
+        im.grid_fact = std::max(1, per_sm) * im.dev.sms;
+    }
+    // Level-ordered kernels: warps draw tasks in level order and spin on the rows they
+    // depend on.  Rows held in registers (one lane, or a group of lanes per row) poll in
+    // rounds and want many warps ahead (1,216 warps best on the 128^3 7-point factor, ~64
+    // levels ahead on the 256^2 5-point one); rows too long for a lane group spin in
+    // blocking waits, and warps far ahead of the critical path then slow its L2
+    // handoffs.  Automatic: kSolveLevelsAhead (rows in registers) or
+    // kSolveLevelsAheadLong (blocking rows) levels' worth of warps, spread over the SMs.
     {
         const int levels = std::max(1, std::max(im.an.nlev_l, im.an.nlev_u));
         const int tasks = std::max(im.L.ntask, im.U.ntask);
         const int cap = im.dev.sms * kSolveWarps;
-        const bool long_rows = n > 0 && (im.nnz - n) > 2ll * kLaneEntries * n;  // mean entries per triangle
+        const bool long_rows = n > 0 && (im.nnz - n) > 2ll * kLaneEntries * n &&  // mean entries per triangle
+                               (im.L.group == 1 || im.U.group == 1);
         const double ahead = long_rows ? kSolveLevelsAheadLong : kSolveLevelsAhead;
         int warps = im.solve_warps > 0 ? im.solve_warps
                                        : static_cast<int>(std::ceil(ahead * static_cast<double>(tasks) / levels));
@@ -689,7 +773,7 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
         if (im.nnz > 0)
             GB_CUDA_CHECK(cudaMemcpyAsync(im.lu.get(), values, sizeof(double) * static_cast<size_t>(im.nnz),
                                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-        int init[kStatusWords] = {0, 0, INT_MAX, 0};
+        int init[kStatusWords] = {0, 0, INT_MAX, im.wait_limit_us};
         GB_CUDA_CHECK(cudaMemcpyAsync(im.status.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
         if (++im.stamp == INT_MAX) {
             im.stamp = 1;
@@ -706,9 +790,10 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
             } else if (shift_kind == 1) {
                 shift = im.shift.get();
             }
-            ilu_factor_kernel<<<im.grid_fact, kFactWarps * kWarp, 0, s>>>(
+            auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
+            kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
                 n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(), shift, im.done.get(),
-                im.stamp, im.counters.get(), im.status.get());
+                im.stamp, im.counters.get(), im.status.get(), im.fact_cap);
             GB_CUDA_CHECK(cudaGetLastError());
             im.launches += 1;
             if (im.blk64) {
@@ -862,6 +947,7 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
     cudaStream_t s = im.stream;
     // what must start at zero (counters, status) and at the sentinel (y, x)
     GB_CUDA_CHECK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned) + kStatusWords * sizeof(int), s));
+    GB_CUDA_CHECK(cudaMemcpyAsync(status + kStatusWaitLimitUs, &im.wait_limit_us, sizeof(int), cudaMemcpyHostToDevice, s));
     fill_sentinel(y, n, s, im.dev.sms);
     fill_sentinel(d_x, n, s, im.dev.sms);
     double* b = const_cast<double*>(d_b);  // read only: no scale is passed to the forward sweep
@@ -869,10 +955,9 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
         launch_block<double, false>(im.LB64, s, b, nullptr, y, counters + 1, status, nullptr, 0);
         launch_block<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
     } else if (im.L.ntask > 0) {
-        sptrsv_lower_kernel<double><<<im.grid_solve, im.solve_threads, 0, s>>>(im.L.view<double>(), b, nullptr, y,
-                                                                            counters + 1, status, nullptr, 0);
-        sptrsv_upper_kernel<double><<<im.grid_solve, im.solve_threads, 0, s>>>(im.U.view<double>(), y, d_x, counters + 2,
-                                                                            status, nullptr, 0);
+        launch_level_lower<double>(im.L, im.grid_solve, im.solve_threads, s, b, nullptr, y, counters + 1, status,
+                                   nullptr, 0);
+        launch_level_upper<double>(im.U, im.grid_solve, im.solve_threads, s, y, d_x, counters + 2, status, nullptr, 0);
     }
     GB_CUDA_CHECK(cudaGetLastError());
     int h[kStatusWords];

@@ -206,3 +206,105 @@ def test_block_partition_does_not_change_results(golden, block_rows):
     gm.set_preconditioner(ilu)
     res = gm.solve(golden.a, golden.b)
     assert res.ok and abs(res.iterations - golden.gmres_iters) <= 1
+
+
+def banded(n, w, seed):
+    """Diagonally dominant matrix with full bandwidth w on both sides: rows of up to w
+    entries per triangle, a dependency chain of n levels."""
+    rng = np.random.default_rng(seed)
+    rows, cols = [], []
+    for i in range(n):
+        c = np.arange(max(0, i - w), min(n, i + w + 1))
+        rows.append(np.full(c.size, i))
+        cols.append(c)
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    v = rng.uniform(-1.0, 1.0, r.size)
+    v[r == c] = 2.0 * w + 2.0
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rp, r + 1, 1)
+    return g.Csr(n, np.cumsum(rp), c, v)
+
+
+ROW_LANE_CASES = [
+    # (name, matrix, fill level, automatic lanes per row of L)
+    ("lognormal27_12_k0", lambda: g.lognormal27(12, seed=3), 0, 2),
+    ("lognormal27_12_k1", lambda: g.lognormal27(12, seed=3), 1, 4),
+    ("lognormal27_12_k2", lambda: g.lognormal27(12, seed=3), 2, 8),
+    ("banded_100", lambda: banded(1500, 100, 4), 0, 16),
+    ("banded_200", lambda: banded(1200, 200, 5), 0, 32),
+    ("banded_300", lambda: banded(900, 300, 6), 0, 1),
+]
+
+
+def _setup_lanes(f, lanes):
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_ROW_LANES, lanes)
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    return ilu
+
+
+@pytest.mark.parametrize("name,make,lof,lanes", ROW_LANE_CASES, ids=[c[0] for c in ROW_LANE_CASES])
+def test_row_lanes_do_not_change_results(port, name, make, lof, lanes):
+    """Rows spread over a group of lanes are consumed in the same entry order as with one
+    lane per row: identical results in FP64 and in the mixed-precision solve."""
+    a = make()
+    f, _ = port.iluk_symbolic(a, lof) if lof else (a, None)
+    _, b = g.random_rhs(a, seed=7)
+    tol = 1e-8 * float(np.linalg.norm(b))
+    auto = _setup_lanes(f, 0)
+    assert auto.info().row_lanes_lower == lanes and auto.info().row_lanes_upper == lanes
+    x_auto = auto.substitute(b)
+    lu_ref, _ = port.factorize(f)
+    assert rel_err(x_auto, port.substitute(f, lu_ref, b)) <= 1e-12
+    results = {}
+    for req in (1, 0, 2, 4, 8, 16, 32):
+        ilu = auto if req == 0 else _setup_lanes(f, req)
+        if req > 1:
+            assert ilu.info().row_lanes_lower == (1 if lanes == 1 else max(lanes, req))
+        assert np.array_equal(ilu.substitute(b), x_auto), req
+        gm = api.Gmres(tol, 30, 1000)
+        gm.set_preconditioner(ilu)
+        gm.set_option(api.GMRES_OPT_MODE, 1)
+        res = gm.solve(a, b)
+        assert res.ok and true_residual(a, b, res.x) <= tol * 1.0001
+        results[req] = (res.iterations, res.x)
+    for req, (its, x) in results.items():
+        assert its == results[1][0] and np.array_equal(x, results[1][1]), req
+
+
+def test_row_lanes_option_checked():
+    ilu = api.IluSolver()
+    for bad in (3, 64, -1, 2.5):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_ROW_LANES, bad)
+
+
+def test_wait_limit_gives_up_and_solver_recovers(port):
+    """A device wait that reaches its limit gives up without faulting: the call reports
+    the timeout, and with the default limit back the same solver factorises and solves
+    correctly (a 1 us limit cuts short the real waits of a long dependency chain)."""
+    a = banded(1500, 100, 4)
+    _, b = g.random_rhs(a, seed=8)
+    lu_ref, _ = port.factorize(a)
+    x_ref = port.substitute(a, lu_ref, b)
+    ilu = api.IluSolver()
+    ilu.set_matrix(a)
+    assert ilu.setup() == 0, api.last_error()
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 1)
+    assert ilu.factorize() == -1
+    assert "timed out" in api.last_error()
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 0)
+    assert ilu.factorize() == 0, api.last_error()
+    assert rel_err(ilu.values(), lu_ref, floor=1e-300) <= 1e-12
+    x = ilu.substitute(b)
+    assert rel_err(x, x_ref) <= 1e-12
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 1)
+    with pytest.raises(RuntimeError, match="timed out"):
+        ilu.substitute(b)
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 0)
+    assert np.array_equal(ilu.substitute(b), x)
+    with pytest.raises(RuntimeError):
+        ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, -5)
