@@ -205,6 +205,27 @@ def _fill_owned(dst_ptr, a: Csr) -> None:
         ctypes.memmove(m.value, _f64(a.values).ctypes.data, 8 * a.nnz)
 
 
+class OwnedCsr:
+    """A CsrMatrix whose arrays the library allocates (SetupCsrMatrix: page-locked where
+    a GPU is usable, so host<->device copies run at full link speed), holding a copy of
+    ``a``.  Usable wherever a HostCsrView is."""
+
+    def __init__(self, a: Csr):
+        self.lib = load()
+        self.s = CsrMatrix()
+        _fill_owned(ctypes.pointer(self.s), a)
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.s)
+
+    def __del__(self):
+        try:
+            self.lib.LLJBASH_DestroyCsrMatrix(ctypes.byref(self.s))
+        except Exception:
+            pass
+
+
 def _owned_to_numpy(m: CsrMatrix) -> Csr:
     n = m.size
     rp = np.ctypeslib.as_array(m.row_ptr, shape=(n + 1,)).copy()
@@ -397,6 +418,16 @@ class Gmres:
         its = ctypes.c_int(0)
         ok = self.lib.LLJBASH_GmresSolve(self.h, view.ref, _dp(b), _dp(x), ctypes.byref(its))
         return SolveResult(bool(ok), int(its.value), x, self.report())
+
+    def solve_buffers(self, matrix, rhs: np.ndarray, x: np.ndarray):
+        """GmresSolve on caller-owned host buffers, without copies: ``matrix`` a
+        HostCsrView or OwnedCsr, ``rhs`` and ``x`` contiguous float64 arrays (``x`` holds
+        the initial guess and receives the solution).  Returns (ok, its)."""
+        assert rhs.dtype == np.float64 and x.dtype == np.float64
+        assert rhs.flags.c_contiguous and x.flags.c_contiguous
+        its = ctypes.c_int(0)
+        ok = self.lib.LLJBASH_GmresSolve(self.h, matrix.ref, _dp(rhs), _dp(x), ctypes.byref(its))
+        return bool(ok), int(its.value)
 
     def solve_device(self, n: int, d_rp: int, d_ci: int, d_val: int, d_rhs: int, d_sol: int):
         """GMRES on device-resident operands (int device addresses); returns (ok, its)."""

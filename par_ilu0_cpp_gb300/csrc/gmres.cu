@@ -153,16 +153,17 @@ void enqueue_piece(PreconditionedGmres::Impl& g, const IluSolver::Impl* ilu, Kry
         spmv_kernel<T, T, T><<<g.grid_spmv, kSpmvWarps * kWarp, 0, st>>>(n, g.rp_p, g.ci_p, ValueOf<T>::get(g), Zs, W,
                                                                           gate, s, ilu ? K.y.get() : nullptr);
     });
+    const int cgs_grid = g.cgs_grid<T>(nchunks);
     L.run(kKDot, [&] {
-        cgs_dot_kernel<T><<<g.grid_blas, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.partial.get(), g.h1.get(),
+        cgs_dot_kernel<T><<<cgs_grid, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.partial.get(), g.h1.get(),
                                                                 g.counters.get(), gate);
     });
     L.run(kKAxpyDot, [&] {
-        cgs_axpy_dot_kernel<T><<<g.grid_blas, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.h1.get(),
+        cgs_axpy_dot_kernel<T><<<cgs_grid, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.h1.get(),
                                                                      g.partial.get(), g.h2.get(), g.counters.get(), gate);
     });
     L.run(kKAxpyNorm, [&] {
-        cgs_axpy_norm_kernel<T><<<g.grid_blas, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.h1.get(), g.h2.get(),
+        cgs_axpy_norm_kernel<T><<<cgs_grid, kBlasThreads, 0, st>>>(nchunks, ld, K.V.get(), s, g.h1.get(), g.h2.get(),
                                                                       g.partial.get(), g.counters.get(), ctl, H, gate);
     });
 }
@@ -289,7 +290,18 @@ void PreconditionedGmres::Impl::init_once() {
     GB_CUDA_CHECK(cudaEventCreate(&ev1));
     GB_CUDA_CHECK(cudaMallocHost(reinterpret_cast<void**>(&ctl_host), sizeof(GmresCtl)));
     grid_spmv = persistent_grid(spmv_kernel<double, double, double>, kSpmvWarps * kWarp, dev.sms, 8);
-    grid_blas = persistent_grid(cgs_axpy_dot_kernel<double>, kBlasThreads, dev.sms, 2);
+    // Gram-Schmidt grids per value type: the blocks all three kernels can keep resident
+    // (FP32: 2 per SM, FP64: 1), so an FP32 pass is not held to the FP64 kernels' warps.
+    auto resident = [&](auto k1, auto k2, auto k3) {
+        int a = 0, b = 0, c = 0;
+        GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k1, kBlasThreads, 0));
+        GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k2, kBlasThreads, 0));
+        GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k3, kBlasThreads, 0));
+        return std::max(1, std::min({a, b, c, 2})) * dev.sms;
+    };
+    grid_blas64 = resident(cgs_dot_kernel<double>, cgs_axpy_dot_kernel<double>, cgs_axpy_norm_kernel<double>);
+    grid_blas32 = resident(cgs_dot_kernel<float>, cgs_axpy_dot_kernel<float>, cgs_axpy_norm_kernel<float>);
+    grid_blas = std::max(grid_blas64, grid_blas32);
     grid_update = 4 * dev.sms;
     GB_CUDA_CHECK(cudaFuncSetAttribute(gmres_backsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sizeof(double) * (kMaxKrylov * kMaxKrylov + kMaxKrylov + 1))));

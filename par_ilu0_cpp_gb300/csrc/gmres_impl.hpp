@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device_util.hpp"
 #include "gmres.hpp"
 #include "gmres_kernels.cuh"
@@ -82,6 +84,19 @@ struct PreconditionedGmres::Impl {
     gb300::GmresCtl* ctl_host = nullptr;  // pinned mirror
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int grid_spmv = 0, grid_blas = 0, grid_update = 0;
+    int grid_blas64 = 0, grid_blas32 = 0;  // resident Gram-Schmidt blocks per value type
+
+    // Gram-Schmidt grid for `nchunks` row chunks of value type T: at most the resident
+    // blocks, and no more blocks than needed for every warp to take the same number of
+    // chunks (a warp with one chunk more than the others would set the pass's length).
+    template <class T>
+    int cgs_grid(long long nchunks) const {
+        const long long cap = sizeof(T) == 8 ? grid_blas64 : grid_blas32;
+        const long long warps = cap * gb300::kBlasWarps;
+        const long long per_warp = std::max<long long>(1, (nchunks + warps - 1) / warps);
+        const long long g = (nchunks + per_warp * gb300::kBlasWarps - 1) / (per_warp * gb300::kBlasWarps);
+        return static_cast<int>(std::max<long long>(1, std::min(g, cap)));
+    }
 
     int mode = gb300::kModePlain;
     double tau = 1e-6;             // mixed mode: relative reduction per inner cycle

@@ -226,7 +226,9 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
 // basis vector the lane's RPL products are summed in registers and reduced across the
 // warp once per chunk (one shuffle tree per 256/512 rows — cheap even with GB300's slow
 // FP64 pipe), and lane 0 adds the warp's sum into a per-warp shared-memory row.  FP32
-// bases form the chunk sums in FP32 and accumulate them in FP64.
+// bases keep the coefficients and the per-warp rows in FP32 (a warp adds a few chunk
+// sums) and sum the rows over warps and blocks in FP64, so their per-basis-vector loops
+// contain no FP64 instruction.
 // ---------------------------------------------------------------------------------
 template <class T>
 struct ChunkCfg;
@@ -287,10 +289,12 @@ __device__ __forceinline__ float warp_sum_any(float v) { return warp_sum_f(v); }
 
 // Adds, for j < nv, the dot product of V[j] with the lane's chunk of w (wv, registers) to
 // the warp's shared-memory row acc_row[j] (lane 0 writes).  r0: the lane's first row.
+// The row has the accumulation type (FP32 for FP32 bases): the loop over the basis runs
+// no FP64 instruction, GB300's FP64 pipe being far narrower than its memory.
 template <class T>
 __device__ __forceinline__ void chunk_dots_rows(const T* __restrict__ V, long long ld, int nv, long long r0,
                                                 const typename ChunkCfg<T>::Acc (&wv)[ChunkCfg<T>::RPL],
-                                                double* acc_row) {
+                                                typename ChunkCfg<T>::Acc* acc_row) {
     using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     const int lane = threadIdx.x & 31;
@@ -302,22 +306,25 @@ __device__ __forceinline__ void chunk_dots_rows(const T* __restrict__ V, long lo
 #pragma unroll
         for (int u = 0; u < RPL; ++u) p = fma(static_cast<Acc>(v[u]), wv[u], p);
         p = warp_sum_any(p);
-        if (lane == 0) acc_row[j] += static_cast<double>(p);
+        if (lane == 0) acc_row[j] += p;
     }
 }
 
-// Sums the per-warp rows acc_s[w][j] over warps into the block partials (all threads).
-__device__ __forceinline__ void warp_rows_to_partial(double (*acc_s)[kMaxKrylov + 1], int nv, double* partial) {
+// Sums the per-warp rows acc_s[w][j] over warps, in FP64, into the block partials (all
+// threads).
+template <class Acc>
+__device__ __forceinline__ void warp_rows_to_partial(Acc (*acc_s)[kMaxKrylov + 1], int nv, double* partial) {
     __syncthreads();
     for (int j = threadIdx.x; j < nv; j += blockDim.x) {
         double s = 0.0;
-        for (int k = 0; k < kBlasWarps; ++k) s += acc_s[k][j];
+        for (int k = 0; k < kBlasWarps; ++k) s += static_cast<double>(acc_s[k][j]);
         partial[static_cast<size_t>(blockIdx.x) * kPartialStride + j] = s;
     }
 }
 
-__device__ __forceinline__ void zero_warp_rows(double (*acc_s)[kMaxKrylov + 1], int nv) {
-    for (int e = threadIdx.x; e < kBlasWarps * (kMaxKrylov + 1); e += blockDim.x) (&acc_s[0][0])[e] = 0.0;
+template <class Acc>
+__device__ __forceinline__ void zero_warp_rows(Acc (*acc_s)[kMaxKrylov + 1], int nv) {
+    for (int e = threadIdx.x; e < kBlasWarps * (kMaxKrylov + 1); e += blockDim.x) (&acc_s[0][0])[e] = Acc(0);
     __syncthreads();
     (void)nv;
 }
@@ -330,7 +337,7 @@ __global__ void __launch_bounds__(kBlasThreads)
     using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     constexpr int R = kWarp * RPL;
-    __shared__ double acc_s[kBlasWarps][kMaxKrylov + 1];
+    __shared__ Acc acc_s[kBlasWarps][kMaxKrylov + 1];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int nv = s + 1;
@@ -359,12 +366,12 @@ __global__ void __launch_bounds__(kBlasThreads)
     using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     constexpr int R = kWarp * RPL;
-    __shared__ double acc_s[kBlasWarps][kMaxKrylov + 1];
-    __shared__ double sh[kMaxKrylov + 1];
+    __shared__ Acc acc_s[kBlasWarps][kMaxKrylov + 1];
+    __shared__ Acc sh[kMaxKrylov + 1];  // coefficients in the accumulation type, converted once
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int nv = s + 1;
-    for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = __ldcg(h1 + j);
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = static_cast<Acc>(__ldcg(h1 + j));
     zero_warp_rows(acc_s, nv);
     T* wvec = V + static_cast<long long>(s + 1) * ld;
     for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
@@ -378,7 +385,7 @@ __global__ void __launch_bounds__(kBlasThreads)
         for (int j = 0; j < nv; ++j) {
             T v[RPL];
             load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
-            const Acc hj = static_cast<Acc>(sh[j]);
+            const Acc hj = sh[j];
 #pragma unroll
             for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
         }
@@ -470,21 +477,21 @@ __global__ void __launch_bounds__(kBlasThreads)
                          const double* __restrict__ h2, double* partial, unsigned* counter, GmresCtl* ctl, Hess H,
                          const int* gate) {
     if (gate_closed(gate, s)) return;
+    using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     constexpr int R = kWarp * RPL;
-    __shared__ double sh[kMaxKrylov + 1];
+    __shared__ Acc sh[kMaxKrylov + 1];  // coefficients in the accumulation type, converted once
     __shared__ double s_red[kBlasWarps];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int nv = s + 1;
-    for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = __ldcg(h2 + j);
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) sh[j] = static_cast<Acc>(__ldcg(h2 + j));
     __syncthreads();
     T* wv = V + static_cast<long long>(s + 1) * ld;
     double ss = 0.0;
     for (long long c = blockIdx.x * static_cast<long long>(kBlasWarps) + w; c < nchunks;
          c += static_cast<long long>(gridDim.x) * kBlasWarps) {
         const long long r0 = c * R + lane * RPL;
-        using Acc = typename ChunkCfg<T>::Acc;
         T a[RPL];
         Acc x[RPL];
         load_rpl<T>(wv + r0, a);
@@ -493,15 +500,15 @@ __global__ void __launch_bounds__(kBlasThreads)
         for (int j = 0; j < nv; ++j) {
             T v[RPL];
             load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
-            const Acc hj = static_cast<Acc>(sh[j]);
+            const Acc hj = sh[j];
 #pragma unroll
             for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
         }
-        typename ChunkCfg<T>::Acc q = 0;
+        Acc q = 0;
 #pragma unroll
         for (int u = 0; u < RPL; ++u) {
             a[u] = static_cast<T>(x[u]);
-            q = fma(static_cast<typename ChunkCfg<T>::Acc>(a[u]), static_cast<typename ChunkCfg<T>::Acc>(a[u]), q);
+            q = fma(static_cast<Acc>(a[u]), static_cast<Acc>(a[u]), q);
         }
         ss += static_cast<double>(q);
         store_rpl<T>(wv + r0, a);

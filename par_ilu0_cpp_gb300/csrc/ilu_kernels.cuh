@@ -223,8 +223,9 @@ constexpr int kLaneEntries = 8;  // entries a lane holds in registers
 constexpr int kRowLanesMax = 32;  // largest lane group per row (rows of up to 256 entries)
 // Automatic size of the level-ordered substitution grid: warps for this many levels of
 // tasks (averaged over the factor), at most kSolveWarps per SM.
-constexpr double kSolveLevelsAhead = 48.0;
-constexpr double kSolveLevelsAheadLong = 4.0;  // rows longer than kRowLanesMax * kLaneEntries
+constexpr double kSolveLevelsAhead = 48.0;      // one lane per row
+constexpr double kSolveLevelsAheadGroup = 10.0;  // lane groups (long rows)
+constexpr double kSolveLevelsAheadLong = 4.0;    // rows longer than kRowLanesMax * kLaneEntries
 
 // Per-lane progressive solve of a warp's 32 rows (one per lane), for rows with at most
 // kLaneEntries entries held in registers (c: column or -1, v: value).  Every round a

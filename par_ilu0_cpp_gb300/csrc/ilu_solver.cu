@@ -735,19 +735,20 @@ void IluSolver::SetupMatrix() {
         im.grid_fact = std::max(1, per_sm) * im.dev.sms;
     }
     // Level-ordered kernels: warps draw tasks in level order and spin on the rows they
-    // depend on.  Rows held in registers (one lane, or a group of lanes per row) poll in
-    // rounds and want many warps ahead (1,216 warps best on the 128^3 7-point factor, ~64
-    // levels ahead on the 256^2 5-point one); rows too long for a lane group spin in
+    // depend on.  Rows of one lane poll in rounds and want many warps ahead (1,216 warps
+    // best on the 128^3 7-point factor, ~64 levels ahead on the 256^2 5-point one); lane
+    // groups want about 10 levels ahead (27-point factors on 64^3: 300-400 warps, ILU(1)
+    // sweeps 1.0 ms against 1.34 ms at 1,216); rows too long for a lane group spin in
     // blocking waits, and warps far ahead of the critical path then slow its L2
-    // handoffs.  Automatic: kSolveLevelsAhead (rows in registers) or
-    // kSolveLevelsAheadLong (blocking rows) levels' worth of warps, spread over the SMs.
+    // handoffs.  Automatic: that many levels' worth of warps, spread over the SMs.
     {
         const int levels = std::max(1, std::max(im.an.nlev_l, im.an.nlev_u));
         const int tasks = std::max(im.L.ntask, im.U.ntask);
         const int cap = im.dev.sms * kSolveWarps;
         const bool long_rows = n > 0 && (im.nnz - n) > 2ll * kLaneEntries * n &&  // mean entries per triangle
                                (im.L.group == 1 || im.U.group == 1);
-        const double ahead = long_rows ? kSolveLevelsAheadLong : kSolveLevelsAhead;
+        const bool groups = im.L.group > 1 || im.U.group > 1;
+        const double ahead = long_rows ? kSolveLevelsAheadLong : (groups ? kSolveLevelsAheadGroup : kSolveLevelsAhead);
         int warps = im.solve_warps > 0 ? im.solve_warps
                                        : static_cast<int>(std::ceil(ahead * static_cast<double>(tasks) / levels));
         warps = std::max(1, std::min(cap, warps));

@@ -285,12 +285,14 @@ def test_row_lanes_option_checked():
 def test_wait_limit_gives_up_and_solver_recovers(port):
     """A device wait that reaches its limit gives up without faulting: the call reports
     the timeout, and with the default limit back the same solver factorises and solves
-    correctly (a 1 us limit cuts short the real waits of a long dependency chain)."""
+    correctly (a 1 us limit cuts short the real waits of a long dependency chain; the
+    sweeps get a warp per task, so tasks far down the 1,500-level chain wait long)."""
     a = banded(1500, 100, 4)
     _, b = g.random_rhs(a, seed=8)
     lu_ref, _ = port.factorize(a)
     x_ref = port.substitute(a, lu_ref, b)
     ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_SOLVE_WARPS, 1024)
     ilu.set_matrix(a)
     assert ilu.setup() == 0, api.last_error()
     ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 1)
