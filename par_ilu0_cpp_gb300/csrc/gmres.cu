@@ -47,7 +47,7 @@ PreconditionedGmres::~PreconditionedGmres() {
 
 namespace {
 
-constexpr long long kLdAlign = 512;  // whole CGS chunks of 512 rows
+constexpr long long kLdAlign = 512;  // whole Gram-Schmidt chunks (at most 256 rows)
 
 template <class T>
 void ensure_krylov(Krylov<T>& K, int n, int im, cudaStream_t s, int sms) {

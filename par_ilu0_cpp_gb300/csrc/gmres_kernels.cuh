@@ -220,93 +220,165 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
 //   axpy_dot:    w <- w - V h1;  h2 = V^T w
 //   axpy_norm:   w <- w - V h2;  ||w||; then (last block) H(:,s) = h1 + h2,
 //                H(s+1,s) = ||w||, Givens update and loop control.
-// Work split: each warp owns chunks of R = 32 * RPL consecutive rows, lane l the RPL
-// contiguous rows [l RPL, (l+1) RPL) of a chunk, so every load of a basis vector is one
-// fully coalesced 1-2 KB access per warp.  The chunk of w stays in registers; for each
-// basis vector the lane's RPL products are summed in registers and reduced across the
-// warp once per chunk (one shuffle tree per 256/512 rows — cheap even with GB300's slow
-// FP64 pipe), and lane 0 adds the warp's sum into a per-warp shared-memory row.  FP32
-// bases keep the coefficients and the per-warp rows in FP32 (a warp adds a few chunk
-// sums) and sum the rows over warps and blocks in FP64, so their per-basis-vector loops
-// contain no FP64 instruction.
+// Work split: each warp owns chunks of R = 32 * RPL consecutive rows (128 FP32 / 256
+// FP64), lane l the RPL contiguous rows [l RPL, (l+1) RPL) of a chunk, so every load of
+// a basis vector is one fully coalesced 512 B / 2 KB access per warp.  The chunk of w
+// stays in registers.  The basis is read JB vectors at a time, all loads of a batch in
+// flight together; for the dots, the lane's RPL products of each vector are summed in
+// registers and the JB sums are reduced across the warp together (warp_sum_batch), then
+// added into a per-warp shared-memory row.  Short chunks keep the axpy_dot pass's second
+// read of a warp's basis rows within L2's reach (2 KB chunks sent half of them to DRAM).
+// FP32 bases keep the coefficients and the per-warp rows in FP32 (a warp adds a few
+// chunk sums) and sum the rows over warps and blocks in FP64, so their per-basis-vector
+// loops contain no FP64 instruction.
 // ---------------------------------------------------------------------------------
+// Resident blocks per SM the Gram-Schmidt kernels are compiled for: two for FP32 (64
+// registers per thread), one for FP64 (whose kernels are bound by the FP64 pipe).
+template <class T>
+constexpr int kBlasMinBlocks = sizeof(T) == 4 ? 2 : 1;
+
 template <class T>
 struct ChunkCfg;
+// RPL: rows per lane (a chunk is 32 RPL rows, one 16-byte load per lane per 4 FP32 /
+// 2 FP64 rows); JB / JBA: basis vectors loaded (and, for dots, reduced) as one batch in
+// the dot pass / the passes with an axpy (smaller batches there stay clear of spills).
 template <>
 struct ChunkCfg<double> {
-    static constexpr int RPL = 16;
+    static constexpr int RPL = 8;
+    static constexpr int JB = 4;
+    static constexpr int JBA = 2;
     using Acc = double;
 };
 template <>
 struct ChunkCfg<float> {
-    static constexpr int RPL = 8;
+    static constexpr int RPL = 4;
+    static constexpr int JB = 8;
+    static constexpr int JBA = 4;
     using Acc = float;
 };
 
-template <class T>
-__device__ __forceinline__ void load_rpl(const T* p, T (&v)[ChunkCfg<T>::RPL]);
-template <>
-__device__ __forceinline__ void load_rpl<double>(const double* p, double (&v)[16]) {
+template <class T, int RPL>
+__device__ __forceinline__ void load_rpl(const T* p, T (&v)[RPL]) {
+    if constexpr (sizeof(T) == 4) {
+        static_assert(RPL % 4 == 0, "whole float4 loads");
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const double2 t = reinterpret_cast<const double2*>(p)[k];
-        v[2 * k] = t.x;
-        v[2 * k + 1] = t.y;
+        for (int k = 0; k < RPL / 4; ++k) {
+            const float4 t = reinterpret_cast<const float4*>(p)[k];
+            v[4 * k] = t.x;
+            v[4 * k + 1] = t.y;
+            v[4 * k + 2] = t.z;
+            v[4 * k + 3] = t.w;
+        }
+    } else {
+        static_assert(RPL % 2 == 0, "whole double2 loads");
+#pragma unroll
+        for (int k = 0; k < RPL / 2; ++k) {
+            const double2 t = reinterpret_cast<const double2*>(p)[k];
+            v[2 * k] = t.x;
+            v[2 * k + 1] = t.y;
+        }
     }
 }
-template <>
-__device__ __forceinline__ void load_rpl<float>(const float* p, float (&v)[8]) {
+template <class T, int RPL>
+__device__ __forceinline__ void store_rpl(T* p, const T (&v)[RPL]) {
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const float4 t = reinterpret_cast<const float4*>(p)[k];
-        v[4 * k] = t.x;
-        v[4 * k + 1] = t.y;
-        v[4 * k + 2] = t.z;
-        v[4 * k + 3] = t.w;
+        for (int k = 0; k < RPL / 4; ++k)
+            reinterpret_cast<float4*>(p)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < RPL / 2; ++k) reinterpret_cast<double2*>(p)[k] = make_double2(v[2 * k], v[2 * k + 1]);
     }
-}
-template <class T>
-__device__ __forceinline__ void store_rpl(T* p, const T (&v)[ChunkCfg<T>::RPL]);
-template <>
-__device__ __forceinline__ void store_rpl<double>(double* p, const double (&v)[16]) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) reinterpret_cast<double2*>(p)[k] = make_double2(v[2 * k], v[2 * k + 1]);
-}
-template <>
-__device__ __forceinline__ void store_rpl<float>(float* p, const float (&v)[8]) {
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-        reinterpret_cast<float4*>(p)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
 }
 
-__device__ __forceinline__ float warp_sum_f(float v) {
+// Sums each of the JB per-lane values a[0..JB) over the warp (JB a power of two <= 32)
+// with JB - 1 + log2(32 / JB) shuffles instead of 5 JB: each halving step keeps half of
+// the values in each lane and adds the partner lane's copy of that half.  Lane l ends
+// with the full sum of value batch_index<JB>(l); the lanes whose low log2(32 / JB) bits
+// are zero hold distinct values.
+template <int JB, class A>
+__device__ __forceinline__ A warp_sum_batch(A (&a)[JB], int lane) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int h = JB / 2, o = 16; h >= 1; h >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const A send = up ? a[i] : a[i + h];
+            const A keep = up ? a[i + h] : a[i];
+            a[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    A v = a[0];
+#pragma unroll
+    for (int o = 16 / JB; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
-__device__ __forceinline__ double warp_sum_any(double v) { return warp_sum(v); }
-__device__ __forceinline__ float warp_sum_any(float v) { return warp_sum_f(v); }
+template <int JB>
+__device__ __forceinline__ int batch_index(int lane) {
+    int q = 0;
+#pragma unroll
+    for (int h = JB / 2, o = 16; h >= 1; h >>= 1, o >>= 1)
+        if (lane & o) q += h;
+    return q;
+}
 
 // Adds, for j < nv, the dot product of V[j] with the lane's chunk of w (wv, registers) to
-// the warp's shared-memory row acc_row[j] (lane 0 writes).  r0: the lane's first row.
-// The row has the accumulation type (FP32 for FP32 bases): the loop over the basis runs
-// no FP64 instruction, GB300's FP64 pipe being far narrower than its memory.
-template <class T>
+// the warp's shared-memory row acc_row[j].  r0: the lane's first row.  The basis is read
+// in batches of JB vectors (all loads of a batch in flight together) and each batch is
+// reduced across the warp at once (warp_sum_batch).  The row has the accumulation type
+// (FP32 for FP32 bases): the loop over the basis runs no FP64 instruction, GB300's FP64
+// pipe being far narrower than its memory.
+template <class T, int JB>
 __device__ __forceinline__ void chunk_dots_rows(const T* __restrict__ V, long long ld, int nv, long long r0,
                                                 const typename ChunkCfg<T>::Acc (&wv)[ChunkCfg<T>::RPL],
                                                 typename ChunkCfg<T>::Acc* acc_row) {
     using Acc = typename ChunkCfg<T>::Acc;
     constexpr int RPL = ChunkCfg<T>::RPL;
     const int lane = threadIdx.x & 31;
-#pragma unroll 4
-    for (int j = 0; j < nv; ++j) {
-        T v[RPL];
-        load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
-        Acc p = Acc(0);
+    const int q = batch_index<JB>(lane);
+    const bool writer = (lane & (32 / JB - 1)) == 0;
+    for (int j0 = 0; j0 < nv; j0 += JB) {
+        T v[JB][RPL];
 #pragma unroll
-        for (int u = 0; u < RPL; ++u) p = fma(static_cast<Acc>(v[u]), wv[u], p);
-        p = warp_sum_any(p);
-        if (lane == 0) acc_row[j] += p;
+        for (int b = 0; b < JB; ++b)
+            if (j0 + b < nv) load_rpl<T, RPL>(V + static_cast<long long>(j0 + b) * ld + r0, v[b]);
+        Acc p[JB];
+#pragma unroll
+        for (int b = 0; b < JB; ++b) {
+            Acc t = Acc(0);
+            if (j0 + b < nv) {
+#pragma unroll
+                for (int u = 0; u < RPL; ++u) t = fma(static_cast<Acc>(v[b][u]), wv[u], t);
+            }
+            p[b] = t;
+        }
+        const Acc tot = warp_sum_batch<JB>(p, lane);
+        if (writer && j0 + q < nv) acc_row[j0 + q] += tot;
+    }
+}
+
+// x -= sum_j sh[j] V[j] over the lane's rows (ascending j, the FMA order of a plain
+// loop), the basis read in batches of JBA vectors.
+template <class T>
+__device__ __forceinline__ void chunk_axpy_rows(const T* __restrict__ V, long long ld, int nv, long long r0,
+                                                const typename ChunkCfg<T>::Acc* sh,
+                                                typename ChunkCfg<T>::Acc (&x)[ChunkCfg<T>::RPL]) {
+    using Acc = typename ChunkCfg<T>::Acc;
+    constexpr int RPL = ChunkCfg<T>::RPL;
+    constexpr int JB = ChunkCfg<T>::JBA;
+    for (int j0 = 0; j0 < nv; j0 += JB) {
+        T v[JB][RPL];
+#pragma unroll
+        for (int b = 0; b < JB; ++b)
+            if (j0 + b < nv) load_rpl<T, RPL>(V + static_cast<long long>(j0 + b) * ld + r0, v[b]);
+#pragma unroll
+        for (int b = 0; b < JB; ++b) {
+            if (j0 + b < nv) {
+                const Acc hj = sh[j0 + b];
+#pragma unroll
+                for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[b][u]), x[u]);
+            }
+        }
     }
 }
 
@@ -330,7 +402,7 @@ __device__ __forceinline__ void zero_warp_rows(Acc (*acc_s)[kMaxKrylov + 1], int
 }
 
 template <class T>
-__global__ void __launch_bounds__(kBlasThreads)
+__global__ void __launch_bounds__(kBlasThreads, kBlasMinBlocks<T>)
     cgs_dot_kernel(long long nchunks, long long ld, const T* __restrict__ V, int s, double* partial, double* h1,
                    unsigned* counter, const int* gate) {
     if (gate_closed(gate, s)) return;
@@ -347,11 +419,11 @@ __global__ void __launch_bounds__(kBlasThreads)
          c += static_cast<long long>(gridDim.x) * kBlasWarps) {
         const long long r0 = c * R + lane * RPL;
         T a[RPL];
-        load_rpl<T>(wvec + r0, a);
+        load_rpl<T, RPL>(wvec + r0, a);
         Acc wv[RPL];
 #pragma unroll
         for (int u = 0; u < RPL; ++u) wv[u] = static_cast<Acc>(a[u]);
-        chunk_dots_rows<T>(V, ld, nv, r0, wv, acc_s[w]);
+        chunk_dots_rows<T, ChunkCfg<T>::JB>(V, ld, nv, r0, wv, acc_s[w]);
     }
     warp_rows_to_partial(acc_s, nv, partial);
     if (!arrive_last(counter)) return;
@@ -359,7 +431,7 @@ __global__ void __launch_bounds__(kBlasThreads)
 }
 
 template <class T>
-__global__ void __launch_bounds__(kBlasThreads)
+__global__ void __launch_bounds__(kBlasThreads, kBlasMinBlocks<T>)
     cgs_axpy_dot_kernel(long long nchunks, long long ld, T* __restrict__ V, int s, const double* __restrict__ h1,
                         double* partial, double* h2, unsigned* counter, const int* gate) {
     if (gate_closed(gate, s)) return;
@@ -379,23 +451,17 @@ __global__ void __launch_bounds__(kBlasThreads)
         const long long r0 = c * R + lane * RPL;
         T a[RPL];
         Acc x[RPL];
-        load_rpl<T>(wvec + r0, a);
+        load_rpl<T, RPL>(wvec + r0, a);
 #pragma unroll
         for (int u = 0; u < RPL; ++u) x[u] = static_cast<Acc>(a[u]);
-        for (int j = 0; j < nv; ++j) {
-            T v[RPL];
-            load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
-            const Acc hj = sh[j];
-#pragma unroll
-            for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
-        }
+        chunk_axpy_rows<T>(V, ld, nv, r0, sh, x);
 #pragma unroll
         for (int u = 0; u < RPL; ++u) {
             a[u] = static_cast<T>(x[u]);
             x[u] = static_cast<Acc>(a[u]);  // the dots use the stored (rounded) values
         }
-        store_rpl<T>(wvec + r0, a);
-        chunk_dots_rows<T>(V, ld, nv, r0, x, acc_s[w]);
+        store_rpl<T, RPL>(wvec + r0, a);
+        chunk_dots_rows<T, ChunkCfg<T>::JBA>(V, ld, nv, r0, x, acc_s[w]);
     }
     warp_rows_to_partial(acc_s, nv, partial);
     if (!arrive_last(counter)) return;
@@ -472,7 +538,7 @@ __device__ __forceinline__ void arnoldi_control(GmresCtl* ctl, Hess H, int s, co
 }
 
 template <class T>
-__global__ void __launch_bounds__(kBlasThreads)
+__global__ void __launch_bounds__(kBlasThreads, kBlasMinBlocks<T>)
     cgs_axpy_norm_kernel(long long nchunks, long long ld, T* __restrict__ V, int s, const double* __restrict__ h1,
                          const double* __restrict__ h2, double* partial, unsigned* counter, GmresCtl* ctl, Hess H,
                          const int* gate) {
@@ -494,16 +560,10 @@ __global__ void __launch_bounds__(kBlasThreads)
         const long long r0 = c * R + lane * RPL;
         T a[RPL];
         Acc x[RPL];
-        load_rpl<T>(wv + r0, a);
+        load_rpl<T, RPL>(wv + r0, a);
 #pragma unroll
         for (int u = 0; u < RPL; ++u) x[u] = static_cast<Acc>(a[u]);
-        for (int j = 0; j < nv; ++j) {
-            T v[RPL];
-            load_rpl<T>(V + static_cast<long long>(j) * ld + r0, v);
-            const Acc hj = sh[j];
-#pragma unroll
-            for (int u = 0; u < RPL; ++u) x[u] = fma(-hj, static_cast<Acc>(v[u]), x[u]);
-        }
+        chunk_axpy_rows<T>(V, ld, nv, r0, sh, x);
         Acc q = 0;
 #pragma unroll
         for (int u = 0; u < RPL; ++u) {
@@ -511,7 +571,7 @@ __global__ void __launch_bounds__(kBlasThreads)
             q = fma(static_cast<Acc>(a[u]), static_cast<Acc>(a[u]), q);
         }
         ss += static_cast<double>(q);
-        store_rpl<T>(wv + r0, a);
+        store_rpl<T, RPL>(wv + r0, a);
     }
     ss = warp_sum(ss);
     if (lane == 0) s_red[w] = ss;
