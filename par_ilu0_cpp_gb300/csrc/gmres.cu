@@ -289,7 +289,7 @@ void PreconditionedGmres::Impl::init_once() {
     GB_CUDA_CHECK(cudaEventCreate(&ev0));
     GB_CUDA_CHECK(cudaEventCreate(&ev1));
     GB_CUDA_CHECK(cudaMallocHost(reinterpret_cast<void**>(&ctl_host), sizeof(GmresCtl)));
-    grid_spmv = persistent_grid(spmv_kernel<double, double, double>, kSpmvWarps * kWarp, dev.sms, 8);
+    grid_spmv = persistent_grid(spmv_kernel<double, double, double>, kSpmvWarps * kWarp, dev.sms, 16);
     // Gram-Schmidt grids per value type: the blocks all three kernels can keep resident
     // (FP32: 2 per SM, FP64: 1), so an FP32 pass is not held to the FP64 kernels' warps.
     auto resident = [&](auto k1, auto k2, auto k3) {

@@ -24,7 +24,6 @@ constexpr int kMaxKrylov = 128;       // largest supported restart length m
 constexpr int kBlasWarps = 16;        // warps per block of the vector kernels
 constexpr int kBlasThreads = kBlasWarps * kWarp;
 constexpr int kSpmvWarps = 4;
-constexpr int kSpmvStage = 768;       // CSR entries of one 32-row chunk staged in smem
 constexpr int kPartialStride = kMaxKrylov + 8;  // doubles per block in the partial buffers
 
 enum CtlStatus { kCtlRunning = 0, kCtlConverged = 1, kCtlNan = 2 };
@@ -90,40 +89,23 @@ __device__ __forceinline__ void reduce_partials(const double* partial, int nbloc
 }
 
 // ---------------------------------------------------------------------------------
-// CSR SpMV, one warp per chunk of 32 consecutive rows.  The chunk's entries are one
-// contiguous CSR range; they are staged in shared memory with coalesced loads and each
-// lane then sums its row in column order (as CsrMatVec, src/csr_matrix.cpp:163-171).
-// Chunks with more than kSpmvStage entries read their rows directly.
+// CSR SpMV, one row per thread: each thread sums its row in column order (as CsrMatVec,
+// src/csr_matrix.cpp:163-171) with the loads of up to 8 entries (columns, values, then
+// the x gathers) in flight at once.  No shared memory, so 64 warps per SM stay resident;
+// consecutive threads read consecutive rows, and their entry loads share cache lines.
+// (A warp-per-32-row-chunk layout staged through shared memory ran at 38% of HBM peak:
+// two dependent round trips per chunk and smem-limited occupancy.)
 // ---------------------------------------------------------------------------------
 // Row sums accumulate in the matrix's value type AT (FP64 for the plain path, FP32 for
 // the mixed-precision inner cycles, whose SpMV is FP32 throughout).
 template <class AT, class XT>
-__device__ __forceinline__ AT spmv_row_chunk(int n, const int* __restrict__ rp, const int* __restrict__ ci,
-                                             const AT* __restrict__ av, const XT* __restrict__ x, int r0, int* scol,
-                                             AT* sval, int& row_out) {
-    const int lane = threadIdx.x & 31;
-    const int rend = min(r0 + kWarp, n);
-    const int e0 = __ldg(rp + r0);
-    const int e1 = __ldg(rp + rend);
-    const int row = r0 + lane;
-    row_out = row < n ? row : -1;
+__device__ __forceinline__ AT spmv_row(const int* __restrict__ rp, const int* __restrict__ ci,
+                                       const AT* __restrict__ av, const XT* __restrict__ x, int row) {
+    const int pb = __ldg(rp + row);
+    const int pe = __ldg(rp + row + 1);
     AT acc = AT(0);
-    if (e1 - e0 <= kSpmvStage) {
-        for (int e = e0 + lane; e < e1; e += kWarp) {
-            scol[e - e0] = __ldg(ci + e);
-            sval[e - e0] = __ldg(av + e);
-        }
-        __syncwarp();
-        if (row < n) {
-            const int b = __ldg(rp + row) - e0;
-            const int e = __ldg(rp + row + 1) - e0;
-            for (int p = b; p < e; ++p) acc = fma(sval[p], static_cast<AT>(__ldg(x + scol[p])), acc);
-        }
-        __syncwarp();
-    } else if (row < n) {
-        for (int p = __ldg(rp + row); p < __ldg(rp + row + 1); ++p)
-            acc = fma(__ldg(av + p), static_cast<AT>(__ldg(x + __ldg(ci + p))), acc);
-    }
+#pragma unroll 8
+    for (int p = pb; p < pe; ++p) acc = fma(__ldg(av + p), static_cast<AT>(__ldg(x + __ldg(ci + p))), acc);
     return acc;
 }
 
@@ -140,15 +122,8 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
             reset[i] = Sentinel<YT>::value();
     }
-    __shared__ int s_col[kSpmvWarps][kSpmvStage];
-    __shared__ AT s_val[kSpmvWarps][kSpmvStage];
-    const int w = threadIdx.x >> 5;
-    const int nchunks = ceil_div(n, kWarp);
-    for (int c = blockIdx.x * kSpmvWarps + w; c < nchunks; c += gridDim.x * kSpmvWarps) {
-        int row;
-        const AT acc = spmv_row_chunk(n, rp, ci, av, x, c * kWarp, s_col[w], s_val[w], row);
-        if (row >= 0) y[row] = static_cast<YT>(acc);
-    }
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x)
+        y[row] = static_cast<YT>(spmv_row(rp, ci, av, x, row));
 }
 
 // Cycle start: r = b - A x (FP64), v0 = r (unnormalised, type T), beta = ||r||_2, then
@@ -160,21 +135,14 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
     gmres_residual_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ av,
                           const double* __restrict__ b, const double* __restrict__ x, T* __restrict__ v0, GmresCtl* ctl,
                           Hess H, double* partial, unsigned* counter) {
-    __shared__ int s_col[kSpmvWarps][kSpmvStage];
-    __shared__ double s_val[kSpmvWarps][kSpmvStage];
     __shared__ double s_red[kSpmvWarps];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
-    const int nchunks = ceil_div(n, kWarp);
     double ss = 0.0;
-    for (int c = blockIdx.x * kSpmvWarps + w; c < nchunks; c += gridDim.x * kSpmvWarps) {
-        int row;
-        const double acc = spmv_row_chunk(n, rp, ci, av, x, c * kWarp, s_col[w], s_val[w], row);
-        if (row >= 0) {
-            const double r = b[row] - acc;
-            v0[row] = static_cast<T>(r);
-            ss = fma(r, r, ss);
-        }
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        const double r = b[row] - spmv_row(rp, ci, av, x, row);
+        v0[row] = static_cast<T>(r);
+        ss = fma(r, r, ss);
     }
     ss = warp_sum(ss);
     if (lane == 0) s_red[w] = ss;

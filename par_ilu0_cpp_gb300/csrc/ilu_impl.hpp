@@ -153,7 +153,7 @@ struct IluSolver::Impl {
     int grid_fact = 0;
     // factorisation launch: staged entries per warp, warps per block, pivot-row register
     // window per lane, dynamic shared memory per block
-    int fact_cap = 0, fact_warps = 0, fact_pre = 2;
+    int fact_cap = 0, fact_hcap = 0, fact_warps = 0, fact_pre = 2;
     size_t fact_smem = 0;
     // level-ordered substitution launch: grid_solve CTAs of solve_threads threads
     int grid_solve = 0, solve_threads = 0;

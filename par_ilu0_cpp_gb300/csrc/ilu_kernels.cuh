@@ -21,6 +21,7 @@ namespace gb300 {
 constexpr int kFactWarps = 8;    // most warps per block of the factorisation kernel
 constexpr int kFactCap = 128;    // least row length staged in shared memory per warp
 constexpr int kFactEntryBytes = 2 * sizeof(double) + 3 * sizeof(int);  // staged bytes per entry
+constexpr int kFactHashMin = 24;  // rows longer than this locate update positions by hashing
 constexpr int kFactSmemMax = 200 * 1024;  // dynamic shared memory of one factorisation block
 constexpr int kSolveWarps = 8;   // warps per block of the substitution kernels
 
@@ -72,16 +73,22 @@ __device__ __forceinline__ bool gate_closed(const int* gate, int step) {
 // whose rows have more than 64 entries above the diagonal) are loaded into registers
 // while the current pivot is eliminated.  The sequential chain per pivot is then one
 // division (one lane) and a shared-memory search-and-update, instead of three dependent
-// global round trips.  Each warp stages up to `cap` entries (dynamic shared memory,
-// kFactEntryBytes per entry and warp, sized by the host to the longest row where it
-// fits); longer rows are eliminated in global memory.  Row k's values are read at L2
-// (ld.cg) after an acquire on its ready flag; row j publishes with fence + release.
-// `shift` (optional) is added to the diagonal before elimination.
+// global round trips.  The update position of a column in row j is found by binary
+// search over the staged columns for short rows; rows longer than kFactHashMin entries
+// build an open-addressing table (column -> position, hcap slots per warp, linear
+// probing) once and look positions up in one or two probes: a binary search over tens
+// of entries is a chain of dependent shared-memory loads and divergent branches per
+// update, and it set the pace of 27-point ILU(k) rows with ~45 pivots.  Each warp stages
+// up to `cap` entries (dynamic shared memory, kFactEntryBytes per entry plus 8 bytes per
+// table slot and warp, sized by the host to the longest row where it fits); longer rows
+// are eliminated in global memory.  Row k's values are read at L2 (ld.cg) after an
+// acquire on its ready flag; row j publishes with fence + release.  `shift` (optional) is
+// added to the diagonal before elimination.
 template <int PRE>
 __global__ void __launch_bounds__(kFactWarps * kWarp)
     ilu_factor_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const int* __restrict__ diag,
                       const int* __restrict__ order, double* lu, const double* __restrict__ shift, int* done,
-                      int stamp, unsigned* counter, int* status, int cap) {
+                      int stamp, unsigned* counter, int* status, int cap, int hcap) {
     extern __shared__ double fact_smem[];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
@@ -89,9 +96,12 @@ __global__ void __launch_bounds__(kFactWarps * kWarp)
     const size_t wc = static_cast<size_t>(w) * cap, nc_ = static_cast<size_t>(nw) * cap;
     double* sval = fact_smem + wc;
     double* sukk = fact_smem + nc_ + wc;
-    int* scol = reinterpret_cast<int*>(fact_smem + 2 * nc_) + wc;
-    int* skd = reinterpret_cast<int*>(fact_smem + 2 * nc_) + nc_ + wc;
-    int* ske = reinterpret_cast<int*>(fact_smem + 2 * nc_) + 2 * nc_ + wc;
+    int* ibase = reinterpret_cast<int*>(fact_smem + 2 * nc_);
+    int* scol = ibase + wc;
+    int* skd = ibase + nc_ + wc;
+    int* ske = ibase + 2 * nc_ + wc;
+    int* hkey = ibase + 3 * nc_ + static_cast<size_t>(w) * hcap;
+    int* hpos = ibase + 3 * nc_ + static_cast<size_t>(nw) * hcap + static_cast<size_t>(w) * hcap;
     int q = draw_ticket(counter, n, lane);
     while (q < n) {
         const int qn = draw_ticket(counter, n, lane);
@@ -115,7 +125,38 @@ __global__ void __launch_bounds__(kFactWarps * kWarp)
                     sukk[t] = __ldcg(lu + kd);
                 }
             }
+            // column -> position table of row j (long rows): hsize slots, a power of two
+            // of at least twice the row length, keys -1 where empty
+            const bool hashed = len > kFactHashMin;
+            int hsize = 0, hshift = 0;
+            if (hashed) {
+                hsize = 64;
+                while (hsize < 2 * len) hsize <<= 1;
+                hshift = 32 - (31 - __clz(hsize));
+                for (int h = lane; h < hsize; h += kWarp) hkey[h] = -1;
+            }
             __syncwarp();
+            if (hashed) {
+                for (int t = lane; t < len; t += kWarp) {
+                    const int c = scol[t];
+                    unsigned h = (static_cast<unsigned>(c) * 0x9E3779B1u) >> hshift;
+                    while (atomicCAS(hkey + h, -1, c) != -1) h = (h + 1) & static_cast<unsigned>(hsize - 1);
+                    hpos[h] = t;
+                }
+                __syncwarp();
+            }
+            // position of column c in row j (c lies beyond position t), -1 if absent
+            auto locate = [&](int c, int t) -> int {
+                if (!hashed) return find_sorted(scol, t + 1, len, c);
+                unsigned h = (static_cast<unsigned>(c) * 0x9E3779B1u) >> hshift;
+                for (int probe = 0; probe < hsize; ++probe) {
+                    const int k = hkey[h];
+                    if (k == c) return hpos[h];
+                    if (k < 0) return -1;
+                    h = (h + 1) & static_cast<unsigned>(hsize - 1);
+                }
+                return -1;
+            };
             // strict-upper entries of pivot row t held by this lane: p = kd + 1 + lane + 32 u
             int nc[PRE];
             double nv[PRE];
@@ -148,13 +189,13 @@ __global__ void __launch_bounds__(kFactWarps * kWarp)
 #pragma unroll
                 for (int u = 0; u < PRE; ++u) {
                     if (cc[u] >= 0) {
-                        const int pos = find_sorted(scol, t + 1, len, cc[u]);
+                        const int pos = locate(cc[u], t);
                         if (pos >= 0) sval[pos] = fma(-cv[u], l, sval[pos]);
                     }
                 }
                 // strict-upper entries beyond the register window (long pivot rows)
                 for (int p = skd[t] + 1 + lane + PRE * kWarp; p < ske[t]; p += kWarp) {
-                    const int pos = find_sorted(scol, t + 1, len, ci[p]);
+                    const int pos = locate(ci[p], t);
                     if (pos >= 0) sval[pos] = fma(-__ldcg(lu + p), l, sval[pos]);
                 }
                 __syncwarp();

@@ -718,15 +718,22 @@ void IluSolver::SetupMatrix() {
             maxlen = std::max(maxlen, rp[r + 1] - rp[r]);
             maxup = std::max(maxup, rp[r + 1] - im.an.diag[r] - 1);
         }
+        // per warp: cap staged entries plus a column -> position table of hcap slots
+        auto hcap_of = [](int c) {
+            int h = 64;
+            while (h < 2 * c) h <<= 1;
+            return h;
+        };
+        auto warp_bytes = [&](int c) { return static_cast<long long>(c) * kFactEntryBytes + 8ll * hcap_of(c); };
         int cap = std::max(kFactCap, ceil_div(maxlen, kWarp) * kWarp);
-        const int cap_max = kFactSmemMax / kFactEntryBytes / kWarp * kWarp;
-        if (cap > cap_max) cap = cap_max;  // longer rows: global-memory elimination
+        while (cap > kFactCap && warp_bytes(cap) > kFactSmemMax) cap -= kWarp;  // longer rows: global memory
         int warps = kFactWarps;
-        while (warps > 1 && static_cast<long long>(warps) * cap * kFactEntryBytes > kFactSmemMax) --warps;
+        while (warps > 1 && warps * warp_bytes(cap) > kFactSmemMax) --warps;
         im.fact_cap = cap;
+        im.fact_hcap = hcap_of(cap);
         im.fact_warps = warps;
         im.fact_pre = maxup > 2 * kWarp ? 8 : 2;
-        im.fact_smem = static_cast<size_t>(warps) * cap * kFactEntryBytes;
+        im.fact_smem = static_cast<size_t>(warps * warp_bytes(cap));
         auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
         GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(im.fact_smem)));
@@ -794,7 +801,7 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
             auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
             kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
                 n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(), shift, im.done.get(),
-                im.stamp, im.counters.get(), im.status.get(), im.fact_cap);
+                im.stamp, im.counters.get(), im.status.get(), im.fact_cap, im.fact_hcap);
             GB_CUDA_CHECK(cudaGetLastError());
             im.launches += 1;
             if (im.blk64) {
