@@ -60,6 +60,7 @@ struct BlockPack {
     int block_rows = 0;   // rows per block (the last block may be shorter)
     int ntask = 0;
     int kmax = 0;         // most entries of a row
+    int stride = 0;       // entries per lane of every task (3, 4, 8: the kernel's registers; 0: off / len)
     long long slots = 0;
     int threads = 0;      // CTA size
     int cl = 0;           // cluster size of the cluster variant (0: plain variant)
@@ -80,6 +81,7 @@ struct BlockPack {
         p.block_rows = block_rows;
         p.halo = halo;
         p.cl = cl;
+        p.stride = stride;
         p.exps = exps.get();
         p.blk_row = blk_row.get();
         p.blk_task = blk_task.get();

@@ -636,6 +636,9 @@ struct BlockTri {
     int halo = 0;
     int cl = 0;
     const int* exps = nullptr;      // [32 * ntask]
+    // > 0 (the kernel's KM): every task holds `stride` entries per lane and task t's
+    // slots start at t * stride * 32 (off / len are not read); 0: per-task off / len
+    int stride = 0;
 };
 
 // ---- thread-block cluster helpers (distributed shared memory) ----
@@ -766,12 +769,17 @@ struct BlockTask {
     T b, d;
 };
 
-template <class T, bool UPPER, int KM>
+template <class T, bool UPPER, int KM, bool FIXED>
 __device__ __forceinline__ void load_block_task(const BlockTri<T>& P, int t, int lane, const T* in,
                                                 BlockTask<T, KM>& s) {
     s.row = P.rows[t * kWarp + lane];
-    s.off = P.off[t];
-    s.K = P.len[t];
+    if constexpr (FIXED) {
+        s.off = t * (KM * kWarp);  // compile-time task length: no off / len loads, fixed loop bounds
+        s.K = KM;
+    } else {
+        s.off = P.off[t];
+        s.K = P.len[t];
+    }
 #pragma unroll
     for (int u = 0; u < KM; ++u) {
         const int sidx = s.off + u * kWarp + lane;
@@ -803,7 +811,7 @@ __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const Blo
 }
 
 // Solves block `blk` (its solution xs[0 .. rows) already at the sentinel).
-template <class T, bool UPPER, int KM>
+template <class T, bool UPPER, int KM, bool FIXED>
 __device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in, bool scaled, T sc, T* xs, T* out,
                                             unsigned remote, int* status) {
     const int lane = threadIdx.x & 31;
@@ -815,11 +823,11 @@ __device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in
     // when the block was taken; loading two tasks ahead measured slower by ~2%).
     BlockTask<T, KM> A;
     int t = P.blk_task[blk] + w;
-    if (t < t1) load_block_task<T, UPPER, KM>(P, t, lane, in, A);
+    if (t < t1) load_block_task<T, UPPER, KM, FIXED>(P, t, lane, in, A);
     while (t < t1) {
         const BlockTask<T, KM> cur = A;
         const int tn = t + nw;
-        if (tn < t1) load_block_task<T, UPPER, KM>(P, tn, lane, in, A);
+        if (tn < t1) load_block_task<T, UPPER, KM, FIXED>(P, tn, lane, in, A);
         solve_block_task<T, UPPER, KM>(P, cur, lane, scaled, sc, in, xs, base, out, remote, status);
         t = tn;
     }
@@ -875,8 +883,11 @@ __device__ __forceinline__ void prefetch_block(const BlockTri<T>& P, int blk, co
 // out must hold the sentinel for every row on entry.  Dynamic shared memory: the
 // largest block's rows x sizeof(T).
 // KM: entries per row held in registers (3 or 4 when no row of the factor has more, else
-// kLaneEntries); longer rows take the entry-by-entry path.
-template <class T, bool UPPER, int KM>
+// kLaneEntries); longer rows take the entry-by-entry path.  FIXED: every task holds KM
+// entries per lane (factors whose rows fit in registers), so the task layout and the
+// loops over a lane's entries have compile-time bounds (7% faster FP32 7-point sweeps
+// than per-task lengths loaded from off / len).
+template <class T, bool UPPER, int KM, bool FIXED>
 __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
     sptrsv_block_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
                         const int* gate, int step) {
@@ -893,7 +904,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
         prefetch_block<T, UPPER>(P, blk, in);
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
         __syncthreads();
-        solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, 0u, status);
+        solve_block<T, UPPER, KM, FIXED>(P, blk, in, scaled, sc, xs, out, 0u, status);
         finish_block(P, blk, in, scaled, sc, xs, out);
     }
 }
@@ -906,7 +917,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
 // the consumer's entry codes point: in-cluster handoffs never touch L2.  Rank 0 reads its
 // cross-block values from L2 as in the plain variant.  Dynamic shared memory:
 // (block_rows + halo) x sizeof(T).
-template <class T, bool UPPER, int KM>
+template <class T, bool UPPER, int KM, bool FIXED>
 __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
     sptrsv_block_cluster_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
                                 const int* gate, int step) {
@@ -947,7 +958,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
         if (active) {
             const bool push = rank + 1 < CL && pos + 1 < P.nblk;
             const unsigned remote = push ? map_shared_rank(xs + P.block_rows, rank + 1) : 0u;
-            solve_block<T, UPPER, KM>(P, blk, in, scaled, sc, xs, out, remote, status);
+            solve_block<T, UPPER, KM, FIXED>(P, blk, in, scaled, sc, xs, out, remote, status);
         }
         if (active) finish_block(P, blk, in, scaled, sc, xs, out);
         __syncthreads();

@@ -262,6 +262,10 @@ static int choose_block_rows(int n, const int* rp, const int* ci, const std::vec
 // [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1]) descending plus the
 // diagonal position.  A value type is marked as fitting when the largest block's
 // solution fits in `smem_budget` bytes of shared memory.
+// Entries per lane held in registers by the block-local kernel for rows of at most
+// `row_max` entries (the kernel specialisations: 3, 4, kLaneEntries).
+static int block_km_for(int row_max) { return row_max <= 3 ? 3 : (row_max <= 4 ? 4 : kLaneEntries); }
+
 static void build_block_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
                              int block_rows, int elem, size_t smem_budget, int cl, BlockPack& P, cudaStream_t s) {
     const int S = std::max(1, std::min(block_rows, std::max(n, 1)));
@@ -273,6 +277,12 @@ static void build_block_pack(int n, const int* rp, const int* ci, const std::vec
     std::vector<int> depth(static_cast<size_t>(S)), cnt, ord;
     long long slots = 0;
     int max_level_tasks = 1;
+    // Factors whose rows fit a lane's registers get one task length for all tasks: the
+    // register count of the kernel that solves them (block_km_for), so that task t's
+    // slots start at t * stride * 32 and the kernel's loops have compile-time bounds.
+    int row_max = 0;
+    for (int r = 0; r < n; ++r) row_max = std::max(row_max, eend(r) - ebeg(r));
+    const int stride = row_max <= kLaneEntries ? block_km_for(row_max) : 0;
     for (int c = 0; c < nblk; ++c) {
         const int lo = c * S;
         const int hi = std::min(n, lo + S);
@@ -305,6 +315,7 @@ static void build_block_pack(int n, const int* rp, const int* ci, const std::vec
                         if (!lower) dsrc.push_back(-1);
                     }
                 }
+                if (stride > 0) K = stride;
                 off.push_back(static_cast<int>(slots));
                 len.push_back(K);
                 slots += static_cast<long long>(K) * kWarp;
@@ -340,6 +351,7 @@ static void build_block_pack(int n, const int* rp, const int* ci, const std::vec
     P.nblk = nblk;
     P.block_rows = S;
     P.ntask = ntask;
+    P.stride = stride;
     P.kmax = len.empty() ? 0 : *std::max_element(len.begin(), len.end());
     P.slots = slots;
     // two tasks in flight per level of the widest block level, 4 .. kBlockWarpsMax warps
@@ -467,11 +479,11 @@ static cudaLaunchConfig_t cluster_launch_config(const BlockPack& P, int grid, si
 // Raises the kernel's dynamic shared-memory limit to the pack's footprint and records how
 // many CTAs to launch: the resident CTAs (plain variant) or the resident clusters times
 // the cluster size (cluster variant; 0 when a cluster cannot be scheduled).
-template <class T, bool UPPER, int KM>
+template <class T, bool UPPER, int KM, bool FIXED>
 static void configure_block_km(BlockPack& P, int sms) {
     const int bytes = static_cast<int>(std::max<size_t>(P.smem, 16));
     if (P.cl) {
-        auto* kern = sptrsv_block_cluster_kernel<T, UPPER, KM>;
+        auto* kern = sptrsv_block_cluster_kernel<T, UPPER, KM, FIXED>;
         GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         const int nq = ceil_div(P.nblk, P.cl);
         cudaLaunchAttribute attr[1];
@@ -484,35 +496,37 @@ static void configure_block_km(BlockPack& P, int sms) {
         P.grid = std::min(nclusters, nq) * P.cl;
         return;
     }
-    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, UPPER, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GB_CUDA_CHECK(cudaFuncSetAttribute(sptrsv_block_kernel<T, UPPER, KM, FIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        bytes));
     int per_sm = 0;
-    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_block_kernel<T, UPPER, KM>, P.threads,
+    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sptrsv_block_kernel<T, UPPER, KM, FIXED>, P.threads,
                                                                static_cast<size_t>(bytes)));
     P.grid = std::max(1, per_sm) * sms;
 }
 
 template <class T, bool UPPER>
 static void configure_block(BlockPack& P, int sms) {
-    if (P.kmax <= 3)
-        configure_block_km<T, UPPER, 3>(P, sms);
-    else if (P.kmax <= 4)
-        configure_block_km<T, UPPER, 4>(P, sms);
+    if (P.stride == 3)
+        configure_block_km<T, UPPER, 3, true>(P, sms);
+    else if (P.stride == 4)
+        configure_block_km<T, UPPER, 4, true>(P, sms);
+    else if (P.stride == kLaneEntries)
+        configure_block_km<T, UPPER, kLaneEntries, true>(P, sms);
     else
-        configure_block_km<T, UPPER, kLaneEntries>(P, sms);
+        configure_block_km<T, UPPER, kLaneEntries, false>(P, sms);
 }
 
-template <class T, bool UPPER, int KM>
+template <class T, bool UPPER, int KM, bool FIXED>
 static void launch_block_km(const BlockPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
                             int* status, const int* gate, int step) {
     if (P.cl) {
         cudaLaunchAttribute attr[1];
         cudaLaunchConfig_t cfg = cluster_launch_config(P, P.grid, P.smem, s, attr);
-        GB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, sptrsv_block_cluster_kernel<T, UPPER, KM>, P.view<T>(), in, scale, out,
+        GB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, sptrsv_block_cluster_kernel<T, UPPER, KM, FIXED>, P.view<T>(), in, scale, out,
                                          counter, status, gate, step));
         return;
     }
-    sptrsv_block_kernel<T, UPPER, KM><<<std::min(P.grid, P.nblk), P.threads, P.smem, s>>>(P.view<T>(), in, scale, out,
+    sptrsv_block_kernel<T, UPPER, KM, FIXED><<<std::min(P.grid, P.nblk), P.threads, P.smem, s>>>(P.view<T>(), in, scale, out,
                                                                                         counter, status, gate, step);
 }
 
@@ -520,12 +534,14 @@ template <class T, bool UPPER>
 static void launch_block(const BlockPack& P, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
                          int* status, const int* gate, int step) {
     if (P.nblk == 0) return;
-    if (P.kmax <= 3)
-        launch_block_km<T, UPPER, 3>(P, s, in, scale, out, counter, status, gate, step);
-    else if (P.kmax <= 4)
-        launch_block_km<T, UPPER, 4>(P, s, in, scale, out, counter, status, gate, step);
+    if (P.stride == 3)
+        launch_block_km<T, UPPER, 3, true>(P, s, in, scale, out, counter, status, gate, step);
+    else if (P.stride == 4)
+        launch_block_km<T, UPPER, 4, true>(P, s, in, scale, out, counter, status, gate, step);
+    else if (P.stride == kLaneEntries)
+        launch_block_km<T, UPPER, kLaneEntries, true>(P, s, in, scale, out, counter, status, gate, step);
     else
-        launch_block_km<T, UPPER, kLaneEntries>(P, s, in, scale, out, counter, status, gate, step);
+        launch_block_km<T, UPPER, kLaneEntries, false>(P, s, in, scale, out, counter, status, gate, step);
 }
 
 template <class T>
