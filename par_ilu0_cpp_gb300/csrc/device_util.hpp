@@ -50,6 +50,7 @@ struct DeviceInfo {
     int device = 0;
     int sms = 0;
     int smem_optin = 0;  // largest dynamic + static shared memory of one CTA (bytes)
+    int smem_per_sm = 0;  // shared memory of one SM (bytes)
 };
 
 inline DeviceInfo current_device() {
@@ -57,6 +58,7 @@ inline DeviceInfo current_device() {
     GB_CUDA_CHECK(cudaGetDevice(&d.device));
     GB_CUDA_CHECK(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, d.device));
     GB_CUDA_CHECK(cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, d.device));
+    GB_CUDA_CHECK(cudaDeviceGetAttribute(&d.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, d.device));
     return d;
 }
 

@@ -613,6 +613,9 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
 constexpr int kBlockWarpsMax = 16;
 constexpr int kBlockCluster = 8;  // CTAs per cluster of the cluster variant (portable maximum)
 constexpr int kPubGlobal = 1 << 30;
+constexpr int kPubSlotBits = 15;  // halo slot + 1 of a row, per distance d = 1, 2
+constexpr int kPubSlotMask = (1 << kPubSlotBits) - 1;
+constexpr int kHaloDepth = 2;     // positions ahead a row is pushed to (cluster variant)
 
 template <class T>
 struct BlockTri {
@@ -629,9 +632,10 @@ struct BlockTri {
     const T* dvals = nullptr;       // [32 * ntask] diagonal (upper factor only; FP32: 1 / u_ii)
     // Per-row publication words: bit kPubGlobal = another block reads the row through L2
     // (store it to `out` as soon as it is computed; the others reach `out` in a coalesced
-    // copy when their block is done); bits 0-29 = halo slot + 1 (cluster variant: blocks
-    // at processing positions q*cl .. q*cl + cl - 1 run on one cluster and the rows the
-    // next position's block reads are pushed into that CTA's halo xs[block_rows + slot]).
+    // copy when their block is done); bits [15 (d - 1), 15 d) = halo slot + 1 of the row in
+    // the CTA d = 1, 2 positions ahead (cluster variant: blocks at processing positions
+    // q*cl .. q*cl + cl - 1 run on one cluster and the rows a position's block reads from
+    // the two positions before it are pushed into its halo xs[block_rows + slot]).
     int block_rows = 0;
     int halo = 0;
     int cl = 0;
@@ -692,9 +696,24 @@ __device__ __forceinline__ T block_dep(int code, const T* xs, const T* out) {
 
 // Per-lane progressive solve of one task's rows (at most KM entries each);
 // publishes each row to shared memory and to `out` the moment its last entry is consumed.
+// Publishes row `row` (value r): the block's shared memory, the halos of the cluster
+// CTAs one and two positions ahead (remote / remote2, 0 when none) where the row has a
+// slot there, and `out` when another block reads it through L2.
+template <class T>
+__device__ __forceinline__ void block_publish(int row, T r, T* xs, int base, T* out, unsigned remote, unsigned remote2,
+                                              int ex) {
+    st_volatile_shared(xs + (row - base), r);
+    const int s1 = (ex & kPubSlotMask) - 1;
+    if (remote != 0u && s1 >= 0) st_cluster(remote + static_cast<unsigned>(s1) * sizeof(T), r);
+    const int s2 = ((ex >> kPubSlotBits) & kPubSlotMask) - 1;
+    if (remote2 != 0u && s2 >= 0) st_cluster(remote2 + static_cast<unsigned>(s2) * sizeof(T), r);
+    if (ex & kPubGlobal) st_relaxed(out + row, r);
+}
+
 template <class T, bool UPPER, int KM>
 __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)[KM], const T (&v)[KM], T acc, T d,
-                                                  T* xs, int base, T* out, unsigned remote, int ex, int* status) {
+                                                  T* xs, int base, T* out, unsigned remote, unsigned remote2, int ex,
+                                                  int* status) {
     int k = 0;
     bool done = row < 0;
     WaitBudget wb;
@@ -718,10 +737,7 @@ __device__ __forceinline__ void block_progressive(int row, int K, const int (&c)
             if (k >= K) {
                 // FP64: the reference's division; FP32 (mixed path): d holds 1 / u_ii
                 const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / d : acc * d) : acc);
-                st_volatile_shared(xs + (row - base), r);
-                const int slot = (ex & (kPubGlobal - 1)) - 1;
-                if (remote != 0u && slot >= 0) st_cluster(remote + static_cast<unsigned>(slot) * sizeof(T), r);
-                if (ex & kPubGlobal) st_relaxed(out + row, r);
+                block_publish(row, r, xs, base, out, remote, remote2, ex);
                 done = true;
             }
         }
@@ -794,18 +810,16 @@ __device__ __forceinline__ void load_block_task(const BlockTri<T>& P, int t, int
 template <class T, bool UPPER, int KM>
 __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const BlockTask<T, KM>& s, int lane,
                                                  bool scaled, T sc, T* in, T* xs, int base, T* out, unsigned remote,
-                                                 int* status) {
+                                                 unsigned remote2, int* status) {
     T acc = scaled ? s.b * sc : s.b;
     if (s.K <= KM) {
-        block_progressive<T, UPPER, KM>(s.row, s.K, s.c, s.v, acc, s.d, xs, base, out, remote, s.ex, status);
+        block_progressive<T, UPPER, KM>(s.row, s.K, s.c, s.v, acc, s.d, xs, base, out, remote, remote2, s.ex,
+                                        status);
     } else {
         acc = block_long_row(s.off, s.K, lane, P.codes, P.vals, acc, xs, out, status);
         if (s.row >= 0) {
             const T r = Sentinel<T>::canon(UPPER ? (sizeof(T) == 8 ? acc / s.d : acc * s.d) : acc);
-            st_volatile_shared(xs + (s.row - base), r);
-            const int slot = (s.ex & (kPubGlobal - 1)) - 1;
-            if (remote != 0u && slot >= 0) st_cluster(remote + static_cast<unsigned>(slot) * sizeof(T), r);
-            if (s.ex & kPubGlobal) st_relaxed(out + s.row, r);
+            block_publish(s.row, r, xs, base, out, remote, remote2, s.ex);
         }
     }
 }
@@ -813,7 +827,7 @@ __device__ __forceinline__ void solve_block_task(const BlockTri<T>& P, const Blo
 // Solves block `blk` (its solution xs[0 .. rows) already at the sentinel).
 template <class T, bool UPPER, int KM, bool FIXED>
 __device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in, bool scaled, T sc, T* xs, T* out,
-                                            unsigned remote, int* status) {
+                                            unsigned remote, unsigned remote2, int* status) {
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
@@ -828,7 +842,7 @@ __device__ __forceinline__ void solve_block(const BlockTri<T>& P, int blk, T* in
         const BlockTask<T, KM> cur = A;
         const int tn = t + nw;
         if (tn < t1) load_block_task<T, UPPER, KM, FIXED>(P, tn, lane, in, A);
-        solve_block_task<T, UPPER, KM>(P, cur, lane, scaled, sc, in, xs, base, out, remote, status);
+        solve_block_task<T, UPPER, KM>(P, cur, lane, scaled, sc, in, xs, base, out, remote, remote2, status);
         t = tn;
     }
 }
@@ -904,7 +918,7 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
         prefetch_block<T, UPPER>(P, blk, in);
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) xs[i] = Sentinel<T>::value();
         __syncthreads();
-        solve_block<T, UPPER, KM, FIXED>(P, blk, in, scaled, sc, xs, out, 0u, status);
+        solve_block<T, UPPER, KM, FIXED>(P, blk, in, scaled, sc, xs, out, 0u, 0u, status);
         finish_block(P, blk, in, scaled, sc, xs, out);
     }
 }
@@ -912,11 +926,11 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
 // Cluster variant: launched with clusters of P.cl CTAs.  The cluster's CTA of rank r takes
 // processing position q * cl + r of the cluster's ticket q (tickets in dependency order:
 // no co-residency assumption between clusters; the CTAs of one cluster are co-scheduled
-// by the hardware).  Each CTA pushes the rows that the next position's block reads into
-// that CTA's shared-memory halo (xs[block_rows + slot], distributed shared memory), where
-// the consumer's entry codes point: in-cluster handoffs never touch L2.  Rank 0 reads its
-// cross-block values from L2 as in the plain variant.  Dynamic shared memory:
-// (block_rows + halo) x sizeof(T).
+// by the hardware).  Each CTA pushes the rows that the blocks one and two positions
+// ahead read into those CTAs' shared-memory halos (xs[block_rows + slot], distributed
+// shared memory), where the consumers' entry codes point: in-cluster handoffs never
+// touch L2.  Sources outside the cluster are read from L2 as in the plain variant.
+// Dynamic shared memory: (block_rows + halo) x sizeof(T).
 template <class T, bool UPPER, int KM, bool FIXED>
 __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
     sptrsv_block_cluster_kernel(BlockTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
@@ -957,8 +971,10 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
         cluster_sync_all();
         if (active) {
             const bool push = rank + 1 < CL && pos + 1 < P.nblk;
+            const bool push2 = rank + 2 < CL && pos + 2 < P.nblk;
             const unsigned remote = push ? map_shared_rank(xs + P.block_rows, rank + 1) : 0u;
-            solve_block<T, UPPER, KM, FIXED>(P, blk, in, scaled, sc, xs, out, remote, status);
+            const unsigned remote2 = push2 ? map_shared_rank(xs + P.block_rows, rank + 2) : 0u;
+            solve_block<T, UPPER, KM, FIXED>(P, blk, in, scaled, sc, xs, out, remote, remote2, status);
         }
         if (active) finish_block(P, blk, in, scaled, sc, xs, out);
         __syncthreads();

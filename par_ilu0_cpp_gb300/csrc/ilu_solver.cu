@@ -182,6 +182,7 @@ static int block_levels(int lo, int hi, bool lower, const int* rp, const int* ci
 // level-ordered kernel's cost per level (a fixed handoff plus a term per row).
 constexpr double kModelBlockLevelUs = 0.35;
 constexpr double kModelBlockHopUs = 2.0;
+constexpr double kModelClusterHopUs = 0.5;  // handoff into a halo of the same cluster
 constexpr double kModelLevelUs = 0.6;
 constexpr double kModelLevelRowUs = 9e-5;
 
@@ -212,49 +213,112 @@ static int plane_offset(int n, const int* rp, const int* ci, const std::vector<i
 // Modelled critical path (us) of the forward sweep with the block-local kernel and
 // blocks of B rows: every row finishes one block-level after its latest dependency,
 // plus a handoff when that dependency lies in another block.
-static double block_schedule_model(int n, const int* rp, const int* ci, const std::vector<int>& diag, int B) {
+// R: CTAs resident at once; block b starts only once block b - R is done (blocks go to
+// CTAs by tickets in order), which bounds schedules with more blocks than CTAs.
+static double block_schedule_model(int n, const int* rp, const int* ci, const std::vector<int>& diag, int B, int cl,
+                                   int R) {
     std::vector<double> t(static_cast<size_t>(n));
+    std::vector<double> bend(static_cast<size_t>(ceil_div(n, B)), 0.0);
     double T = 0.0;
     for (int r = 0; r < n; ++r) {
-        double m = 0.0;
         const int br = r / B;
+        double m = br >= R ? bend[static_cast<size_t>(br - R)] : 0.0;
         for (int p = rp[r]; p < diag[r]; ++p) {
             const int c = ci[p];
-            m = std::max(m, t[c] + (c / B == br ? 0.0 : kModelBlockHopUs));
+            const int bc = c / B;
+            const double hop = bc == br ? 0.0
+                               : (cl > 1 && br - bc <= kHaloDepth && br / cl == bc / cl) ? kModelClusterHopUs
+                                                                                          : kModelBlockHopUs;
+            m = std::max(m, t[c] + hop);
         }
         t[r] = m + kModelBlockLevelUs;
+        bend[static_cast<size_t>(br)] = std::max(bend[static_cast<size_t>(br)], t[r]);
         T = std::max(T, t[r]);
     }
     return T;
 }
 
-// Block size of the block-local schedule for values of `elem` bytes, or 0 when the
-// level-ordered kernel is expected to be faster.  Candidates are multiples of the plane
-// size that fit in shared memory; rows with more than kLaneEntries entries take the
-// block kernel's slow path, so such factors keep the level kernel.
-static int choose_block_rows(int n, const int* rp, const int* ci, const std::vector<int>& diag, int nlev, int elem,
-                             size_t smem_budget) {
-    if (n <= 0) return 0;
+// Halo rows a CTA of the cluster variant needs: the most distinct rows that a block reads
+// from the blocks 1 .. kHaloDepth positions before it in its cluster (lower triangle).
+static int halo_rows_needed(int n, const int* rp, const int* ci, const std::vector<int>& diag, int B, int cl) {
+    int H = 0;
+    std::vector<int> mark(static_cast<size_t>(n), -1);
+    for (int b = 1; b * static_cast<long long>(B) < n; ++b) {
+        if (b % cl == 0) continue;
+        int cnt = 0;
+        const int lo = b * B, hi = std::min(n, lo + B);
+        const int src_lo = std::max((b / cl) * cl, b - kHaloDepth) * B;
+        for (int r = lo; r < hi; ++r)
+            for (int p = rp[r]; p < diag[r]; ++p) {
+                const int c = ci[p];
+                if (c >= src_lo && c < lo && mark[c] != b) {
+                    mark[c] = b;
+                    ++cnt;
+                }
+            }
+        H = std::max(H, cnt);
+    }
+    return H;
+}
+
+// Block-local schedules for values of `elem` bytes, cheapest first by the cost model
+// (block_schedule_model), those the model expects to beat the level-ordered kernel only
+// (empty: keep the level kernel).  Candidates: multiples of the plane size that fit in
+// shared memory, each with clusters (block + halo must fit) and without.  Rows with more than kLaneEntries entries take the block kernel's slow path,
+// so such factors keep the level kernel.
+struct BlockChoice {
+    int rows;
+    int cl;
+    double us;
+};
+
+static std::vector<BlockChoice> choose_block_schedules(int n, const int* rp, const int* ci,
+                                                       const std::vector<int>& diag, int nlev, int elem,
+                                                       size_t smem_budget, size_t smem_per_sm, int sms) {
+    std::vector<BlockChoice> out;
+    if (n <= 0) return out;
     int kmax = 0;
     for (int r = 0; r < n; ++r) kmax = std::max({kmax, diag[r] - rp[r], rp[r + 1] - diag[r] - 1});
-    if (kmax > kLaneEntries) return 0;
+    if (kmax > kLaneEntries) return out;
     const long long max_rows = static_cast<long long>(smem_budget / static_cast<size_t>(elem));
     const double level_us =
         std::max(1, nlev) * (kModelLevelUs + kModelLevelRowUs * static_cast<double>(n) / std::max(1, nlev));
-    if (n <= max_rows) return block_schedule_model(n, rp, ci, diag, n) < level_us ? n : 0;
+    // resident CTAs: by shared memory per SM; clusters of cl CTAs sit within one GPC,
+    // and about 80% of the SMs can hold whole clusters of 8 (15 on 152 SMs, measured)
+    auto resident = [&](long long bytes, int cl) {
+        const int per_sm = std::max<int>(1, static_cast<int>(smem_per_sm / static_cast<size_t>(std::max<long long>(bytes, 1))));
+        return cl > 1 ? std::max(cl, (sms * 4 / 5 / cl) * cl) * per_sm : sms * per_sm;
+    };
+    if (n <= max_rows) {
+        const double us = block_schedule_model(n, rp, ci, diag, n, 0, 1);
+        if (us < level_us) out.push_back({n, 0, us});
+        return out;
+    }
     const int P = plane_offset(n, rp, ci, diag);
-    if (P <= 0) return 0;
-    int best = 0;
-    double best_us = level_us;
-    for (long long B = P; B <= max_rows && B < n; B *= 2) {
-        const double us = block_schedule_model(n, rp, ci, diag, static_cast<int>(B));
-        if (us < best_us) {
-            best_us = us;
-            best = static_cast<int>(B);
+    if (P <= 0) return out;
+    // (Half-plane blocks, whose halos reach two positions back, were tried for FP64 on
+    // 128^3, where a plane plus a one-plane halo does not fit: twice the blocks, more
+    // than stay resident at once, and 7% slower sweeps than one-plane blocks without
+    // clusters; they stay available through LLJBASH_ILU_OPT_BLOCK_ROWS.)
+    std::vector<long long> sizes;
+    for (long long B = P; B <= max_rows && B < n; B *= 2) sizes.push_back(B);
+    for (long long B : sizes) {
+        if (B > max_rows || B >= n) continue;
+        for (int cl : {kBlockCluster, 0}) {
+            const long long H = cl > 0 ? halo_rows_needed(n, rp, ci, diag, static_cast<int>(B), cl) : 0;
+            if (B + H > max_rows) continue;
+            const int R = resident((B + H) * elem, cl);
+            const double us = block_schedule_model(n, rp, ci, diag, static_cast<int>(B), cl, R);
+            if (us < level_us) out.push_back({static_cast<int>(B), cl, us});
         }
     }
-    return best;
+    std::sort(out.begin(), out.end(), [](const BlockChoice& a, const BlockChoice& b) { return a.us < b.us; });
+    return out;
 }
+
+// Entries per lane held in registers by the block-local kernel for rows of at most
+// `row_max` entries (the kernel specialisations: 3, 4, kLaneEntries).
+static int block_km_for(int row_max) { return row_max <= 3 ? 3 : (row_max <= 4 ? 4 : kLaneEntries); }
 
 // Host construction of a block-local packed factor (see BlockTri): contiguous blocks of
 // `block_rows` rows; inside a block the rows in block-internal level order (ascending row
@@ -262,10 +326,6 @@ static int choose_block_rows(int n, const int* rp, const int* ci, const std::vec
 // [rp[r], diag[r]) ascending; upper: entries (diag[r], rp[r+1]) descending plus the
 // diagonal position.  A value type is marked as fitting when the largest block's
 // solution fits in `smem_budget` bytes of shared memory.
-// Entries per lane held in registers by the block-local kernel for rows of at most
-// `row_max` entries (the kernel specialisations: 3, 4, kLaneEntries).
-static int block_km_for(int row_max) { return row_max <= 3 ? 3 : (row_max <= 4 ? 4 : kLaneEntries); }
-
 static void build_block_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, bool lower,
                              int block_rows, int elem, size_t smem_budget, int cl, BlockPack& P, cudaStream_t s) {
     const int S = std::max(1, std::min(block_rows, std::max(n, 1)));
@@ -357,64 +417,71 @@ static void build_block_pack(int n, const int* rp, const int* ci, const std::vec
     // two tasks in flight per level of the widest block level, 4 .. kBlockWarpsMax warps
     P.threads = kWarp * std::max(4, std::min(kBlockWarpsMax, 2 * max_level_tasks));
     // Cluster halos (cl > 0): the block at processing position p (ascending blocks for L,
-    // descending for U) reads the rows of position p - 1 that it depends on from its
-    // shared-memory halo when both positions are in one cluster (p % cl != 0).  Halo
-    // slots follow ascending row order; the producer's rows carry their slot in `exps`.
-    std::vector<int> exps;
+    // descending for U) reads the rows of positions p - 1 .. p - kHaloDepth that it depends
+    // on from its shared-memory halo when those positions are in its cluster
+    // (p - d >= cl * (p / cl)).  Halo slots: the rows of p - 1 in ascending row order, then
+    // those of p - 2; the producer's rows carry their slot for the block d positions
+    // ahead in `exps` (kPubSlotBits bits per distance).
+    std::vector<int> exps(rows.size(), 0);
     int H = 0;
+    bool halo_ok = true;
     if (cl > 1) {
-        exps.assign(rows.size(), -1);
         std::vector<int> slot_of(static_cast<size_t>(S), -1), used;
         for (int pos = 1; pos < nblk; ++pos) {
             if (pos % cl == 0) continue;
             const int cb = lower ? pos : nblk - 1 - pos;
-            const int pb = lower ? pos - 1 : nblk - pos;
-            const int plo = blk_row[pb], phi = blk_row[pb + 1];
-            used.clear();
-            for (int t = blk_task[cb]; t < blk_task[cb + 1]; ++t)
-                for (long long q = off[t]; q < off[t] + static_cast<long long>(len[t]) * kWarp; ++q) {
-                    const int col = codes[static_cast<size_t>(q)];
-                    if (col >= plo && col < phi && slot_of[col - plo] < 0) {
-                        slot_of[col - plo] = 0;
-                        used.push_back(col);
+            int base = 0;
+            for (int d = 1; d <= kHaloDepth && pos % cl >= d; ++d) {
+                const int pb = lower ? pos - d : nblk - 1 - (pos - d);
+                const int plo = blk_row[pb], phi = blk_row[pb + 1];
+                used.clear();
+                for (int t = blk_task[cb]; t < blk_task[cb + 1]; ++t)
+                    for (long long q = off[t]; q < off[t] + static_cast<long long>(len[t]) * kWarp; ++q) {
+                        const int col = codes[static_cast<size_t>(q)];
+                        if (col >= plo && col < phi && slot_of[col - plo] < 0) {
+                            slot_of[col - plo] = 0;
+                            used.push_back(col);
+                        }
                     }
-                }
-            std::sort(used.begin(), used.end());
-            for (size_t k = 0; k < used.size(); ++k) slot_of[used[k] - plo] = static_cast<int>(k);
-            H = std::max(H, static_cast<int>(used.size()));
-            for (int t = blk_task[cb]; t < blk_task[cb + 1]; ++t)
-                for (long long q = off[t]; q < off[t] + static_cast<long long>(len[t]) * kWarp; ++q) {
-                    int& code = codes[static_cast<size_t>(q)];
-                    if (code >= plo && code < phi) code = -2 - (S + slot_of[code - plo]);
-                }
-            for (int t = blk_task[pb]; t < blk_task[pb + 1]; ++t)
-                for (int l = 0; l < kWarp; ++l) {
-                    const int r = rows[static_cast<size_t>(t) * kWarp + l];
-                    if (r >= 0) exps[static_cast<size_t>(t) * kWarp + l] = slot_of[r - plo];
-                }
-            for (int col : used) slot_of[col - plo] = -1;
+                std::sort(used.begin(), used.end());
+                for (size_t k = 0; k < used.size(); ++k) slot_of[used[k] - plo] = base + static_cast<int>(k);
+                for (int t = blk_task[cb]; t < blk_task[cb + 1]; ++t)
+                    for (long long q = off[t]; q < off[t] + static_cast<long long>(len[t]) * kWarp; ++q) {
+                        int& code = codes[static_cast<size_t>(q)];
+                        if (code >= plo && code < phi) code = -2 - (S + slot_of[code - plo]);
+                    }
+                for (int t = blk_task[pb]; t < blk_task[pb + 1]; ++t)
+                    for (int l = 0; l < kWarp; ++l) {
+                        const int r = rows[static_cast<size_t>(t) * kWarp + l];
+                        if (r >= 0 && slot_of[r - plo] >= 0)
+                            exps[static_cast<size_t>(t) * kWarp + l] |= (slot_of[r - plo] + 1) << (kPubSlotBits * (d - 1));
+                    }
+                for (int col : used) slot_of[col - plo] = -1;
+                base += static_cast<int>(used.size());
+            }
+            H = std::max(H, base);
         }
+        if (H >= (1 << kPubSlotBits) - 1) halo_ok = false;  // slots + 1 must fit their fields
     }
-    // Per-row publication word (`pub`): bit 30 = some block reads the row through L2
-    // (a code >= 0 names it), so its value is stored to `out` the moment it is computed;
-    // bits 0-29 = halo slot + 1 (0: none).  Rows without bit 30 reach `out` in one
-    // coalesced copy when their block is done.
+    // Per-row publication word (`pub`): bit kPubGlobal = some block reads the row through
+    // L2 (a code >= 0 names it), so its value is stored to `out` the moment it is
+    // computed; then for d = 1, 2 a field of kPubSlotBits bits = the halo slot + 1 of the
+    // row in the CTA d positions ahead (0: none).  Rows without kPubGlobal reach `out` in
+    // one coalesced copy when their block is done.
     {
         std::vector<unsigned char> global_read(static_cast<size_t>(n), 0);
         for (int code : codes)
             if (code >= 0) global_read[static_cast<size_t>(code)] = 1;
-        if (exps.empty()) exps.assign(rows.size(), -1);
         for (size_t q = 0; q < rows.size(); ++q) {
             const int r = rows[q];
-            const int slot = exps[q];
-            exps[q] = (r >= 0 && global_read[static_cast<size_t>(r)] ? (1 << 30) : 0) | (slot + 1);
+            if (r >= 0 && global_read[static_cast<size_t>(r)]) exps[q] |= kPubGlobal;
         }
     }
     P.cl = cl > 1 ? cl : 0;
     P.halo = H;
     P.elem = elem;
     P.smem = static_cast<size_t>(elem) * (static_cast<size_t>(S) + static_cast<size_t>(H));
-    P.fits = P.smem <= smem_budget;
+    P.fits = P.smem <= smem_budget && halo_ok;
     P.exps.upload(exps.data(), exps.size(), s);
     P.blk_row.upload(blk_row.data(), blk_row.size(), s);
     P.blk_task.upload(blk_task.data(), blk_task.size(), s);
@@ -679,15 +746,21 @@ void IluSolver::SetupMatrix() {
         // which the model prefers the level-ordered kernel, keeps the level kernel
         const size_t budget = static_cast<size_t>(std::max(0, im.dev.smem_optin - 1024));
         for (int elem : {8, 4}) {
-            const int B = im.block_rows > 0 ? im.block_rows
-                                            : choose_block_rows(n, rp, ci, im.an.diag, im.an.nlev_l, elem, budget);
-            if (B <= 0) continue;
+            // candidates in order: the model's ranking, or an explicit block size with
+            // clusters first (block + halo must fit and a cluster be schedulable)
+            std::vector<BlockChoice> cand;
+            if (im.block_rows > 0) {
+                cand = {{im.block_rows, kBlockCluster, 0.0}, {im.block_rows, 0, 0.0}};
+            } else {
+                cand = choose_block_schedules(n, rp, ci, im.an.diag, im.an.nlev_l, elem, budget,
+                                              static_cast<size_t>(im.dev.smem_per_sm), im.dev.sms);
+            }
             BlockPack& lb = elem == 8 ? im.LB64 : im.LB32;
             BlockPack& ub = elem == 8 ? im.UB64 : im.UB32;
-            // cluster variant first (block + halo must fit and a cluster be schedulable),
-            // else the plain variant
             bool ok = false;
-            for (int cl : {kBlockCluster, 0}) {
+            for (const BlockChoice& ch : cand) {
+                const int B = ch.rows;
+                const int cl = ch.cl;
                 if (cl > 0 && n <= B) continue;  // a single block has no handoffs
                 build_block_pack(n, rp, ci, im.an.diag, true, B, elem, budget, cl, lb, s);
                 build_block_pack(n, rp, ci, im.an.diag, false, B, elem, budget, cl, ub, s);

@@ -310,3 +310,36 @@ def test_wait_limit_gives_up_and_solver_recovers(port):
     assert np.array_equal(ilu.substitute(b), x)
     with pytest.raises(RuntimeError):
         ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, -5)
+
+
+@pytest.mark.parametrize("planes", [0.5, 1, 2])
+def test_cluster_halos_two_positions_back(planes):
+    """Half-plane blocks read the block two positions back (the k-1 neighbours) and the
+    one before (the j-1 row): with clusters both are pushed into the consumer's halo.
+    Every block size gives the level-ordered kernel's results bit for bit, in FP64
+    substitution and in the mixed-precision solve."""
+    nx = 24
+    a = g.convdiff3d(nx)
+    f, _ = api.iluk_symbolic(a, 0)
+    _, b = g.random_rhs(a, seed=11)
+    tol = 1e-8 * float(np.linalg.norm(b))
+
+    def run(block_rows):
+        ilu = api.IluSolver()
+        ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
+        ilu.set_matrix(f)
+        assert ilu.setup() == 0, api.last_error()
+        assert ilu.factorize() == 0, api.last_error()
+        x = ilu.substitute(b)
+        gm = api.Gmres(tol, 30, 1000)
+        gm.set_preconditioner(ilu)
+        gm.set_option(api.GMRES_OPT_MODE, 1)
+        res = gm.solve(a, b)
+        assert res.ok
+        return ilu.info(), x, res
+
+    _, x_ref, res_ref = run(-1)
+    info, x, res = run(int(planes * nx * nx))
+    assert info.block_rows_fp64 == int(planes * nx * nx) and info.block_cluster_fp64 == 8
+    assert np.array_equal(x, x_ref)
+    assert res.iterations == res_ref.iterations and np.array_equal(res.x, res_ref.x)
