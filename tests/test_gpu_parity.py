@@ -343,3 +343,87 @@ def test_cluster_halos_two_positions_back(planes):
     assert info.block_rows_fp64 == int(planes * nx * nx) and info.block_cluster_fp64 == 8
     assert np.array_equal(x, x_ref)
     assert res.iterations == res_ref.iterations and np.array_equal(res.x, res_ref.x)
+
+
+def _csr_from_dense_rows(n, cols_of_row, vals_of_row):
+    rp = np.zeros(n + 1, dtype=np.int64)
+    for i in range(n):
+        rp[i + 1] = rp[i] + len(cols_of_row[i])
+    ci = np.concatenate([np.asarray(c, dtype=np.int64) for c in cols_of_row]) if n else np.zeros(0, np.int64)
+    va = np.concatenate([np.asarray(v, dtype=np.float64) for v in vals_of_row]) if n else np.zeros(0)
+    return g.Csr(n, rp, ci, va)
+
+
+def ragged(n, kmax, seed):
+    """Non-symmetric pattern, rows with 0 .. kmax off-diagonal entries at random columns,
+    diagonally dominant values."""
+    rng = np.random.default_rng(seed)
+    cols, vals = [], []
+    for i in range(n):
+        k = int(rng.integers(0, kmax + 1))
+        c = np.unique(rng.integers(0, n, size=k))
+        c = c[c != i]
+        v = rng.uniform(-1.0, 1.0, size=c.size)
+        cc = np.append(c, i)
+        vv = np.append(v, np.abs(v).sum() + 1.0)
+        o = np.argsort(cc)
+        cols.append(cc[o])
+        vals.append(vv[o])
+    return _csr_from_dense_rows(n, cols, vals)
+
+
+def test_single_row_and_diagonal_only():
+    one = _csr_from_dense_rows(1, [[0]], [[4.0]])
+    ilu = factorize(one)
+    assert ilu.values()[0] == 4.0
+    assert ilu.substitute(np.array([2.0]))[0] == 0.5
+    res, _, _ = api.ilu_gmres(one, np.array([2.0]), tol=1e-12, restart=5, maxit=10)
+    assert res.ok and abs(res.x[0] - 0.5) <= 1e-15
+    n = 1000
+    d = np.linspace(1.0, 3.0, n)
+    diag = _csr_from_dense_rows(n, [[i] for i in range(n)], [[d[i]] for i in range(n)])
+    ilu = factorize(diag)
+    assert np.array_equal(ilu.values(), d)
+    b = np.arange(n, dtype=np.float64) + 1.0
+    assert np.array_equal(ilu.substitute(b), b / d)
+    res, _, _ = api.ilu_gmres(diag, b, tol=1e-10, restart=10, maxit=50)
+    assert res.ok and res.iterations <= 1
+    assert np.max(np.abs(res.x - b / d)) <= 1e-12 * np.max(np.abs(b / d))
+
+
+def test_empty_matrix():
+    empty = g.Csr(0, np.zeros(1, np.int64), np.zeros(0, np.int64), np.zeros(0))
+    ilu = api.IluSolver()
+    ilu.set_matrix(empty)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    assert ilu.substitute(np.zeros(0)).size == 0
+
+
+@pytest.mark.parametrize("lof", [0, 1])
+def test_ragged_rows_against_oracle(port, lof):
+    """Rows of 0 .. 40 off-diagonal entries at random columns: factors and substitution
+    against the oracle, the level-ordered and block-local schedules (with clusters) and
+    one lane per row against lane groups bit for bit, and the mixed-precision solve."""
+    a = ragged(3000, 40, seed=12 + lof)
+    f, _ = port.iluk_symbolic(a, lof)
+    lu_ref, _ = port.factorize(f)
+    _, b = g.random_rhs(a, seed=13)
+    x_ref = port.substitute(f, lu_ref, b)
+    results = []
+    for opts in ({}, {api.ILU_OPT_ROW_LANES: 1}, {api.ILU_OPT_BLOCK_ROWS: 256}, {api.ILU_OPT_BLOCK_ROWS: 1000}):
+        ilu = api.IluSolver()
+        for k, v in opts.items():
+            ilu.set_option(k, v)
+        ilu.set_matrix(f)
+        assert ilu.setup() == 0, api.last_error()
+        assert ilu.factorize() == 0, api.last_error()
+        assert rel_err(ilu.values(), lu_ref, floor=1e-300) <= 1e-12
+        x = ilu.substitute(b)
+        assert rel_err(x, x_ref) <= 1e-12
+        results.append(x)
+    for x in results[1:]:
+        assert np.array_equal(x, results[0])
+    tol = 1e-8 * float(np.linalg.norm(b))
+    res, _, _ = api.ilu_gmres(a, b, lof=lof, tol=tol, restart=30, maxit=1000, mode=1, relative=False)
+    assert res.ok and true_residual(a, b, res.x) <= tol * 1.0001
