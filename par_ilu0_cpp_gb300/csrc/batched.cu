@@ -136,8 +136,18 @@ __device__ void factor_system(const BatchDesc& D, int s, double* red, float* P) 
 }
 
 // Solve item (system s, right-hand side r).
+__device__ __forceinline__ float warp_sum_f32(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// The loops over a system's rows run in FP32 only (coefficients converted once into `cf`,
+// per-thread and per-warp partial sums in FP32, warps combined in FP64): GB300's FP64
+// pipe is far narrower than its FP32 one, and a conversion or FP64 add per element and
+// basis vector set the pace of the Gram-Schmidt passes.
 __device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double* H, double* hc, double* cs,
-                           double* sn, double* rs, int* flag) {
+                           double* sn, double* rs, float* cf, int* flag) {
     if (threadIdx.x == 0) *flag = wait_flag(D.ready + s, D.epoch, D.status) ? 1 : 0;
     __syncthreads();
     const SysView S = sys_view(D, s);
@@ -230,8 +240,8 @@ __device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double
                     const float* vj = V + static_cast<long long>(j) * ws;
                     float part = 0.f;
                     for (int k = tid; k < n; k += T) part = fmaf(vj[k], w[k], part);
-                    const double wsum = warp_sum(static_cast<double>(part));
-                    if ((tid & 31) == 0) red[(tid >> 5) * (kBatchMaxM + 1) + j] = wsum;
+                    const float wsum = warp_sum_f32(part);
+                    if ((tid & 31) == 0) red[(tid >> 5) * (kBatchMaxM + 1) + j] = static_cast<double>(wsum);
                 }
                 __syncthreads();
                 for (int j = tid; j <= i; j += T) {
@@ -242,20 +252,19 @@ __device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double
                     } else {
                         hc[j] += t;
                     }
-                    cs[kBatchMaxM + j] = t;  // this pass's coefficients (scratch above the rotations)
+                    cf[j] = static_cast<float>(t);  // this pass's coefficients
                 }
                 __syncthreads();
                 for (int k = tid; k < n; k += T) {
                     float a = w[k];
-                    for (int j = 0; j <= i; ++j)
-                        a = fmaf(-static_cast<float>(cs[kBatchMaxM + j]), V[static_cast<long long>(j) * ws + k], a);
+                    for (int j = 0; j <= i; ++j) a = fmaf(-cf[j], V[static_cast<long long>(j) * ws + k], a);
                     w[k] = a;
                 }
                 __syncthreads();
             }
-            double nn = 0.0;
-            for (int k = tid; k < n; k += T) nn = fma(static_cast<double>(w[k]), static_cast<double>(w[k]), nn);
-            const double hnext = sqrt(block_sum(nn, red));
+            float nn = 0.f;
+            for (int k = tid; k < n; k += T) nn = fmaf(w[k], w[k], nn);
+            const double hnext = sqrt(block_sum(static_cast<double>(nn), red));
             if (tid == 0) {
                 // Givens update of column i (src/gmres.cpp:238-256)
                 double prev = hc[0];
@@ -295,11 +304,12 @@ __device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double
                 for (int j = ii + 1; j <= last; ++j) t -= H[j * (kBatchMaxM + 1) + ii] * rs[j];
                 rs[ii] = t / H[ii * (kBatchMaxM + 1) + ii];
             }
+            for (int j = 0; j <= last; ++j) cf[j] = static_cast<float>(rs[j]);
         }
         __syncthreads();
         for (int k = tid; k < n; k += T) {
             float d = 0.f;
-            for (int j = 0; j <= last; ++j) d = fmaf(static_cast<float>(rs[j]), Z[static_cast<long long>(j) * ws + k], d);
+            for (int j = 0; j <= last; ++j) d = fmaf(cf[j], Z[static_cast<long long>(j) * ws + k], d);
             x[k] += static_cast<double>(d);
         }
         __syncthreads();
@@ -322,6 +332,7 @@ __global__ void __launch_bounds__(kBatchThreads) batched_ilu_gmres_kernel(BatchD
     __shared__ double cs[2 * kBatchMaxM + 2];
     __shared__ double sn[kBatchMaxM + 1];
     __shared__ double rs[kBatchMaxM + 2];
+    __shared__ float cf[kBatchMaxM + 2];
     __shared__ float P[kMlpParams];
     __shared__ int flag[2];
     __shared__ int s_ticket;
@@ -332,7 +343,7 @@ __global__ void __launch_bounds__(kBatchThreads) batched_ilu_gmres_kernel(BatchD
             factor_system(D, D.sys_of_slot[job], red, P);
         } else {
             const int k = job - nsys_run;
-            solve_item(D, D.sys_of_slot[k / D.nrhs], k % D.nrhs, red, H, hc, cs, sn, rs, flag);
+            solve_item(D, D.sys_of_slot[k / D.nrhs], k % D.nrhs, red, H, hc, cs, sn, rs, cf, flag);
         }
     }
 }
