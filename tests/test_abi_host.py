@@ -183,3 +183,24 @@ def test_read_mm_matches_reference(tmp_path):
     assert np.array_equal(mine.row_ptr, theirs.row_ptr)
     assert np.array_equal(mine.col_idx, theirs.col_idx)
     assert np.array_equal(mine.values, theirs.values)
+
+
+def test_ilu_option_values_checked():
+    """Option values are validated on the host, before any device work."""
+    ilu = api.IluSolver()
+    for v in (0, 1, 2, 4, 8, 16, 32):
+        ilu.set_option(api.ILU_OPT_ROW_LANES, v)
+    for v in (3, 64, -1, 2.5):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_ROW_LANES, v)
+    for v in (0, 1, 4000000):
+        ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, v)
+    for v in (-1, 0.5, 3e9):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, v)
+    for v in (-1, 0, 16384):
+        ilu.set_option(api.ILU_OPT_BLOCK_ROWS, v)
+    with pytest.raises(RuntimeError):
+        ilu.set_option(api.ILU_OPT_BLOCK_ROWS, -2)
+    with pytest.raises(RuntimeError):
+        ilu.set_option(12345, 1)
