@@ -611,7 +611,8 @@ __device__ __forceinline__ int draw_block_ticket(unsigned* counter, int nblk, in
 // descending, src/ilu_solver.cpp:687-696, 719-729): results are identical.
 // ---------------------------------------------------------------------------------
 constexpr int kBlockWarpsMax = 16;
-constexpr int kBlockCluster = 8;  // CTAs per cluster of the cluster variant (portable maximum)
+constexpr int kBlockCluster = 8;      // CTAs per cluster of the cluster variant (portable maximum)
+constexpr int kBlockClusterBig = 16;  // non-portable cluster size, tried first where it can be scheduled
 constexpr int kPubGlobal = 1 << 30;
 constexpr int kPubSlotBits = 15;  // halo slot + 1 of a row, per distance d = 1, 2
 constexpr int kPubSlotMask = (1 << kPubSlotBits) - 1;
