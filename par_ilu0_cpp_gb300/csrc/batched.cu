@@ -325,7 +325,9 @@ __device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double
 
 }  // namespace
 
-__global__ void __launch_bounds__(kBatchThreads) batched_ilu_gmres_kernel(BatchDesc D, int nsys_run) {
+// Two CTAs per SM (64 registers per thread): the autotuner's two-CTA shape must really
+// be resident, and the solve items are latency-bound, so two per SM beat one.
+__global__ void __launch_bounds__(kBatchThreads, 2) batched_ilu_gmres_kernel(BatchDesc D, int nsys_run) {
     __shared__ double red[kBatchWarps * (kBatchMaxM + 1)];
     __shared__ double H[(kBatchMaxM + 1) * kBatchMaxM];
     __shared__ double hc[kBatchMaxM + 2];
