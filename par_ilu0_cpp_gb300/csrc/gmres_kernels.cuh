@@ -592,9 +592,13 @@ template <class T>
 __global__ void __launch_bounds__(256)
     gmres_update_kernel(int n, long long ld, T* __restrict__ Z, double* __restrict__ x, const GmresCtl* ctl, Hess H) {
     __shared__ double srs[kMaxKrylov];
+    __shared__ float srs32[kMaxKrylov];  // FP32 path: the coefficients converted once
     if (ctl->status != kCtlRunning || ctl->steps == 0) return;
     const int nz = ctl->i + 1;
-    for (int j = threadIdx.x; j < nz; j += blockDim.x) srs[j] = H.rs()[j];
+    for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+        srs[j] = H.rs()[j];
+        srs32[j] = static_cast<float>(H.rs()[j]);
+    }
     __syncthreads();
     // plain path: x += sum_j rs[j] z_j in FP64 in ascending j; mixed path: the
     // correction sum_j rs[j] z_j is formed in FP32 and added to the FP64 x.  Eight
@@ -613,7 +617,7 @@ __global__ void __launch_bounds__(256)
                 if constexpr (sizeof(Acc) == sizeof(double)) {
                     xv = fma(srs[j + u], static_cast<double>(z[u]), xv);
                 } else {
-                    d = fma(static_cast<Acc>(srs[j + u]), static_cast<Acc>(z[u]), d);
+                    d = fma(srs32[j + u], static_cast<Acc>(z[u]), d);
                 }
             }
         }
@@ -622,7 +626,7 @@ __global__ void __launch_bounds__(256)
             if constexpr (sizeof(Acc) == sizeof(double)) {
                 xv = fma(srs[j], static_cast<double>(z), xv);
             } else {
-                d = fma(static_cast<Acc>(srs[j]), static_cast<Acc>(z), d);
+                d = fma(srs32[j], static_cast<Acc>(z), d);
             }
         }
         x[r] = xv + static_cast<double>(d);
