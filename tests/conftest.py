@@ -100,3 +100,54 @@ def rel_err(x, ref, floor=None):
     if floor is None:
         floor = 1e-3 * float(np.max(np.abs(ref))) if np.any(ref) else 1.0
     return float(np.max(np.abs(x - ref) / np.maximum(np.abs(ref), floor)))
+
+
+# ---- matrix builders shared by the GPU parity tests and the oracle tests ----
+def csr_from_rows(n, cols_of_row, vals_of_row):
+    """Csr from per-row column and value lists (columns ascending)."""
+    from par_ilu0_cpp_gb300 import generators as g
+
+    rp = np.zeros(n + 1, dtype=np.int64)
+    for i in range(n):
+        rp[i + 1] = rp[i] + len(cols_of_row[i])
+    ci = np.concatenate([np.asarray(c, dtype=np.int64) for c in cols_of_row]) if n else np.zeros(0, np.int64)
+    va = np.concatenate([np.asarray(v, dtype=np.float64) for v in vals_of_row]) if n else np.zeros(0)
+    return g.Csr(n, rp, ci, va)
+
+
+def banded(n, w, seed):
+    """Diagonally dominant matrix with full bandwidth w on both sides: rows of up to w
+    entries per triangle, a dependency chain of n levels."""
+    from par_ilu0_cpp_gb300 import generators as g
+
+    rng = np.random.default_rng(seed)
+    rows, cols = [], []
+    for i in range(n):
+        c = np.arange(max(0, i - w), min(n, i + w + 1))
+        rows.append(np.full(c.size, i))
+        cols.append(c)
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    v = rng.uniform(-1.0, 1.0, r.size)
+    v[r == c] = 2.0 * w + 2.0
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rp, r + 1, 1)
+    return g.Csr(n, np.cumsum(rp), c, v)
+
+
+def ragged(n, kmax, seed):
+    """Non-symmetric pattern, rows with 0 .. kmax off-diagonal entries at random columns,
+    diagonally dominant values."""
+    rng = np.random.default_rng(seed)
+    cols, vals = [], []
+    for i in range(n):
+        k = int(rng.integers(0, kmax + 1))
+        c = np.unique(rng.integers(0, n, size=k))
+        c = c[c != i]
+        v = rng.uniform(-1.0, 1.0, size=c.size)
+        cc = np.append(c, i)
+        vv = np.append(v, np.abs(v).sum() + 1.0)
+        o = np.argsort(cc)
+        cols.append(cc[o])
+        vals.append(vv[o])
+    return csr_from_rows(n, cols, vals)

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import rel_err
+from conftest import banded, csr_from_rows, ragged, rel_err
 from par_ilu0_cpp_gb300 import api
 from par_ilu0_cpp_gb300 import generators as g
 
@@ -208,24 +208,6 @@ def test_block_partition_does_not_change_results(golden, block_rows):
     assert res.ok and abs(res.iterations - golden.gmres_iters) <= 1
 
 
-def banded(n, w, seed):
-    """Diagonally dominant matrix with full bandwidth w on both sides: rows of up to w
-    entries per triangle, a dependency chain of n levels."""
-    rng = np.random.default_rng(seed)
-    rows, cols = [], []
-    for i in range(n):
-        c = np.arange(max(0, i - w), min(n, i + w + 1))
-        rows.append(np.full(c.size, i))
-        cols.append(c)
-    r = np.concatenate(rows)
-    c = np.concatenate(cols)
-    v = rng.uniform(-1.0, 1.0, r.size)
-    v[r == c] = 2.0 * w + 2.0
-    rp = np.zeros(n + 1, dtype=np.int64)
-    np.add.at(rp, r + 1, 1)
-    return g.Csr(n, np.cumsum(rp), c, v)
-
-
 ROW_LANE_CASES = [
     # (name, matrix, fill level, automatic lanes per row of L)
     ("lognormal27_12_k0", lambda: g.lognormal27(12, seed=3), 0, 2),
@@ -345,35 +327,8 @@ def test_cluster_halos_two_positions_back(planes):
     assert res.iterations == res_ref.iterations and np.array_equal(res.x, res_ref.x)
 
 
-def _csr_from_dense_rows(n, cols_of_row, vals_of_row):
-    rp = np.zeros(n + 1, dtype=np.int64)
-    for i in range(n):
-        rp[i + 1] = rp[i] + len(cols_of_row[i])
-    ci = np.concatenate([np.asarray(c, dtype=np.int64) for c in cols_of_row]) if n else np.zeros(0, np.int64)
-    va = np.concatenate([np.asarray(v, dtype=np.float64) for v in vals_of_row]) if n else np.zeros(0)
-    return g.Csr(n, rp, ci, va)
-
-
-def ragged(n, kmax, seed):
-    """Non-symmetric pattern, rows with 0 .. kmax off-diagonal entries at random columns,
-    diagonally dominant values."""
-    rng = np.random.default_rng(seed)
-    cols, vals = [], []
-    for i in range(n):
-        k = int(rng.integers(0, kmax + 1))
-        c = np.unique(rng.integers(0, n, size=k))
-        c = c[c != i]
-        v = rng.uniform(-1.0, 1.0, size=c.size)
-        cc = np.append(c, i)
-        vv = np.append(v, np.abs(v).sum() + 1.0)
-        o = np.argsort(cc)
-        cols.append(cc[o])
-        vals.append(vv[o])
-    return _csr_from_dense_rows(n, cols, vals)
-
-
 def test_single_row_and_diagonal_only():
-    one = _csr_from_dense_rows(1, [[0]], [[4.0]])
+    one = csr_from_rows(1, [[0]], [[4.0]])
     ilu = factorize(one)
     assert ilu.values()[0] == 4.0
     assert ilu.substitute(np.array([2.0]))[0] == 0.5
@@ -381,7 +336,7 @@ def test_single_row_and_diagonal_only():
     assert res.ok and abs(res.x[0] - 0.5) <= 1e-15
     n = 1000
     d = np.linspace(1.0, 3.0, n)
-    diag = _csr_from_dense_rows(n, [[i] for i in range(n)], [[d[i]] for i in range(n)])
+    diag = csr_from_rows(n, [[i] for i in range(n)], [[d[i]] for i in range(n)])
     ilu = factorize(diag)
     assert np.array_equal(ilu.values(), d)
     b = np.arange(n, dtype=np.float64) + 1.0
