@@ -353,6 +353,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(values, dist, device):
+    """Each value's maximum over the ranks (the slowest replica sets every timing); the
+    values unchanged without a process group."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
 def run_ours(args):
     import torch
 
@@ -455,10 +467,7 @@ def run_ours(args):
     clk = clocks.stop()
     launches1 = sum(s[0].info().kernel_launches + s[1].report().kernel_launches for s in solvers.values())
     ms = {k: float(np.mean(v)) for k, v in times.items()}
-    if dist is not None:
-        t = torch.tensor([ms["mixed"], ms["plain"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms["mixed"], ms["plain"] = float(t[0]), float(t[1])
+    ms["mixed"], ms["plain"] = max_over_ranks([ms["mixed"], ms["plain"]], dist, "cuda")
 
     # accuracy of the headline answer (FP64 true residual, forward error vs x_true)
     step("mixed")
