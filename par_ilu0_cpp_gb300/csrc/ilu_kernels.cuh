@@ -641,9 +641,6 @@ struct BlockTri {
     int halo = 0;
     int cl = 0;
     const int* exps = nullptr;      // [32 * ntask]
-    // > 0 (the kernel's KM): every task holds `stride` entries per lane and task t's
-    // slots start at t * stride * 32 (off / len are not read); 0: per-task off / len
-    int stride = 0;
 };
 
 // ---- thread-block cluster helpers (distributed shared memory) ----
