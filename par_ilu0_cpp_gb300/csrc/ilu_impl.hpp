@@ -81,7 +81,6 @@ struct BlockPack {
         p.block_rows = block_rows;
         p.halo = halo;
         p.cl = cl;
-        p.stride = stride;
         p.exps = exps.get();
         p.blk_row = blk_row.get();
         p.blk_task = blk_task.get();
