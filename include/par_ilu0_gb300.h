@@ -45,7 +45,11 @@ bool LLJBASH_GmresSolveDevice(GmresHdl hdl, int n, const int* d_row_ptr, const i
  * of the library, so n is limited to 2,097,152 rows (larger n returns -1).  The first
  * call on a device resolves that array's address (cudaGetSymbolAddress) and should be
  * made before any stream capture.  Every call shares the array; calls whose GPU work
- * overlaps race on it.  Same return codes as the other entry points. */
+ * overlaps race on it.  The work runs on the solver's own stream (created non-blocking,
+ * so it is not ordered after the legacy default stream): d_b must be complete when the
+ * call is made (synchronise the stream that produced it first), and the call blocks
+ * until d_x is written.  The device that is current must be the one the solver was set
+ * up on (another one returns -1).  Same return codes as the other entry points. */
 int LLJBASH_IluSolverSubstituteDeviceNoAlloc(IluSolverHdl hdl, const double* d_b, double* d_x);
 
 /* ILU solver options. */

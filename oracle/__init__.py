@@ -6,14 +6,17 @@ Python bindings for the two CPU checkers of the ILU(k)+GMRES path:
   algorithm (built by oracle/build_port.sh into oracle/_build/libport.so; builds on
   any host, so it is also the CPU baseline on machines without the reference).
 * ``ref``: the reference's own unmodified sources compiled against the shim in
-  oracle/shim (oracle/build_ref.sh -> oracle/_ref/libref.so); only available where
-  the reference checkout is present.
+  oracle/shim (oracle/build_ref.sh -> oracle/_ref/libref.so, libref_strict.so and the
+  threaded-BLAS timing build libref_omp.so); available where the reference checkout is
+  present, or where oracle/_ref/src holds the copy staged by build_ref.sh (oracle/_ref
+  is git-ignored and travels with the working tree).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
 package.  The product library never does.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import os
 import subprocess
@@ -24,6 +27,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libport.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
 REF_STRICT_SO = os.path.join(HERE, "_ref", "libref_strict.so")
+REF_OMP_SO = os.path.join(HERE, "_ref", "libref_omp.so")
+REF_STAGE = os.path.join(HERE, "_ref", "src")
+# where the reference checkout is read from (PAR_ILU0_REFERENCE_DIR overrides)
+DEFAULT_REFERENCE_DIR = "/root/reference"
+
+
+def reference_dir() -> str:
+    return os.environ.get("PAR_ILU0_REFERENCE_DIR", DEFAULT_REFERENCE_DIR)
 
 _I = ctypes.POINTER(ctypes.c_int)
 _D = ctypes.POINTER(ctypes.c_double)
@@ -42,11 +53,37 @@ def build_port() -> str:
     return PORT_SO
 
 
-def build_ref(reference_dir: str = "/root/reference") -> str | None:
-    if not os.path.isfile(os.path.join(reference_dir, "src", "ilu_solver.cpp")):
+def build_ref(ref_dir: str | None = None) -> str | None:
+    """Builds oracle/_ref from the reference checkout, or from the staged copy in
+    oracle/_ref/src where the checkout is absent; None when neither exists."""
+    ref_dir = ref_dir or reference_dir()
+    have = os.path.isfile(os.path.join(ref_dir, "src", "ilu_solver.cpp"))
+    staged = os.path.isfile(os.path.join(REF_STAGE, "src", "ilu_solver.cpp"))
+    if not (have or staged):
         return None
-    subprocess.run([os.path.join(HERE, "build_ref.sh"), reference_dir], check=True, stdout=subprocess.DEVNULL)
+    subprocess.run([os.path.join(HERE, "build_ref.sh"), ref_dir if have else REF_STAGE], check=True,
+                   stdout=subprocess.DEVNULL)
     return REF_SO
+
+
+@contextlib.contextmanager
+def c_stdout_to_stderr():
+    """Sends what native code prints to stdout (the reference prints its setup times
+    there) to stderr for the duration, so that a caller's own stdout (one JSON line)
+    stays clean."""
+    import sys
+
+    libc = ctypes.CDLL(None)
+    sys.stdout.flush()
+    libc.fflush(None)
+    saved = os.dup(1)
+    try:
+        os.dup2(2, 1)
+        yield
+    finally:
+        libc.fflush(None)
+        os.dup2(saved, 1)
+        os.close(saved)
 
 
 def _i32(a):
@@ -189,3 +226,54 @@ class Ref(_Lib):
                                     _dp(_f64(b)), _dp(x), ctypes.c_double(tol), int(restart), int(maxit),
                                     int(nthreads), ctypes.byref(its), _dp(times), _dp(stat))
         return dict(ok=bool(ok), iters=int(its.value), x=x, times=times, stat=stat)
+
+    def session(self, a, lof, tol, restart, maxit, nthreads):
+        """The test/benchmark.cpp repetition loop: symbolic + first setup now, then
+        RefSession.step() = one repetition (Factorize + GMRES timed)."""
+        return RefSession(self, a, lof, tol, restart, maxit, nthreads)
+
+
+class RefSession:
+    def __init__(self, ref, a, lof, tol, restart, maxit, nthreads):
+        lib = ref.lib
+        lib.ref_session_create.restype = ctypes.c_void_p
+        lib.ref_session_set_threads.restype = ctypes.c_double
+        lib.ref_session_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_session_step.argtypes = [ctypes.c_void_p, _D, _D, _I, _D]
+        lib.ref_session_destroy.argtypes = [ctypes.c_void_p]
+        self.lib = lib
+        self.n = a.n
+        self._keep = (_i32(a.row_ptr), _i32(a.col_idx), _f64(a.values))
+        times = np.zeros(2)
+        with c_stdout_to_stderr():
+            self.h = lib.ref_session_create(a.n, _ip(self._keep[0]), _ip(self._keep[1]), _dp(self._keep[2]), int(lof),
+                                            int(restart), int(maxit), ctypes.c_double(tol), int(nthreads),
+                                            _dp(times))
+        self.symbolic_s, self.setup_s = float(times[0]), float(times[1])
+        self.threads = int(nthreads)
+
+    def set_threads(self, nthreads: int) -> float:
+        self.threads = int(nthreads)
+        with c_stdout_to_stderr():
+            return float(self.lib.ref_session_set_threads(self.h, int(nthreads)))
+
+    def step(self, b):
+        """Returns (ok, iters, x, factorize_s, gmres_s)."""
+        bb = _f64(b)
+        x = np.empty(self.n)
+        its = ctypes.c_int(0)
+        times = np.zeros(2)
+        with c_stdout_to_stderr():
+            ok = self.lib.ref_session_step(self.h, _dp(bb), _dp(x), ctypes.byref(its), _dp(times))
+        return bool(ok), int(its.value), x, float(times[0]), float(times[1])
+
+    def close(self):
+        if self.h:
+            self.lib.ref_session_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,32 +1,57 @@
 #!/usr/bin/env bash
-# Oracle test infrastructure: builds the UNMODIFIED reference sources (read in place
-# under the reference checkout) together with oracle/ref_driver.cpp and the MKL /
-# SuiteSparse / tictoc stand-ins in oracle/shim into oracle/_ref/libref.so.
-# Nothing is copied out of the reference tree; outputs go to oracle/_ref/ only.
+# Oracle test infrastructure: builds the UNMODIFIED reference sources together with
+# oracle/ref_driver.cpp and the MKL / SuiteSparse / tictoc stand-ins in oracle/shim.
+# Outputs go to oracle/_ref/ only (git-ignored):
 #
-#   oracle/build_ref.sh [REFERENCE_DIR]        (default /root/reference)
+#   libref.so         reference flags (CMakeLists.txt:19: -O3 -funroll-loops
+#                     -march=native -ffast-math, plus -fopenmp from src/CMakeLists.txt:12),
+#                     serial BLAS-1 stand-ins (index-order sums); made the golden fixtures
+#   libref_strict.so  -O2 -ffp-contract=off (no fast-math, no FMA), for rounding analysis
+#   libref_omp.so     reference flags with OpenMP-threaded BLAS-1 stand-ins (MKL threads
+#                     its BLAS-1 on long vectors); the CPU timing build
 #
-# Flags follow the reference's Release build (CMakeLists.txt:19): -O3 -funroll-loops
-# -march=native -ffast-math, plus -fopenmp (src/CMakeLists.txt:12).  A second library,
-# libref_strict.so, is built with -O2 -ffp-contract=off (no fast-math, no FMA) for
-# rounding analysis.
+#   oracle/build_ref.sh [REFERENCE_DIR]
+#
+# REFERENCE_DIR defaults to $PAR_ILU0_REFERENCE_DIR, else /root/reference.  When the
+# checkout is there, the sources are compiled where they lie and the files this build
+# reads are also staged under oracle/_ref/src, so that a machine the working tree is
+# copied to without the checkout can rebuild from the staged copy (the only other
+# source this script accepts).  Nothing is copied into tracked files.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${PAR_ILU0_REFERENCE_DIR:-/root/reference}}"
 OUT="$HERE/_ref"
-if [ ! -f "$REF/src/ilu_solver.cpp" ]; then
-    echo "reference sources not found under $REF" >&2
+STAGE="$OUT/src"
+mkdir -p "$OUT"
+if [ -f "$REF/src/ilu_solver.cpp" ]; then
+    rm -rf "$STAGE.tmp"
+    mkdir -p "$STAGE.tmp"
+    cp -r "$REF/src" "$REF/include" "$REF/include_c" "$REF/src_c" "$STAGE.tmp/"
+    rm -rf "$STAGE"
+    mv "$STAGE.tmp" "$STAGE"
+elif [ -f "$STAGE/src/ilu_solver.cpp" ]; then
+    REF="$STAGE"
+else
+    echo "reference sources not found under $REF or $STAGE" >&2
     exit 1
 fi
-mkdir -p "$OUT"
 SRCS=("$REF/src/csr_matrix.cpp" "$REF/src/iluk.cpp" "$REF/src/ilu_solver.cpp" "$REF/src/gmres.cpp"
       "$REF/src_c/ilu_solver_c.cpp" "$REF/src_c/gmres_c.cpp" "$HERE/ref_driver.cpp")
 INC=(-I"$HERE/shim" -I"$REF/include" -I"$REF/include_c" -I"$REF/src")
 COMMON=(-std=c++17 -fPIC -shared -fopenmp -include cstdio -include cstdlib -w)
-g++ "${COMMON[@]}" -O3 -funroll-loops -march=native -ffast-math -DNDEBUG "${INC[@]}" "${SRCS[@]}" \
-    -o "$OUT/libref.so.tmp" -Wl,--no-undefined -lgomp -lm
-mv "$OUT/libref.so.tmp" "$OUT/libref.so"
+FAST=(-O3 -funroll-loops -march=native -ffast-math -DNDEBUG)
+g++ "${COMMON[@]}" "${FAST[@]}" "${INC[@]}" "${SRCS[@]}" -o "$OUT/libref.so.tmp" -Wl,--no-undefined -lgomp -lm &
+P1=$!
 g++ "${COMMON[@]}" -O2 -ffp-contract=off -DNDEBUG "${INC[@]}" "${SRCS[@]}" \
-    -o "$OUT/libref_strict.so.tmp" -Wl,--no-undefined -lgomp -lm
+    -o "$OUT/libref_strict.so.tmp" -Wl,--no-undefined -lgomp -lm &
+P2=$!
+g++ "${COMMON[@]}" "${FAST[@]}" -DSHIM_THREADED_BLAS "${INC[@]}" "${SRCS[@]}" \
+    -o "$OUT/libref_omp.so.tmp" -Wl,--no-undefined -lgomp -lm &
+P3=$!
+wait $P1
+wait $P2
+wait $P3
+mv "$OUT/libref.so.tmp" "$OUT/libref.so"
 mv "$OUT/libref_strict.so.tmp" "$OUT/libref_strict.so"
-echo "built $OUT/libref.so $OUT/libref_strict.so"
+mv "$OUT/libref_omp.so.tmp" "$OUT/libref_omp.so"
+echo "built $OUT/libref.so $OUT/libref_strict.so $OUT/libref_omp.so (sources: $REF)"

@@ -209,4 +209,83 @@ void ref_csr_matvec(int n, const int* rp, const int* ci, const double* val, cons
     CsrMatVec(&a, x, y);
 }
 
+/* ---- timing session: the test/benchmark.cpp:104-170 repetition loop ----------------
+ * ref_session_create: IlukSymbolic(A, lof) and the first SetupMatrix, as the benchmark's
+ * first repetition; ref_session_set_threads: SetThreads + SetupMatrix again (the
+ * reference's subtree schedule depends on the thread count); ref_session_step: one
+ * repetition without setup (scatter A into F, Factorize, x = 0, Solve), the two timed
+ * parts returned in times[0..1] (s) measured with steady_clock. */
+struct RefSession {
+    CsrMatrix a;
+    IluSolver ilu;
+    PreconditionedGmres gmres;
+    std::vector<int> nzmap;
+    int n = 0, nnz = 0, knnz = 0;
+};
+
+static void session_scatter(RefSession* s) {
+    CsrMatrix* f = s->ilu.GetMatrix();
+    std::memset(f->value, 0, sizeof(double) * static_cast<size_t>(s->knnz));
+    for (int i = 0; i < s->nnz; ++i) f->value[s->nzmap[i]] = s->a.value[i];
+}
+
+void* ref_session_create(int n, const int* rp, const int* ci, const double* val, int lof, int restart, int maxit,
+                         double tol, int nthreads, double* times) {
+    auto* s = new RefSession;
+    load_matrix(&s->a, n, rp, ci, val);
+    s->n = n;
+    s->nnz = rp[n];
+    s->nzmap.assign(static_cast<size_t>(s->nnz), -1);
+    s->ilu.SetThreads(nthreads);
+    s->gmres.SetIluPreconditioner(&s->ilu);
+    s->gmres.param().tolerance = tol;
+    s->gmres.param().krylov_subspace_dimension = restart;
+    s->gmres.param().max_iterations = maxit;
+    double t0 = now_s();
+    s->knnz = IlukSymbolic(&s->a, lof, s->ilu.GetMatrix(), s->nzmap.data());
+    double t1 = now_s();
+    session_scatter(s);
+    s->ilu.SetupMatrix();
+    double t2 = now_s();
+    if (times) {
+        times[0] = t1 - t0;
+        times[1] = t2 - t1;
+    }
+    return s;
+}
+
+double ref_session_set_threads(void* hdl, int nthreads) {
+    auto* s = static_cast<RefSession*>(hdl);
+    s->ilu.SetThreads(nthreads);
+    session_scatter(s);
+    double t0 = now_s();
+    s->ilu.SetupMatrix();
+    return now_s() - t0;
+}
+
+int ref_session_step(void* hdl, const double* rhs, double* x, int* iters, double* times) {
+    auto* s = static_cast<RefSession*>(hdl);
+    std::vector<double> b(rhs, rhs + s->n);
+    session_scatter(s);
+    double t0 = now_s();
+    s->ilu.Factorize();
+    double t1 = now_s();
+    std::fill_n(x, s->n, 0.0);
+    double t2 = now_s();
+    auto ret = s->gmres.Solve(&s->a, b.data(), x);
+    double t3 = now_s();
+    if (iters) *iters = ret.second;
+    if (times) {
+        times[0] = t1 - t0;
+        times[1] = t3 - t2;
+    }
+    return ret.first ? 1 : 0;
+}
+
+void ref_session_destroy(void* hdl) {
+    auto* s = static_cast<RefSession*>(hdl);
+    DestroyCsrMatrix(&s->a);
+    delete s;
+}
+
 }  // extern "C"

@@ -4,9 +4,10 @@
  * A minimal stand-in for the parts of Intel MKL that the reference solver calls,
  * so that the reference's own sources (src/ilu_solver.cpp, src/gmres.cpp,
  * src/csr_matrix.cpp, src/iluk.cpp) compile unmodified in this container, where
- * MKL is not installed.  Every routine is a plain serial loop restating the
- * BLAS / sparse-BLAS definition; MKL's own blocking and threading are not
- * reproduced, so sums are taken in index order.
+ * MKL is not installed.  Every routine is a plain loop restating the BLAS /
+ * sparse-BLAS definition; MKL's own blocking is not reproduced.  Sums are taken in
+ * index order, except in the timing build (SHIM_THREADED_BLAS), where long vectors are
+ * split over the OpenMP threads as MKL's threaded BLAS-1 does.
  *
  * Call sites in the reference:
  *   cblas_dcopy/ddot/daxpy/dnrm2/dscal : src/gmres.cpp:181,185,191,220,223,226,233,275
@@ -34,23 +35,51 @@ inline void* mkl_malloc(std::size_t size, int alignment) {
 inline void mkl_free(void* p) { std::free(p); }
 inline void MKL_Free_Buffers() {}
 
+/* SHIM_THREADED_BLAS (the CPU timing build): long unit-stride vectors are split over the
+ * OpenMP threads, as MKL's threaded BLAS-1 does; the sums then follow the threads'
+ * partition instead of index order.  Without it every routine is a serial loop. */
+#ifdef SHIM_THREADED_BLAS
+#define SHIM_PAR(n, inc1, inc2) ((n) >= 32768 && (inc1) == 1 && (inc2) == 1)
+#define SHIM_OMP_FOR _Pragma("omp parallel for schedule(static) if(par)")
+#define SHIM_OMP_SUM _Pragma("omp parallel for schedule(static) reduction(+ : s) if(par)")
+#else
+#define SHIM_PAR(n, inc1, inc2) false
+#define SHIM_OMP_FOR
+#define SHIM_OMP_SUM
+#endif
+
 inline void cblas_dcopy(MKL_INT n, const double* x, MKL_INT incx, double* y, MKL_INT incy) {
+    const bool par = SHIM_PAR(n, incx, incy);
+    (void)par;
+    SHIM_OMP_FOR
     for (MKL_INT i = 0; i < n; ++i) y[i * incy] = x[i * incx];
 }
 inline double cblas_ddot(MKL_INT n, const double* x, MKL_INT incx, const double* y, MKL_INT incy) {
+    const bool par = SHIM_PAR(n, incx, incy);
+    (void)par;
     double s = 0.0;
+    SHIM_OMP_SUM
     for (MKL_INT i = 0; i < n; ++i) s += x[i * incx] * y[i * incy];
     return s;
 }
 inline void cblas_daxpy(MKL_INT n, double a, const double* x, MKL_INT incx, double* y, MKL_INT incy) {
+    const bool par = SHIM_PAR(n, incx, incy);
+    (void)par;
+    SHIM_OMP_FOR
     for (MKL_INT i = 0; i < n; ++i) y[i * incy] += a * x[i * incx];
 }
 inline double cblas_dnrm2(MKL_INT n, const double* x, MKL_INT incx) {
+    const bool par = SHIM_PAR(n, incx, 1);
+    (void)par;
     double s = 0.0;
+    SHIM_OMP_SUM
     for (MKL_INT i = 0; i < n; ++i) s += x[i * incx] * x[i * incx];
     return std::sqrt(s);
 }
 inline void cblas_dscal(MKL_INT n, double a, double* x, MKL_INT incx) {
+    const bool par = SHIM_PAR(n, incx, 1);
+    (void)par;
+    SHIM_OMP_FOR
     for (MKL_INT i = 0; i < n; ++i) x[i * incx] *= a;
 }
 /* 1-based index of the first entry of largest magnitude (BLAS i?amax). */

@@ -7,6 +7,7 @@
 #include <climits>
 #include <numeric>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "analysis.hpp"
@@ -358,6 +359,27 @@ BatchSolver::BatchSolver(int nsys, const int* n, const int* rp_all, const int* c
     : nsys_(nsys), nrhs_(nrhs), m_(restart), rtol_(rtol), maxit_(maxit) {
     if (restart < 1 || restart > kBatchMaxM) throw std::runtime_error("batched restart must be in [1, 64]");
     if (nsys < 1 || nrhs < 1) throw std::runtime_error("batched solve needs systems and right-hand sides");
+    // structural check of every system (row pointers local to the system, columns in
+    // [0, n[s]), strictly ascending) before any device work
+    {
+        long long rpp = 0, srcp = 0;
+        std::vector<int> rpl;
+        for (int s = 0; s < nsys; ++s) {
+            const int ns = n[s];
+            const std::string what = "batched system " + std::to_string(s);
+            if (ns < 0) throw std::runtime_error("invalid CSR matrix (" + what + "): negative size");
+            const int* rp = rp_all + rpp;
+            for (int i = 0; i < ns; ++i)
+                if (rp[i + 1] < rp[i])
+                    throw std::runtime_error("invalid CSR matrix (" + what + "): row_ptr decreases at row " +
+                                             std::to_string(i));
+            rpl.resize(static_cast<size_t>(ns) + 1);
+            for (int i = 0; i <= ns; ++i) rpl[static_cast<size_t>(i)] = rp[i] - rp[0];
+            validate_csr(ns, rpl.data(), ci_all + srcp, what.c_str());
+            rpp += ns + 1;
+            srcp += rpl[static_cast<size_t>(ns)];
+        }
+    }
     dev_ = current_device();
     GB_CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     GB_CUDA_CHECK(cudaEventCreate(&ev0_));

@@ -350,6 +350,7 @@ int LLJBASH_IluSolverGetAnalysis(IluSolverHdl hdl, int* diag, int* etree_lower, 
 int LLJBASH_Gb300AnalyzePattern(int n, const int* row_ptr, const int* col_idx, int* diag, int* etree_lower,
                                 int* etree_upper, int* depth_lower, int* depth_upper, int* nlevels) {
     try {
+        gb300::validate_csr(n, row_ptr, col_idx, "pattern");
         gb300::Analysis an;
         gb300::diagonal_pointers(n, row_ptr, col_idx, an.diag);
         const gb300::DagView gl{row_ptr, col_idx, an.diag.data(), true};

@@ -16,10 +16,13 @@
 #include <algorithm>
 #include <chrono>
 #include <cstddef>
+#include <climits>
 #include <stdexcept>
+#include <string>
 
 #include "common.cuh"
 #include "device_util.hpp"
+#include "analysis.hpp"
 #include "gmres_impl.hpp"
 #include "gmres_kernels.cuh"
 #include "ilu_impl.hpp"
@@ -353,16 +356,31 @@ static std::pair<bool, int> solve_core(PreconditionedGmres::Impl& g, IluSolver* 
 
 std::pair<bool, int> PreconditionedGmres::Solve(const CsrMatrix* mat, double* rhs, double* sol) {
     const auto wall0 = std::chrono::steady_clock::now();
+    // bounds of the arrays first (no device work yet); the O(nnz) part of the check runs
+    // below, while the copies are in flight
+    const int n = mat ? mat->size : -1;
+    if (n < 0 || (n > 0 && (mat->row_ptr == nullptr || mat->row_ptr[0] != 0 || mat->row_ptr[n] < 0 ||
+                            (mat->max_nnz > 0 && mat->row_ptr[n] > mat->max_nnz))))
+        validate_csr(n, mat ? mat->row_ptr : nullptr, mat ? mat->col_idx : nullptr, "GMRES matrix",
+                     mat && mat->max_nnz > 0 ? mat->max_nnz : -1);
     Impl& g = *impl_ensure();
     g.init_once();
-    const int n = mat->size;
-    const long long nnz = mat->row_ptr[n];
+    const long long nnz = n > 0 ? mat->row_ptr[n] : 0;
     cudaStream_t s = g.stream;
     bool refresh = false;
     if (!(g.keep_matrix && g.matrix_loaded && g.n == n && g.nnz == nnz)) {
+        // The structural check runs on the host while the copies are in flight; no
+        // kernel touches the arrays before it has passed.
+        g.matrix_loaded = false;
         g.rp.upload(mat->row_ptr, static_cast<size_t>(n) + 1, s);
         g.ci.upload(mat->col_idx, static_cast<size_t>(nnz), s);
         g.a64.upload(mat->value, static_cast<size_t>(nnz), s);
+        try {
+            validate_csr(n, mat->row_ptr, mat->col_idx, "GMRES matrix", mat->max_nnz > 0 ? mat->max_nnz : -1);
+        } catch (...) {
+            cudaStreamSynchronize(s);
+            throw;
+        }
         refresh = true;
     }
     g.matrix_loaded = true;
@@ -397,10 +415,27 @@ std::pair<bool, int> PreconditionedGmres::SolveDevice(int n, const int* d_row_pt
     Impl& g = *impl_ensure();
     g.init_once();
     long long nnz = 0;
+    if (n < 0) throw std::runtime_error("invalid CSR matrix (GMRES matrix): negative size");
     if (n > 0) {
         int last = 0;
         GB_CUDA_CHECK(cudaMemcpy(&last, d_row_ptr + n, sizeof(int), cudaMemcpyDeviceToHost));
         nnz = last;
+        if (nnz < 0) throw std::runtime_error("invalid CSR matrix (GMRES matrix): row_ptr[n] is negative");
+        // structural check on the device before any kernel indexes with the arrays
+        // (the device arrays are taken to hold n + 1 row pointers and row_ptr[n] entries)
+        const int init = INT_MAX;
+        int* flag = reinterpret_cast<int*>(g.counters.get() + kCounterCheck);
+        GB_CUDA_CHECK(cudaMemcpyAsync(flag, &init, sizeof(int), cudaMemcpyHostToDevice, g.stream));
+        const int grid = static_cast<int>(std::min<long long>(4ll * g.dev.sms, ceil_div<long long>(n, 256)));
+        csr_check_kernel<<<grid, 256, 0, g.stream>>>(n, nnz, d_row_ptr, d_col_idx, flag);
+        GB_CUDA_CHECK(cudaGetLastError());
+        g.launches += 1;
+        int bad = INT_MAX;
+        GB_CUDA_CHECK(cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, g.stream));
+        GB_CUDA_CHECK(cudaStreamSynchronize(g.stream));
+        if (bad != INT_MAX)
+            throw std::runtime_error("invalid CSR matrix (GMRES matrix): row " + std::to_string(bad) +
+                                     " has bad row pointers or column indices outside [0, n) or not ascending");
     }
     g.n = n;
     g.nnz = nnz;

@@ -24,6 +24,10 @@ enum KernelKind {
     kKKinds
 };
 
+// Word of PreconditionedGmres::Impl::counters that the structural check of a
+// device-resident matrix reports into ([0] is the reductions' ticket counter).
+constexpr int kCounterCheck = 3;
+
 // Precision modes of Solve().
 enum SolveMode { kModePlain = 0, kModeMixed = 1 };
 
@@ -79,7 +83,7 @@ struct PreconditionedGmres::Impl {
     gb300::Krylov<double> k64;
     gb300::Krylov<float> k32;
     gb300::DeviceBuffer<double> hh, h1, h2, partial;
-    gb300::DeviceBuffer<unsigned> counters;  // [0] reductions
+    gb300::DeviceBuffer<unsigned> counters;  // [0] reductions, [kCounterCheck] CSR check
     gb300::DeviceBuffer<gb300::GmresCtl> ctl;
     gb300::GmresCtl* ctl_host = nullptr;  // pinned mirror
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

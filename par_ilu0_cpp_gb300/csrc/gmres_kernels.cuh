@@ -11,8 +11,11 @@
 // with leading dimension ld = n rounded up to 512 entries; the padding entries of V are
 // zero and never written with anything else, so whole chunks can be processed without
 // bounds checks.  Basis type T is double (plain path) or float (mixed-precision inner
-// cycles); every reduction (dot products, norms) accumulates in double, and the
-// Hessenberg matrix, rotations and least-squares solution are double.
+// cycles).  Norms accumulate in double from the first product.  Dot products (the
+// Gram-Schmidt coefficients) accumulate in double for FP64 bases; for FP32 bases a warp
+// sums its chunks' products in float (128 rows per chunk, a few chunks per warp) and
+// those sums are added in double across warps and blocks.  The Hessenberg matrix,
+// rotations and least-squares solution are double.
 #pragma once
 
 #include "common.cuh"
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(kSpmvWarps * kWarp)
 // read of a warp's basis rows within L2's reach (2 KB chunks sent half of them to DRAM).
 // FP32 bases keep the coefficients and the per-warp rows in FP32 (a warp adds a few
 // chunk sums) and sum the rows over warps and blocks in FP64, so their per-basis-vector
-// loops contain no FP64 instruction.
+// loops contain no FP64 instruction; the norm (once per step) accumulates in FP64.
 // ---------------------------------------------------------------------------------
 // Resident blocks per SM the Gram-Schmidt kernels are compiled for: two for FP32 (64
 // registers per thread), one for FP64 (whose kernels are bound by the FP64 pipe).
@@ -532,13 +535,12 @@ __global__ void __launch_bounds__(kBlasThreads, kBlasMinBlocks<T>)
 #pragma unroll
         for (int u = 0; u < RPL; ++u) x[u] = static_cast<Acc>(a[u]);
         chunk_axpy_rows<T>(V, ld, nv, r0, sh, x);
-        Acc q = 0;
+        // the norm accumulates in double from the first product, also for FP32 bases
 #pragma unroll
         for (int u = 0; u < RPL; ++u) {
             a[u] = static_cast<T>(x[u]);
-            q = fma(static_cast<Acc>(a[u]), static_cast<Acc>(a[u]), q);
+            ss = fma(static_cast<double>(a[u]), static_cast<double>(a[u]), ss);
         }
-        ss += static_cast<double>(q);
         store_rpl<T, RPL>(wv + r0, a);
     }
     ss = warp_sum(ss);
@@ -651,6 +653,32 @@ __global__ void convert_kernel(long long n, const S* __restrict__ s, D* __restri
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x)
         d[i] = static_cast<D>(s[i]);
+}
+
+// Structural check of a device-resident CSR matrix of n rows and nnz entries (the row
+// pointers hold n + 1 entries, the column indices nnz): row_ptr[0] == 0, row_ptr
+// non-decreasing up to row_ptr[n] == nnz, columns in [0, n) and strictly ascending in
+// each row.  *bad (INT_MAX on entry) receives the smallest offending row.  A row's
+// columns are read only once its bounds have been checked, so no input makes the
+// kernel read outside the two arrays.
+static __global__ void csr_check_kernel(int n, long long nnz, const int* __restrict__ rp, const int* __restrict__ ci,
+                                 int* bad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long b = rp[i], e = rp[i + 1];
+        bool ok = b >= 0 && e >= b && e <= nnz && (i != 0 || b == 0) && (i != n - 1 || e == nnz);
+        if (ok) {
+            int prev = -1;
+            for (long long p = b; p < e; ++p) {
+                const int c = ci[p];
+                if (c < 0 || c >= n || c <= prev) {
+                    ok = false;
+                    break;
+                }
+                prev = c;
+            }
+        }
+        if (!ok) atomicMin(bad, i);
+    }
 }
 
 }  // namespace gb300

@@ -706,6 +706,7 @@ void IluSolver::SetupMatrix() {
     if (n < 0 || aMatrix_.row_ptr == nullptr) throw std::runtime_error("matrix not set");
     const int* rp = aMatrix_.row_ptr;
     const int* ci = aMatrix_.col_idx;
+    validate_csr(n, rp, ci, "ILU matrix", aMatrix_.max_nnz > 0 ? aMatrix_.max_nnz : -1);
     Analysis an;
     diagonal_pointers(n, rp, ci, an.diag);  // throws "missing diag"
     const DagView gl{rp, ci, an.diag.data(), true};
@@ -1040,9 +1041,16 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
     if (n > kNoAllocMaxRows)
         throw std::runtime_error("SubstituteDeviceNoAlloc supports at most 2097152 rows (static scratch limit)");
     if (n == 0) return;
+    // The scratch address and the solver's stream must belong to the same GPU: the
+    // address is resolved with the solver's device current, and a call made while
+    // another device is current is refused instead of mixing the two.
     int device = 0;
     GB_CUDA_CHECK(cudaGetDevice(&device));
-    unsigned char* base = static_cast<unsigned char*>(noalloc_scratch_address(device));
+    if (device != im.dev.device)
+        throw std::runtime_error("SubstituteDeviceNoAlloc: the current device (" + std::to_string(device) +
+                                 ") is not the device the solver was set up on (" + std::to_string(im.dev.device) +
+                                 ")");
+    unsigned char* base = static_cast<unsigned char*>(noalloc_scratch_address(im.dev.device));
     double* y = reinterpret_cast<double*>(base);
     unsigned* counters = reinterpret_cast<unsigned*>(base + kNoAllocMaxRows * sizeof(double));
     int* status = reinterpret_cast<int*>(counters + 4);

@@ -15,7 +15,7 @@ that library through ctypes on small seeded matrices and stores, per case:
   GMRES(m) from x0 = 0 with tol = 1e-8 ||b||: ok flag, its, x   (src/gmres.cpp:138-288)
 
 Run from the repository root (needs the reference checkout):
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [REFERENCE_DIR]   (default: oracle.reference_dir())
 """
 from __future__ import annotations
 
@@ -75,7 +75,7 @@ def cases():
     yield "single_1", g.Csr(1, [0, 1], [0], [3.0]), 0, 5
 
 
-def main(ref_dir: str = "/root/reference") -> None:
+def main(ref_dir: str | None = None) -> None:
     oracle.build_ref(ref_dir)
     ref = oracle.Ref()
     store = {}

@@ -93,6 +93,48 @@ def test_large_against_oracle(port, name, make, lof, m):
     assert true_residual(a, b, res.x) <= tol * 1.0001
 
 
+# The benchmark configurations at full size: 128^3 7-point convection-diffusion with
+# ILU(0) + GMRES(50) (the configuration the headline is measured on: FP64 blocks of
+# 16,384 rows, FP32 clusters over 32,768-row blocks) and the 64^3 27-point lognormal
+# operator with ILU(1) / ILU(2) + GMRES(30) (lane-group sweeps).  Factors and one FP64
+# substitution against the oracle port to 1e-12, plain FP64 GMRES iterations within +-1
+# of the port's, and the FP64 true residual of the plain and mixed-precision solves.
+FULL = [
+    ("convdiff3d_128_ilu0", lambda: g.convdiff3d(128), 0, 50),
+    ("lognormal27_64_ilu1", lambda: g.lognormal27(64, seed=0), 1, 30),
+    ("lognormal27_64_ilu2", lambda: g.lognormal27(64, seed=0), 2, 30),
+]
+
+
+@pytest.mark.parametrize("name,make,lof,m", FULL, ids=[c[0] for c in FULL])
+def test_benchmark_configuration_against_oracle(port, name, make, lof, m):
+    import os
+
+    threads = os.cpu_count() or 1
+    a = make()
+    f, _ = api.iluk_symbolic(a, lof)  # bit-exact with the reference (CPU test)
+    lu_ref, _ = port.factorize(f, nthreads=threads)
+    ilu = factorize(f)
+    assert rel_err(ilu.values(), lu_ref, floor=1e-300) <= 1e-12
+    x_true, b = g.random_rhs(a, seed=0)
+    assert rel_err(ilu.substitute(b), port.substitute(f, lu_ref, b)) <= 1e-12
+    tol = 1e-8 * float(np.linalg.norm(b))
+    ok, its, _, _ = port.gmres(a, f, lu_ref, b, tol, m, 1000, nthreads=threads)
+    assert ok
+    gm = api.Gmres(tol, m, 1000)
+    gm.set_preconditioner(ilu)
+    res = gm.solve(a, b)
+    assert res.ok and abs(res.iterations - its) <= 1, (res.iterations, its)
+    assert true_residual(a, b, res.x) <= tol * 1.0001
+    mixed = api.Gmres(tol, m, 1000)
+    mixed.set_preconditioner(ilu)
+    mixed.set_option(api.GMRES_OPT_MODE, 1)
+    rm = mixed.solve(a, b)
+    assert rm.ok and true_residual(a, b, rm.x) <= tol * 1.0001
+    print(f"{name}: iterations plain {res.iterations} (oracle {its}), mixed {rm.iterations}; forward error "
+          f"plain {np.max(np.abs(res.x - x_true)):.2e}, mixed {np.max(np.abs(rm.x - x_true)):.2e}")
+
+
 def test_modes_are_deterministic():
     a = g.convdiff3d(24)
     x_true, b = g.random_rhs(a, seed=2)

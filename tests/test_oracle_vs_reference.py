@@ -53,3 +53,43 @@ def test_port_matches_reference_build(port, ref, name, make, lof):
     x_ref, _ = ref.substitute(f_ref, lu_ref, b, nthreads=4)
     x = port.substitute(f, lu, b)
     assert rel_err(x, x_ref) <= 1e-12
+
+
+# ---- the benchmark configurations at full size ---------------------------------------
+# The host integer output (ILU(k) pattern, nzmap, diagonal pointers, both elimination
+# trees and both level-depth arrays) of the library against the reference build on the
+# 128^3 7-point ILU(0) factor and the 64^3 27-point ILU(1) / ILU(2) factors (15.7M and
+# 24.0M entries), bit for bit.
+FULL = [
+    ("convdiff3d_128_ilu0", lambda: g.convdiff3d(128), 0),
+    ("lognormal27_64_ilu1", lambda: g.lognormal27(64, seed=0), 1),
+    ("lognormal27_64_ilu2", lambda: g.lognormal27(64, seed=0), 2),
+]
+
+
+@pytest.fixture(scope="module")
+def ref_fast():
+    try:
+        return oracle.Ref(oracle.REF_SO)
+    except OSError as e:
+        pytest.skip(f"reference build not loadable here: {e}")
+
+
+@pytest.mark.parametrize("name,make,lof", FULL, ids=[c[0] for c in FULL])
+def test_host_analysis_bit_exact_at_benchmark_sizes(ref_fast, name, make, lof):
+    from par_ilu0_cpp_gb300 import api
+
+    a = make()
+    f_ref, nz_ref = ref_fast.iluk_symbolic(a, lof)
+    f, nz = api.iluk_symbolic(a, lof)
+    assert np.array_equal(f.row_ptr, f_ref.row_ptr)
+    assert np.array_equal(f.col_idx, f_ref.col_idx)
+    assert np.array_equal(nz, nz_ref)
+    an = api.analyze_pattern(f)
+    assert np.array_equal(an["diag"], ref_fast.diag_ptr(f_ref))
+    assert np.array_equal(an["etree_l"], ref_fast.etree(f_ref, True))
+    assert np.array_equal(an["etree_u"], ref_fast.etree(f_ref, False))
+    depth_l, nl = ref_fast.levels(f_ref, True)
+    depth_u, nu = ref_fast.levels(f_ref, False)
+    assert np.array_equal(an["depth_l"], depth_l) and np.array_equal(an["depth_u"], depth_u)
+    assert list(an["nlev"]) == [nl, nu]

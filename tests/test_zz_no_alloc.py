@@ -19,7 +19,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import banded, rel_err
 from par_ilu0_cpp_gb300 import api
 from par_ilu0_cpp_gb300 import build as nb
 from par_ilu0_cpp_gb300 import generators as g
@@ -58,17 +58,45 @@ class _DeviceArray:
         self.rt.cudaFree(self.ptr)
 
 
-@pytest.mark.parametrize("make", [lambda: g.laplace2d(64), lambda: g.convdiff3d(20),
-                                  lambda: g.lognormal27(8, seed=2)])
-def test_no_alloc_substitution_matches_existing_entry_point(make):
+def _solver(a, block_rows=0, solve_warps=0):
+    f, _ = api.iluk_symbolic(a, 0)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
+    if solve_warps:
+        ilu.set_option(api.ILU_OPT_SOLVE_WARPS, solve_warps)
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    return ilu
+
+
+def _no_alloc(lib, ilu, d_b, d_x):
+    return lib.LLJBASH_IluSolverSubstituteDeviceNoAlloc(ctypes.c_void_p(ilu.h), d_b.ptr, d_x.ptr)
+
+
+# Both substitution schedules: the automatic choice (block-local kernels with clusters on
+# the 3-D grid, block-local on the 2-D one), the block-local kernel forced with an
+# explicit block size, and the level-ordered kernel (-1) on every matrix.
+CASES = [("laplace2d_64_auto", lambda: g.laplace2d(64), 0),
+         ("laplace2d_64_level", lambda: g.laplace2d(64), -1),
+         ("convdiff3d_20_auto", lambda: g.convdiff3d(20), 0),
+         ("convdiff3d_20_block", lambda: g.convdiff3d(20), 800),
+         ("convdiff3d_20_level", lambda: g.convdiff3d(20), -1),
+         ("lognormal27_8_auto", lambda: g.lognormal27(8, seed=2), 0),
+         ("lognormal27_8_level", lambda: g.lognormal27(8, seed=2), -1)]
+
+
+@pytest.mark.parametrize("name,make,block_rows", CASES, ids=[c[0] for c in CASES])
+def test_no_alloc_substitution_matches_existing_entry_point(name, make, block_rows):
     lib = api.load()
     rt = _cudart()
     a = make()
-    f, _ = api.iluk_symbolic(a, 0)
-    ilu = api.IluSolver()
-    ilu.set_matrix(f)
-    assert ilu.setup() == 0
-    assert ilu.factorize() == 0
+    ilu = _solver(a, block_rows)
+    info = ilu.info()
+    if block_rows == -1:
+        assert info.block_rows_fp64 == 0  # level-ordered kernel
+    elif block_rows > 0:
+        assert info.block_rows_fp64 == block_rows  # block-local kernel
     rng = np.random.default_rng(11)
     rhs = [rng.uniform(-1, 1, a.n), rng.uniform(-1, 1, a.n)]
     expected = [ilu.substitute(b) for b in rhs]
@@ -77,10 +105,42 @@ def test_no_alloc_substitution_matches_existing_entry_point(make):
     try:
         for b, ref in zip(rhs, expected):  # two calls in a row share the static scratch
             d_b.put(b)
-            rc = lib.LLJBASH_IluSolverSubstituteDeviceNoAlloc(ctypes.c_void_p(ilu.h), d_b.ptr, d_x.ptr)
+            rc = _no_alloc(lib, ilu, d_b, d_x)
             assert rc == 0, api.last_error()
             assert rel_err(d_x.get(), ref) <= 1e-12
             assert np.array_equal(d_b.get(), b)  # the input is left untouched
+    finally:
+        d_b.free()
+        d_x.free()
+
+
+def test_no_alloc_recovers_after_a_wait_gives_up():
+    """A call whose device-side wait reaches its limit returns -1 and leaves the shared
+    scratch with a set status word; the next call with the normal limit must clear it
+    and match the existing entry point.  A 1 us limit cuts short the real waits of the
+    1,500-level chain of a banded matrix solved by 1,024 warps (the level-ordered kernel
+    takes tasks far ahead of the critical path)."""
+    lib = api.load()
+    rt = _cudart()
+    a = banded(1500, 100, 4)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_SOLVE_WARPS, 1024)
+    ilu.set_matrix(a)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    b = np.random.default_rng(8).uniform(-1, 1, a.n)
+    ref = ilu.substitute(b)
+    d_b = _DeviceArray(rt, a.n)
+    d_x = _DeviceArray(rt, a.n)
+    try:
+        d_b.put(b)
+        ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 1)
+        assert _no_alloc(lib, ilu, d_b, d_x) == -1
+        assert "timed out" in api.last_error()
+        ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 0)
+        for _ in range(2):
+            assert _no_alloc(lib, ilu, d_b, d_x) == 0, api.last_error()
+            assert rel_err(d_x.get(), ref) <= 1e-12
     finally:
         d_b.free()
         d_x.free()
