@@ -87,7 +87,19 @@ enum {
      * default, 4 s).  A wait that reaches it gives up: the call that launched it returns
      * -1 ("dependency wait timed out on the device") and the solver stays usable.  Takes
      * effect at the next launch. */
-    LLJBASH_ILU_OPT_WAIT_LIMIT_US = 5
+    LLJBASH_ILU_OPT_WAIT_LIMIT_US = 5,
+    /* structured-grid sweeps (results are the same as with every other schedule): for
+     * factors that are a full 7-point (3-D) or 5-point (2-D) stencil in natural order, the
+     * triangular sweeps run on a fixed wavefront schedule (a lane walks a grid line in
+     * registers, neighbours arrive by warp shuffles and shared memory), taking precedence
+     * over LLJBASH_ILU_OPT_BLOCK_ROWS.  0 (default): on when the pattern qualifies;
+     * -1: off.  Takes effect at the next IluSolverSetup. */
+    LLJBASH_ILU_OPT_GRID = 6,
+    /* tuning of the structured-grid sweeps (0 = automatic), next IluSolverSetup:
+     * elements per lane along x (1, 2, 4), grid lines per tile, grid planes per tile. */
+    LLJBASH_ILU_OPT_GRID_LANE_ELEMS = 7,
+    LLJBASH_ILU_OPT_GRID_TILE_LINES = 8,
+    LLJBASH_ILU_OPT_GRID_TILE_PLANES = 9
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 
@@ -145,6 +157,13 @@ typedef struct LLJBASH_IluInfo {
     int block_cluster_fp32; /* the same for the FP32 sweeps */
     int row_lanes_lower;  /* lanes per row of the level-ordered lower / upper sweeps */
     int row_lanes_upper;
+    int grid_fp64;        /* 1: the FP64 / FP32 sweeps use the structured-grid schedule */
+    int grid_fp32;
+    int grid_nx, grid_ny, grid_nz;  /* its grid (2-D: grid_ny = 1) */
+    int grid_lane_elems;  /* elements per lane, lines and planes per tile, tiles */
+    int grid_tile_lines;
+    int grid_tile_planes;
+    int grid_tiles;
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

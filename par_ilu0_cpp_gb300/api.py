@@ -50,7 +50,10 @@ class IluInfo(ctypes.Structure):
                 ("factor_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong), ("shift_applied", ctypes.c_int),
                 ("block_rows_fp64", ctypes.c_int), ("block_rows_fp32", ctypes.c_int),
                 ("block_cluster_fp64", ctypes.c_int), ("block_cluster_fp32", ctypes.c_int),
-                ("row_lanes_lower", ctypes.c_int), ("row_lanes_upper", ctypes.c_int)]
+                ("row_lanes_lower", ctypes.c_int), ("row_lanes_upper", ctypes.c_int),
+                ("grid_fp64", ctypes.c_int), ("grid_fp32", ctypes.c_int), ("grid_nx", ctypes.c_int),
+                ("grid_ny", ctypes.c_int), ("grid_nz", ctypes.c_int), ("grid_lane_elems", ctypes.c_int),
+                ("grid_tile_lines", ctypes.c_int), ("grid_tile_planes", ctypes.c_int), ("grid_tiles", ctypes.c_int)]
 
 
 class GmresReport(ctypes.Structure):
@@ -64,6 +67,10 @@ ILU_OPT_BLOCK_ROWS = 2
 ILU_OPT_SOLVE_WARPS = 3
 ILU_OPT_ROW_LANES = 4
 ILU_OPT_WAIT_LIMIT_US = 5
+ILU_OPT_GRID = 6
+ILU_OPT_GRID_LANE_ELEMS = 7
+ILU_OPT_GRID_TILE_LINES = 8
+ILU_OPT_GRID_TILE_PLANES = 9
 GMRES_OPT_MODE = 1
 GMRES_OPT_TAU = 2
 GMRES_OPT_USE_GRAPH = 3

@@ -157,6 +157,22 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 if (value < -1 || value > 1e8) throw std::runtime_error("block rows must be -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);
                 return 0;
+            case LLJBASH_ILU_OPT_GRID:
+                if (value != -1 && value != 0 && value != 1) throw std::runtime_error("grid sweeps must be -1, 0 or 1");
+                s->impl()->grid_mode = static_cast<int>(value);
+                return 0;
+            case LLJBASH_ILU_OPT_GRID_LANE_ELEMS:
+                if (value != 0 && value != 1 && value != 2 && value != 4)
+                    throw std::runtime_error("grid elements per lane must be 0 (automatic), 1, 2 or 4");
+                s->impl()->grid_elems = static_cast<int>(value);
+                return 0;
+            case LLJBASH_ILU_OPT_GRID_TILE_LINES:
+            case LLJBASH_ILU_OPT_GRID_TILE_PLANES:
+                if (value < 0 || value > 1e6 || value != static_cast<int>(value))
+                    throw std::runtime_error("grid tile size must be 0 (automatic) or a positive count");
+                (option == LLJBASH_ILU_OPT_GRID_TILE_LINES ? s->impl()->grid_lines : s->impl()->grid_planes) =
+                    static_cast<int>(value);
+                return 0;
             default:
                 g_last_error = "unknown ILU option";
                 return -1;
@@ -325,6 +341,17 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->block_cluster_fp32 = im->blk32 ? im->LB32.cl : 0;
     info->row_lanes_lower = im->level_packs ? im->L.group : 0;
     info->row_lanes_upper = im->level_packs ? im->U.group : 0;
+    info->grid_fp64 = im->grid64 ? 1 : 0;
+    info->grid_fp32 = im->grid32 ? 1 : 0;
+    if (im->grid64 || im->grid32) {
+        info->grid_nx = im->GP.g.nx;
+        info->grid_ny = im->GP.g.ny;
+        info->grid_nz = im->GP.g.nz;
+        info->grid_lane_elems = im->GP.g.E;
+        info->grid_tile_lines = im->GP.jb;
+        info->grid_tile_planes = im->GP.kc;
+        info->grid_tiles = im->GP.ntile;
+    }
     return 0;
 }
 

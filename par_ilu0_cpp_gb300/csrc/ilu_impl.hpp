@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "device_util.hpp"
+#include "grid_sweep.cuh"
 #include "ilu_kernels.cuh"
 #include "ilu_solver.hpp"
 #include "mlp_impl.hpp"
@@ -99,6 +100,47 @@ struct BlockPack {
     }
 };
 
+// Structured-grid factor (wavefront-lanes sweeps, grid_sweep.cuh): the sweep layout,
+// the coefficient sources (positions in the factor's value array, -1 where absent) and
+// the gathered coefficients and work vectors per value type.
+struct GridPack {
+    GridLayout g;
+    int jb = 1, kc = 1;       // tile shape
+    int ntile = 0;
+    int threads = 0;          // CTA size: nic * jb warps
+    int grid = 0;             // CTAs to launch
+    size_t smem = 0;          // dynamic shared memory of one CTA (type-dependent)
+    DeviceBuffer<long long> pos;                       // [n] layout position of each row
+    DeviceBuffer<int2> tiles_l, tiles_u;               // tickets -> (tile line, tile plane)
+    DeviceBuffer<int> src_lz, src_ly, src_lx, src_uz, src_uy, src_ux, src_ud;  // [len]
+    DeviceBuffer<double> lz64, ly64, lx64, uz64, uy64, ux64, ud64;
+    DeviceBuffer<float> lz32, ly32, lx32, uz32, uy32, ux32, ud32;
+    DeviceBuffer<double> b64, y64, z64;                 // layout work vectors
+    DeviceBuffer<float> b32, y32, z32;
+
+    template <class T>
+    GridTri<T> view(bool upper) const {
+        GridTri<T> p;
+        p.g = g;
+        p.jb = jb;
+        p.kc = kc;
+        p.ntile = ntile;
+        p.tiles = upper ? tiles_u.get() : tiles_l.get();
+        if constexpr (sizeof(T) == 8) {
+            p.cz = upper ? uz64.get() : lz64.get();
+            p.cy = upper ? uy64.get() : ly64.get();
+            p.cx = upper ? ux64.get() : lx64.get();
+            p.d = upper ? ud64.get() : nullptr;
+        } else {
+            p.cz = upper ? uz32.get() : lz32.get();
+            p.cy = upper ? uy32.get() : ly32.get();
+            p.cx = upper ? ux32.get() : lx32.get();
+            p.d = upper ? ud32.get() : nullptr;
+        }
+        return p;
+    }
+};
+
 // Host-side results of the pattern analysis (integer output identical to the
 // reference's; see analysis.hpp).
 struct Analysis {
@@ -132,6 +174,14 @@ struct IluSolver::Impl {
     gb300::BlockPack LB64, UB64, LB32, UB32;
     bool blk64 = false, blk32 = false;
     bool level_packs = false;  // L and U (level-ordered warp layout) are built
+    // structured-grid sweeps (grid_sweep.cuh) per value type, when the factor is a 7- or
+    // 5-point stencil in natural order and grid_mode allows it
+    gb300::GridPack GP;
+    bool grid64 = false, grid32 = false;
+    int grid_mode = 0;       // 0 automatic, 1 force (when structured), -1 off
+    int grid_elems = 0;      // requested elements per lane (0 automatic: 1)
+    int grid_lines = 0;      // requested lines per tile (0 automatic)
+    int grid_planes = 0;     // requested planes per tile (0 automatic)
     unsigned setup_gen = 0;    // incremented by every SetupMatrix
     gb300::DeviceBuffer<double> sb64, sy64, sx64;  // Substitute() work vectors
     gb300::DeviceBuffer<float> sy32;               // FP32 forward-sweep intermediate

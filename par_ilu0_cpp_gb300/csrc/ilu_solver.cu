@@ -625,6 +625,224 @@ static void fill_sentinel(T* p, long long n, cudaStream_t s, int sms) {
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
+// ---- structured-grid sweeps (grid_sweep.cuh) ------------------------------------
+// Grid shape of a factor pattern that is a full 7-point (3-D) or 5-point (2-D) stencil
+// in natural order: strict-lower columns of row r = i + nx j + nx ny k exactly
+// {r - nx ny (k > 0), r - nx (j > 0), r - 1 (i > 0)} and strict-upper columns exactly
+// {r + 1 (i < nx - 1), r + nx (j < ny - 1), r + nx ny (k < nz - 1)}; a 2-D grid is
+// ny = 1 with the line offset as the plane offset.  Returns false otherwise.
+static bool detect_grid(int n, const int* rp, const int* ci, const std::vector<int>& diag, int& nx, int& ny,
+                        int& nz) {
+    if (n < 64) return false;
+    // distinct strict-lower offsets (at most three)
+    int offs[4];
+    int no = 0;
+    for (int r = 0; r < n && no <= 3; ++r)
+        for (int p = rp[r]; p < diag[r] && no <= 3; ++p) {
+            const int o = r - ci[p];
+            bool seen = false;
+            for (int t = 0; t < no; ++t) seen = seen || offs[t] == o;
+            if (!seen) offs[no++] = o;
+        }
+    if (no < 2 || no > 3) return false;
+    std::sort(offs, offs + no);
+    if (offs[0] != 1) return false;
+    const int P = offs[no - 1];
+    nx = offs[1];
+    if (nx < 2 || P % nx != 0 || n % P != 0) return false;
+    ny = no == 3 ? P / nx : 1;
+    if (no == 3 && ny < 2) return false;
+    nz = n / P;
+    if (nz < 2) return false;
+    for (int r = 0; r < n; ++r) {
+        const int i = r % nx;
+        const int j = (r / nx) % ny;
+        const int k = r / P;
+        int want[3], nw = 0;
+        if (k > 0) want[nw++] = r - P;
+        if (no == 3 && j > 0) want[nw++] = r - nx;
+        if (i > 0) want[nw++] = r - 1;
+        if (diag[r] - rp[r] != nw) return false;
+        for (int t = 0; t < nw; ++t)
+            if (ci[rp[r] + t] != want[t]) return false;
+        nw = 0;
+        if (i < nx - 1) want[nw++] = r + 1;
+        if (no == 3 && j < ny - 1) want[nw++] = r + nx;
+        if (k < nz - 1) want[nw++] = r + P;
+        if (rp[r + 1] - diag[r] - 1 != nw) return false;
+        for (int t = 0; t < nw; ++t)
+            if (ci[diag[r] + 1 + t] != want[t]) return false;
+    }
+    return true;
+}
+
+// Tickets of the tile grid in dependency order: anti-diagonals d = tile line + tile
+// plane ascending (lower) or descending with each diagonal reversed (upper).
+static std::vector<int2> grid_tile_order(int tj, int tk, bool upper) {
+    std::vector<int2> t;
+    t.reserve(static_cast<size_t>(tj) * tk);
+    for (int d = 0; d < tj + tk - 1; ++d)
+        for (int a = 0; a < tj; ++a) {
+            const int b = d - a;
+            if (b >= 0 && b < tk) t.push_back(make_int2(a, b));
+        }
+    if (upper) std::reverse(t.begin(), t.end());
+    return t;
+}
+
+// Builds the sweep layout, the coefficient sources and the tile schedule of a factor
+// that detect_grid accepted.  Tile shape: lines per tile (nic warps each, at most
+// kGridMaxWarps warps per CTA) and planes per tile such that there are about as many
+// tiles as SMs; `elems`, `lines`, `planes` override (0 = automatic).
+static void build_grid_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, int nx, int ny, int nz,
+                            int elems, int lines, int planes, int sms, GridPack& G, cudaStream_t s) {
+    GridLayout& g = G.g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.E = elems > 0 ? elems : 1;
+    g.nic = ceil_div(nx, 32 * g.E);
+    g.len = (static_cast<long long>(ny) * g.nic * nz + 31) * 32 * g.E;
+    const int max_lines = std::max(1, kGridMaxWarps / g.nic);
+    G.jb = lines > 0 ? std::min(lines, max_lines) : std::min(ny, max_lines);
+    G.jb = std::max(1, std::min(G.jb, ny));
+    const int tj = ceil_div(ny, G.jb);
+    int tk = std::max(1, std::min(nz, (sms + tj / 2) / std::max(1, tj)));
+    G.kc = planes > 0 ? std::min(planes, nz) : ceil_div(nz, tk);
+    tk = ceil_div(nz, G.kc);
+    G.ntile = tj * tk;
+    G.threads = g.nic * G.jb * kWarp;
+    std::vector<long long> pos(static_cast<size_t>(n));
+    const long long len = g.len;
+    std::vector<int> lz(len, -1), ly(len, -1), lx(len, -1), uz(len, -1), uy(len, -1), ux(len, -1), ud(len, -1);
+    const int P = nx * ny;
+    for (int r = 0; r < n; ++r) {
+        const int i = r % nx, j = (r / nx) % ny, k = r / P;
+        const long long p = g.pos(i, j, k);
+        pos[static_cast<size_t>(r)] = p;
+        int t = rp[r];
+        if (k > 0) lz[p] = t++;
+        if (ny > 1 && j > 0) ly[p] = t++;
+        if (i > 0) lx[p] = t++;
+        t = diag[r];
+        ud[p] = t++;
+        if (i < nx - 1) ux[p] = t++;
+        if (ny > 1 && j < ny - 1) uy[p] = t++;
+        if (k < nz - 1) uz[p] = t++;
+    }
+    G.pos.upload(pos.data(), pos.size(), s);
+    G.src_lz.upload(lz.data(), lz.size(), s);
+    G.src_ly.upload(ly.data(), ly.size(), s);
+    G.src_lx.upload(lx.data(), lx.size(), s);
+    G.src_uz.upload(uz.data(), uz.size(), s);
+    G.src_uy.upload(uy.data(), uy.size(), s);
+    G.src_ux.upload(ux.data(), ux.size(), s);
+    G.src_ud.upload(ud.data(), ud.size(), s);
+    const std::vector<int2> tl = grid_tile_order(tj, tk, false), tu = grid_tile_order(tj, tk, true);
+    G.tiles_l.upload(tl.data(), tl.size(), s);
+    G.tiles_u.upload(tu.data(), tu.size(), s);
+    // host vectors must outlive the asynchronous copies
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));
+}
+
+template <class T>
+static size_t grid_smem_bytes(const GridPack& G) {
+    const size_t nw = static_cast<size_t>(G.threads / kWarp);
+    return nw * (static_cast<size_t>(kGridRingY) * 32 * G.g.E + kGridRingX) * sizeof(T) + nw * sizeof(int);
+}
+
+template <class T, bool UPPER>
+static auto grid_kernel_for(int E) {
+    switch (E) {
+        case 1: return sptrsv_grid_kernel<T, UPPER, 1>;
+        case 2: return sptrsv_grid_kernel<T, UPPER, 2>;
+        case 4: return sptrsv_grid_kernel<T, UPPER, 4>;
+        default: throw std::runtime_error("grid sweep: elements per lane must be 1, 2 or 4");
+    }
+}
+
+// Allocates the coefficient arrays and work vectors of value type T, raises the
+// kernels' shared-memory limit and sizes the grid; false when a CTA cannot be resident.
+template <class T>
+static bool configure_grid(GridPack& G, int sms, size_t smem_optin, cudaStream_t s) {
+    const size_t smem = grid_smem_bytes<T>(G);
+    if (smem > smem_optin) return false;
+    int per_sm = 0;
+    for (bool upper : {false, true}) {
+        auto kern = upper ? grid_kernel_for<T, true>(G.g.E) : grid_kernel_for<T, false>(G.g.E);
+        GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        int r = 0;
+        GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, G.threads, smem));
+        if (r < 1) return false;
+        per_sm = per_sm == 0 ? r : std::min(per_sm, r);
+    }
+    G.grid = std::min(G.ntile, per_sm * sms);
+    const size_t len = static_cast<size_t>(G.g.len);
+    if constexpr (sizeof(T) == 8) {
+        for (auto* b : {&G.lz64, &G.ly64, &G.lx64, &G.uz64, &G.uy64, &G.ux64, &G.ud64, &G.b64}) b->reserve(len);
+        G.y64.reserve(len);
+        G.z64.reserve(len);
+        fill_sentinel(G.y64.get(), static_cast<long long>(len), s, sms);
+        fill_sentinel(G.z64.get(), static_cast<long long>(len), s, sms);
+    } else {
+        for (auto* b : {&G.lz32, &G.ly32, &G.lx32, &G.uz32, &G.uy32, &G.ux32, &G.ud32, &G.b32}) b->reserve(len);
+        G.y32.reserve(len);
+        G.z32.reserve(len);
+        fill_sentinel(G.y32.get(), static_cast<long long>(len), s, sms);
+        fill_sentinel(G.z32.get(), static_cast<long long>(len), s, sms);
+    }
+    return true;
+}
+
+// Gathers the factor values into the coefficient arrays of type T.
+template <class T>
+static void gather_grid(GridPack& G, const double* lu, cudaStream_t s, int sms) {
+    const long long len = G.g.len;
+    const int threads = 256;
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(len, threads), 8LL * sms)));
+    const bool f64 = sizeof(T) == 8;
+    T* dst[7];
+    if constexpr (sizeof(T) == 8) {
+        T* d[7] = {G.lz64.get(), G.ly64.get(), G.lx64.get(), G.uz64.get(), G.uy64.get(), G.ux64.get(), G.ud64.get()};
+        std::copy(d, d + 7, dst);
+    } else {
+        T* d[7] = {G.lz32.get(), G.ly32.get(), G.lx32.get(), G.uz32.get(), G.uy32.get(), G.ux32.get(), G.ud32.get()};
+        std::copy(d, d + 7, dst);
+    }
+    const int* src[7] = {G.src_lz.get(), G.src_ly.get(), G.src_lx.get(), G.src_uz.get(),
+                         G.src_uy.get(), G.src_ux.get(), G.src_ud.get()};
+    for (int a = 0; a < 7; ++a)
+        grid_coef_kernel<T><<<grid, threads, 0, s>>>(len, src[a], lu, dst[a], a == 6 && !f64);
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+template <class T, bool UPPER>
+static void launch_grid(const GridPack& G, cudaStream_t s, const T* in, T* out, unsigned* counter, int* status,
+                        const int* gate, int step) {
+    auto kern = grid_kernel_for<T, UPPER>(G.g.E);
+    kern<<<G.grid, G.threads, grid_smem_bytes<T>(G), s>>>(G.view<T>(UPPER), in, out, counter, status, gate, step);
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+template <class T>
+static void launch_grid_gather(const GridPack& G, int n, cudaStream_t s, T* in, const double* scale, T* lay, T* reset,
+                               const int* gate, int step, int sms) {
+    const int threads = 256;
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(n, threads), 8LL * sms)));
+    grid_gather_kernel<T><<<grid, threads, 0, s>>>(n, G.pos.get(), in, scale, lay, reset, gate, step);
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+template <class T>
+static void launch_grid_scatter(const GridPack& G, int n, cudaStream_t s, T* lay, T* out, const int* gate, int step,
+                                int sms) {
+    const int threads = 256;
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(n, threads), 8LL * sms)));
+    grid_scatter_kernel<T><<<grid, threads, 0, s>>>(n, G.pos.get(), lay, out, gate, step);
+    GB_CUDA_CHECK(cudaGetLastError());
+}
+
+
 }  // namespace gb300
 
 namespace lljbash {
@@ -639,6 +857,15 @@ IluSolver::Impl::~Impl() {
 
 template <class T>
 void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const {
+    if (sizeof(T) == 8 ? grid64 : grid32) {
+        // b (natural order, rescaled in place) -> layout; the forward sweep's layout output
+        // reset to the sentinel in the same pass; `y` is not used
+        T* lb = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.b64.get()) : reinterpret_cast<T*>(GP.b32.get());
+        T* ly = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.y64.get()) : reinterpret_cast<T*>(GP.y32.get());
+        launch_grid_gather<T>(GP, n, s, b, scale, lb, ly, gate, step, dev.sms);
+        launch_grid<T, false>(GP, s, lb, ly, counters.get() + 1, status.get(), gate, step);
+        return;
+    }
     if (sizeof(T) == 8 ? blk64 : blk32) {
         launch_block<T, false>(sizeof(T) == 8 ? LB64 : LB32, s, b, scale, y, counters.get() + 1, status.get(), gate,
                                step);
@@ -650,6 +877,15 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
 
 template <class T>
 void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const {
+    if (sizeof(T) == 8 ? grid64 : grid32) {
+        // layout output of the forward sweep -> backward sweep -> x (natural order); the
+        // layout output is reset to the sentinel by the scatter; `y` is not used
+        T* ly = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.y64.get()) : reinterpret_cast<T*>(GP.y32.get());
+        T* lz = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.z64.get()) : reinterpret_cast<T*>(GP.z32.get());
+        launch_grid<T, true>(GP, s, ly, lz, counters.get() + 2, status.get(), gate, step);
+        launch_grid_scatter<T>(GP, n, s, lz, x, gate, step, dev.sms);
+        return;
+    }
     if (sizeof(T) == 8 ? blk64 : blk32) {
         launch_block<T, true>(sizeof(T) == 8 ? UB64 : UB32, s, y, nullptr, x, counters.get() + 2, status.get(), gate,
                               step);
@@ -661,6 +897,8 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
 
 template <class T>
 const void* IluSolver::Impl::subst_key() const {
+    if (sizeof(T) == 8 ? grid64 : grid32)
+        return sizeof(T) == 8 ? static_cast<const void*>(GP.lz64.get()) : static_cast<const void*>(GP.lz32.get());
     if (sizeof(T) == 8 ? blk64 : blk32) return (sizeof(T) == 8 ? LB64 : LB32).codes.get();
     return L.cols.get();
 }
@@ -797,6 +1035,18 @@ void IluSolver::SetupMatrix() {
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, row_lanes_for(kl, im.row_lanes), im.L, s);
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, row_lanes_for(ku, im.row_lanes), im.U, s);
     }
+    // structured-grid sweeps: 7- / 5-point stencil factors in natural order
+    im.grid64 = im.grid32 = false;
+    if (im.grid_mode >= 0) {
+        int gx = 0, gy = 0, gz = 0;
+        if (detect_grid(n, rp, ci, im.an.diag, gx, gy, gz)) {
+            build_grid_pack(n, rp, ci, im.an.diag, gx, gy, gz, im.grid_elems, im.grid_lines, im.grid_planes,
+                            im.dev.sms, im.GP, s);
+            const size_t optin = static_cast<size_t>(im.dev.smem_optin);
+            im.grid64 = configure_grid<double>(im.GP, im.dev.sms, optin, s);
+            im.grid32 = configure_grid<float>(im.GP, im.dev.sms, optin, s);
+        }
+    }
     const size_t nv = static_cast<size_t>(std::max(n, 1));
     im.sb64.reserve(nv);
     im.sy64.reserve(nv);
@@ -913,6 +1163,14 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
                 gather_level_pack(im.L, true, im.lu.get(), s, im.dev.sms);
                 gather_level_pack(im.U, false, im.lu.get(), s, im.dev.sms);
                 im.launches += 6;
+            }
+            if (im.grid64) {
+                gather_grid<double>(im.GP, im.lu.get(), s, im.dev.sms);
+                im.launches += 7;
+            }
+            if (im.grid32) {
+                gather_grid<float>(im.GP, im.lu.get(), s, im.dev.sms);
+                im.launches += 7;
             }
         }
         GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));

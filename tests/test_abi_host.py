@@ -202,5 +202,20 @@ def test_ilu_option_values_checked():
         ilu.set_option(api.ILU_OPT_BLOCK_ROWS, v)
     with pytest.raises(RuntimeError):
         ilu.set_option(api.ILU_OPT_BLOCK_ROWS, -2)
+    for v in (-1, 0, 1):
+        ilu.set_option(api.ILU_OPT_GRID, v)
+    for v in (2, -2, 0.5):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_GRID, v)
+    for v in (0, 1, 2, 4):
+        ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, v)
+    for v in (3, 8, -1):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, v)
+    for opt in (api.ILU_OPT_GRID_TILE_LINES, api.ILU_OPT_GRID_TILE_PLANES):
+        ilu.set_option(opt, 0)
+        ilu.set_option(opt, 7)
+        with pytest.raises(RuntimeError):
+            ilu.set_option(opt, -3)
     with pytest.raises(RuntimeError):
         ilu.set_option(12345, 1)

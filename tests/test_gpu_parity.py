@@ -238,6 +238,7 @@ def test_block_partition_does_not_change_results(golden, block_rows):
     ref = factorize(golden.f_csr())
     x_ref = ref.substitute(golden.b)
     ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_GRID, -1)  # the block-local kernel, also on stencil matrices
     ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
     ilu.set_matrix(golden.f_csr())
     assert ilu.setup() == 0
@@ -350,6 +351,7 @@ def test_cluster_halos_two_positions_back(planes):
 
     def run(block_rows):
         ilu = api.IluSolver()
+        ilu.set_option(api.ILU_OPT_GRID, -1)  # block-local / level-ordered kernels
         ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
         ilu.set_matrix(f)
         assert ilu.setup() == 0, api.last_error()

@@ -1,0 +1,125 @@
+"""Structured-grid sweeps (LLJBASH_ILU_OPT_GRID): the wavefront-lanes kernels for 7-point
+(3-D) and 5-point (2-D) factors in natural order.
+
+Every row performs the reference's operations in the reference's order, so the grid
+schedule must give results bit-identical to the block-local and level-ordered kernels
+(FP64 substitution, and the FP32 path through identical mixed-precision GMRES runs), and
+1e-12 against the CPU oracle.  Covered: grid shapes whose x extent is and is not a
+multiple of 32, 2-D grids (one line per plane), several lane widths (elements per lane)
+and tile shapes (lines and planes per tile, down to one), and matrices the detection
+must reject (27-point stencils, ILU(1) fill, a permuted 7-point matrix)."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+from par_ilu0_cpp_gb300 import api
+from par_ilu0_cpp_gb300 import generators as g
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def port():
+    oracle.build_port()
+    return oracle.Port()
+
+
+def solver(f, grid=0, elems=0, lines=0, planes=0, block_rows=0):
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_GRID, grid)
+    ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, elems)
+    ilu.set_option(api.ILU_OPT_GRID_TILE_LINES, lines)
+    ilu.set_option(api.ILU_OPT_GRID_TILE_PLANES, planes)
+    ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    return ilu
+
+
+SHAPES = [
+    ("convdiff3d_32", lambda: g.convdiff3d(32)),
+    ("convdiff3d_20x7x9", lambda: g.convdiff3d(20, 7, 9)),
+    ("convdiff3d_70x5x6", lambda: g.convdiff3d(70, 5, 6)),
+    ("convdiff3d_128x3x4", lambda: g.convdiff3d(128, 3, 4)),
+    ("laplace2d_64", lambda: g.laplace2d(64)),
+    ("laplace2d_45x80", lambda: g.laplace2d(45, 80)),
+    ("laplace2d_256", lambda: g.laplace2d(256)),
+]
+
+
+@pytest.mark.parametrize("name,make", SHAPES, ids=[c[0] for c in SHAPES])
+def test_grid_sweep_matches_other_schedules_and_oracle(port, name, make):
+    a = make()
+    f, _ = api.iluk_symbolic(a, 0)
+    ilu = solver(f)
+    info = ilu.info()
+    assert info.grid_fp64 == 1 and info.grid_fp32 == 1, name
+    lu_ref, _ = port.factorize(f)
+    assert rel_err(ilu.values(), lu_ref, floor=1e-300) <= 1e-12
+    _, b = g.random_rhs(a, seed=3)
+    x = ilu.substitute(b)
+    assert rel_err(x, port.substitute(f, lu_ref, b)) <= 1e-12
+    for kw in ({"grid": -1, "block_rows": -1}, {"grid": -1, "block_rows": 0}):
+        other = solver(f, **kw)
+        assert other.info().grid_fp64 == 0
+        assert np.array_equal(other.substitute(b), x), kw
+    assert np.array_equal(ilu.substitute(b), x)  # the layout buffers are back at the sentinel
+
+
+TUNINGS = [dict(elems=1, lines=1, planes=1), dict(elems=1, lines=3, planes=5), dict(elems=2),
+           dict(elems=4, lines=2, planes=3), dict(elems=4), dict(elems=1, lines=8, planes=64)]
+
+
+@pytest.mark.parametrize("kw", TUNINGS, ids=[str(k) for k in TUNINGS])
+@pytest.mark.parametrize("make", [lambda: g.convdiff3d(40, 9, 11), lambda: g.laplace2d(100, 37)],
+                         ids=["convdiff3d_40x9x11", "laplace2d_100x37"])
+def test_grid_tile_shapes_and_lane_widths(make, kw):
+    a = make()
+    f, _ = api.iluk_symbolic(a, 0)
+    ref = solver(f, grid=-1, block_rows=-1)
+    ilu = solver(f, **kw)
+    assert ilu.info().grid_fp64 == 1
+    _, b = g.random_rhs(a, seed=5)
+    assert np.array_equal(ilu.substitute(b), ref.substitute(b))
+
+
+@pytest.mark.parametrize("make", [lambda: g.convdiff3d(48), lambda: g.laplace2d(160)],
+                         ids=["convdiff3d_48", "laplace2d_160"])
+def test_grid_gmres_identical_to_block_schedule(make):
+    """Plain FP64 and mixed-precision GMRES with the grid sweeps take the same iterations
+    and return the same solution as with the block-local / level-ordered sweeps."""
+    a = make()
+    f, _ = api.iluk_symbolic(a, 0)
+    _, b = g.random_rhs(a, seed=7)
+    tol = 1e-8 * float(np.linalg.norm(b))
+    out = {}
+    for grid in (0, -1):
+        ilu = solver(f, grid=grid)
+        for mode in (0, 1):
+            gm = api.Gmres(tol, 40, 1000)
+            gm.set_preconditioner(ilu)
+            gm.set_option(api.GMRES_OPT_MODE, mode)
+            res = gm.solve(a, b)
+            assert res.ok
+            out[(grid, mode)] = (res.iterations, res.x)
+    for mode in (0, 1):
+        assert out[(0, mode)][0] == out[(-1, mode)][0]
+        assert np.array_equal(out[(0, mode)][1], out[(-1, mode)][1])
+
+
+def test_grid_detection_rejects_other_patterns():
+    permuted = g.convdiff3d(12)
+    n = permuted.n
+    perm = np.random.default_rng(0).permutation(n)
+    sp = permuted.to_scipy()[perm][:, perm].tocsr()
+    sp.sort_indices()
+    cases = {
+        "lognormal27": api.iluk_symbolic(g.lognormal27(8, seed=1), 0)[0],
+        "convdiff3d_ilu1": api.iluk_symbolic(g.convdiff3d(12), 1)[0],
+        "permuted": g.Csr(n, sp.indptr, sp.indices, sp.data),
+    }
+    for name, f in cases.items():
+        ilu = solver(f)
+        assert ilu.info().grid_fp64 == 0, name
