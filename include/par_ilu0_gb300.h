@@ -92,7 +92,8 @@ enum {
      * factors that are a full 7-point (3-D) or 5-point (2-D) stencil in natural order, the
      * triangular sweeps run on a fixed wavefront schedule (a lane walks a grid line in
      * registers, neighbours arrive by warp shuffles and shared memory), taking precedence
-     * over LLJBASH_ILU_OPT_BLOCK_ROWS.  0 (default): on when the pattern qualifies;
+     * over LLJBASH_ILU_OPT_BLOCK_ROWS.  1: on when the pattern qualifies; 0 (default,
+     * automatic): off, the block-local kernels being faster on the grids measured;
      * -1: off.  Takes effect at the next IluSolverSetup. */
     LLJBASH_ILU_OPT_GRID = 6,
     /* tuning of the structured-grid sweeps (0 = automatic), next IluSolverSetup:

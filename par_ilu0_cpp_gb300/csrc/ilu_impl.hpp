@@ -178,7 +178,7 @@ struct IluSolver::Impl {
     // 5-point stencil in natural order and grid_mode allows it
     gb300::GridPack GP;
     bool grid64 = false, grid32 = false;
-    int grid_mode = 0;       // 0 automatic, 1 force (when structured), -1 off
+    int grid_mode = 0;       // 1: on when the pattern qualifies; 0 (automatic) and -1: off
     int grid_elems = 0;      // requested elements per lane (0 automatic: 1)
     int grid_lines = 0;      // requested lines per tile (0 automatic)
     int grid_planes = 0;     // requested planes per tile (0 automatic)

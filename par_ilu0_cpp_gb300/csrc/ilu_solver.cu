@@ -1037,7 +1037,9 @@ void IluSolver::SetupMatrix() {
     }
     // structured-grid sweeps: 7- / 5-point stencil factors in natural order
     im.grid64 = im.grid32 = false;
-    if (im.grid_mode >= 0) {
+    // (automatic = off: on GB300 the block-local / cluster kernels measure faster on the
+    // stencil grids tried so far; the grid schedule runs when requested)
+    if (im.grid_mode > 0) {
         int gx = 0, gy = 0, gz = 0;
         if (detect_grid(n, rp, ci, im.an.diag, gx, gy, gz)) {
             build_grid_pack(n, rp, ci, im.an.diag, gx, gy, gz, im.grid_elems, im.grid_lines, im.grid_planes,

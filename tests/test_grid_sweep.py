@@ -1,4 +1,4 @@
-"""Structured-grid sweeps (LLJBASH_ILU_OPT_GRID): the wavefront-lanes kernels for 7-point
+"""Structured-grid sweeps (LLJBASH_ILU_OPT_GRID = 1): the wavefront-lanes kernels for 7-point
 (3-D) and 5-point (2-D) factors in natural order.
 
 Every row performs the reference's operations in the reference's order, so the grid
@@ -25,7 +25,7 @@ def port():
     return oracle.Port()
 
 
-def solver(f, grid=0, elems=0, lines=0, planes=0, block_rows=0):
+def solver(f, grid=1, elems=0, lines=0, planes=0, block_rows=0):
     ilu = api.IluSolver()
     ilu.set_option(api.ILU_OPT_GRID, grid)
     ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, elems)
@@ -61,7 +61,7 @@ def test_grid_sweep_matches_other_schedules_and_oracle(port, name, make):
     _, b = g.random_rhs(a, seed=3)
     x = ilu.substitute(b)
     assert rel_err(x, port.substitute(f, lu_ref, b)) <= 1e-12
-    for kw in ({"grid": -1, "block_rows": -1}, {"grid": -1, "block_rows": 0}):
+    for kw in ({"grid": -1, "block_rows": -1}, {"grid": 0, "block_rows": 0}):
         other = solver(f, **kw)
         assert other.info().grid_fp64 == 0
         assert np.array_equal(other.substitute(b), x), kw
@@ -95,7 +95,7 @@ def test_grid_gmres_identical_to_block_schedule(make):
     _, b = g.random_rhs(a, seed=7)
     tol = 1e-8 * float(np.linalg.norm(b))
     out = {}
-    for grid in (0, -1):
+    for grid in (1, -1):
         ilu = solver(f, grid=grid)
         for mode in (0, 1):
             gm = api.Gmres(tol, 40, 1000)
@@ -105,8 +105,8 @@ def test_grid_gmres_identical_to_block_schedule(make):
             assert res.ok
             out[(grid, mode)] = (res.iterations, res.x)
     for mode in (0, 1):
-        assert out[(0, mode)][0] == out[(-1, mode)][0]
-        assert np.array_equal(out[(0, mode)][1], out[(-1, mode)][1])
+        assert out[(1, mode)][0] == out[(-1, mode)][0]
+        assert np.array_equal(out[(1, mode)][1], out[(-1, mode)][1])
 
 
 def test_grid_detection_rejects_other_patterns():
