@@ -53,6 +53,16 @@ def build_port() -> str:
     return PORT_SO
 
 
+def reference_file(rel: str) -> str | None:
+    """Path of a reference source file (e.g. "test/test.c") in the checkout, else in the
+    copy staged by build_ref.sh; None when neither has it."""
+    for base in (reference_dir(), REF_STAGE):
+        path = os.path.join(base, rel)
+        if os.path.isfile(path):
+            return path
+    return None
+
+
 def build_ref(ref_dir: str | None = None) -> str | None:
     """Builds oracle/_ref from the reference checkout, or from the staged copy in
     oracle/_ref/src where the checkout is absent; None when neither exists."""

@@ -14,7 +14,9 @@
 #
 # REFERENCE_DIR defaults to $PAR_ILU0_REFERENCE_DIR, else /root/reference.  When the
 # checkout is there, the sources are compiled where they lie and the files this build
-# reads are also staged under oracle/_ref/src, so that a machine the working tree is
+# reads (and the reference's C test programs test/test.c, test/amd_test.c, which the
+# tests compile unchanged against this library's headers) are also staged under
+# oracle/_ref/src, so that a machine the working tree is
 # copied to without the checkout can rebuild from the staged copy (the only other
 # source this script accepts).  Nothing is copied into tracked files.
 set -euo pipefail
@@ -27,6 +29,8 @@ if [ -f "$REF/src/ilu_solver.cpp" ]; then
     rm -rf "$STAGE.tmp"
     mkdir -p "$STAGE.tmp"
     cp -r "$REF/src" "$REF/include" "$REF/include_c" "$REF/src_c" "$STAGE.tmp/"
+    mkdir -p "$STAGE.tmp/test"
+    cp "$REF/test/test.c" "$REF/test/amd_test.c" "$STAGE.tmp/test/"
     rm -rf "$STAGE"
     mv "$STAGE.tmp" "$STAGE"
 elif [ -f "$STAGE/src/ilu_solver.cpp" ]; then

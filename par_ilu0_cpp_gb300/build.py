@@ -6,6 +6,8 @@ Produces, under par_ilu0_cpp_gb300/lib/:
   the CsrMatrix utilities, IlukSymbolic and all CUDA kernels.
 * ``libpar-ilu0-gmres_c.so`` — the LLJBASH_* C ABI (include/ilu_solver_c.h, gmres_c.h,
   par_ilu0_gb300.h) on top of it.
+* ``par-ilu0-benchmark`` — the command-line benchmark (the reference's test/benchmark.cpp
+  options), over both libraries.
 
 These are the two libraries the reference builds (src/CMakeLists.txt:11,
 src_c/CMakeLists.txt:2), with the same names.  Translation units compile in parallel;
@@ -30,6 +32,7 @@ LIB = os.path.join(PKG, "lib")
 
 CORE_LIB = "libpar-ilu0-gmres.so"
 C_LIB = "libpar-ilu0-gmres_c.so"
+BENCH_EXE = "par-ilu0-benchmark"  # the command-line benchmark (csrc/benchmark_main.cpp)
 
 CORE_SOURCES = ["host_csr.cpp", "ilu_solver.cu", "gmres.cu", "mlp.cu", "batched.cu"]
 C_SOURCES = ["c_api.cu"]
@@ -96,6 +99,15 @@ def build(debug: bool = False, verbose: bool = False) -> str:
         os.replace(tmp, out)
         if verbose:
             print("built", out, file=sys.stderr)
+    # the command-line benchmark: host C++ over both libraries
+    exe = os.path.join(LIB, BENCH_EXE)
+    cxx = shutil.which(os.environ.get("CXX", "g++")) or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-I" + INCLUDE, os.path.join(CSRC, "benchmark_main.cpp"), "-o", exe + ".tmp",
+           "-L" + LIB, "-l:" + C_LIB, "-l:" + CORE_LIB, "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"build failed for {BENCH_EXE}:\n{res.stdout}\n{res.stderr}")
+    os.replace(exe + ".tmp", exe)
     return LIB
 
 
