@@ -100,7 +100,13 @@ enum {
      * elements per lane along x (1, 2, 4), grid lines per tile, grid planes per tile. */
     LLJBASH_ILU_OPT_GRID_LANE_ELEMS = 7,
     LLJBASH_ILU_OPT_GRID_TILE_LINES = 8,
-    LLJBASH_ILU_OPT_GRID_TILE_PLANES = 9
+    LLJBASH_ILU_OPT_GRID_TILE_PLANES = 9,
+    /* order in which the factorisation kernel's warps take rows (results are the same
+     * for every order): 0 (default) level order (the reference's Levelization); 1 the
+     * reference's subtree scheduler (src/subtree.hpp tree_schedule, one worker per SM):
+     * the workers' independent subtrees interleaved row by row, then the remaining
+     * (separator) rows in elimination-tree post order.  Next IluSolverSetup. */
+    LLJBASH_ILU_OPT_TICKET_ORDER = 11
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 
@@ -180,6 +186,18 @@ int LLJBASH_IluSolverGetAnalysis(IluSolverHdl hdl, int* diag, int* etree_lower, 
  * no device.  Returns -2 when a row has no diagonal entry. */
 int LLJBASH_Gb300AnalyzePattern(int n, const int* row_ptr, const int* col_idx, int* diag, int* etree_lower,
                                 int* etree_upper, int* depth_lower, int* depth_upper, int* nlevels /* [2] */);
+
+/* The reference's subtree scheduler (src/subtree.hpp:103-475 tree_schedule, no row
+ * stripping), restated on the host with identical integer output, for the L-DAG
+ * (upper = 0; row weights diag - row_ptr + 1, as the reference's factorisation and forward
+ * substitution) or the reverse U-DAG (upper = 1; weights row_ptr[v+1] - diag[v]).
+ * Outputs (any may be NULL): part_ptr[nproc + 2], partitions[n] (workers' subtree rows,
+ * then the queue rows), task_queue[*ntasks + 1] (granularity > 1: queue tasks in
+ * priority order; at most n + 1 entries), the elimination-tree subtree sizes and
+ * weights [n + 1] (index n: the virtual root).  Host only; touches no device. */
+int LLJBASH_Gb300TreeSchedule(int n, const int* row_ptr, const int* col_idx, int upper, int nproc, int granularity,
+                              double relax, int* part_ptr, int* partitions, int* task_queue, int* ntasks,
+                              int* subtree_size, int* subtree_weight);
 
 /* Batched persistent solver (no counterpart in the reference): nsys independent
  * systems of uneven size, nrhs right-hand sides each, solved in ONE persistent kernel

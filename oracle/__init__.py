@@ -237,6 +237,23 @@ class Ref(_Lib):
                                     int(nthreads), ctypes.byref(its), _dp(times), _dp(stat))
         return dict(ok=bool(ok), iters=int(its.value), x=x, times=times, stat=stat)
 
+    def tree_schedule(self, a, upper, nproc, granularity=1, relax=1.0):
+        """The reference's tree_schedule on a's pattern (see ref_driver.cpp)."""
+        n = a.n
+        rp, ci = _i32(a.row_ptr), _i32(a.col_idx)
+        d = self.diag_ptr(a)
+        out = {"part_ptr": np.zeros(nproc + 2, dtype=np.int32), "partitions": np.zeros(n, dtype=np.int32),
+               "task_queue": np.zeros(n + 1, dtype=np.int32), "subtree_size": np.zeros(n + 1, dtype=np.int32),
+               "subtree_weight": np.zeros(n + 1, dtype=np.int32)}
+        f = self.lib.ref_tree_schedule
+        f.restype = ctypes.c_int
+        with c_stdout_to_stderr():
+            nt = f(n, _ip(rp), _ip(ci), _ip(d), int(not upper), int(nproc), int(granularity), ctypes.c_double(relax),
+                   _ip(out["part_ptr"]), _ip(out["partitions"]), _ip(out["task_queue"]), _ip(out["subtree_size"]),
+                   _ip(out["subtree_weight"]))
+        out["task_queue"] = out["task_queue"][: nt + 1] if nt else out["task_queue"][:0]
+        return out
+
     def session(self, a, lof, tol, restart, maxit, nthreads):
         """The test/benchmark.cpp repetition loop: symbolic + first setup now, then
         RefSession.step() = one repetition (Factorize + GMRES timed)."""

@@ -288,4 +288,63 @@ void ref_session_destroy(void* hdl) {
     delete s;
 }
 
+/* ---- subtree scheduler (src/subtree.hpp tree_schedule) ------------------------------
+ * The reference's tree_schedule on the L-DAG (lower != 0, load weights diag - row_ptr + 1
+ * as its factorisation / forward substitution) or the reverse U-DAG (weights
+ * row_ptr[v+1] - diag[v], as its backward substitution), no row stripping.  Outputs
+ * part_ptr[nproc + 2], partitions[n], task_queue[ntasks + 1] (granularity > 1) and the
+ * subtree sizes / weights [n + 1] from its own init_subtree.  Returns ntasks. */
+struct RefNnzBalancer {
+    using weight_t = int;
+    const int* begin;
+    const int* end;
+    int base;
+    int granu;
+    weight_t weight_in_subtree(int i) const { return end[i] - begin[i] + base; }
+    weight_t weight_in_queue(int i) const { return end[i] - begin[i] + base; }
+    int queue_granularity() const { return granu; }
+};
+
+int ref_tree_schedule(int n, const int* rp, const int* ci, const int* diag, int lower, int nproc, int granularity,
+                      double relax, int* part_ptr, int* partitions, int* task_queue, int* subtree_size,
+                      int* subtree_weight) {
+    int* tq = nullptr;
+    int ntasks = 0;
+    if (lower) {
+        RefNnzBalancer lb{rp, diag, 1, granularity};
+        ntasks = tree_schedule(nproc, 0, n, 1, ConstBiasArray<int>(const_cast<int*>(rp)), diag, ci, part_ptr, partitions,
+                               tq, lb, relax, -1.0);
+    } else {
+        RefNnzBalancer lb{diag, rp + 1, 0, granularity};
+        ntasks = tree_schedule(nproc, n - 1, -1, -1, ConstBiasArray<int>(const_cast<int*>(diag), 1), rp + 1, ci, part_ptr,
+                               partitions, tq, lb, relax, -1.0);
+    }
+    if (tq != nullptr) {
+        if (task_queue) std::copy_n(tq, ntasks + 1, task_queue);
+        delete[] tq;
+    }
+    // subtree sizes and weights exactly as partition_subtree computes them
+    std::vector<int> stripped(static_cast<size_t>(n), 0), parent(static_cast<size_t>(n)), root(static_cast<size_t>(n) + 1);
+    std::vector<int> size(static_cast<size_t>(n) + 1), weight(static_cast<size_t>(n) + 1);
+    const int vb = lower ? 0 : n - 1, ve = lower ? n : -1, vd = lower ? 1 : -1;
+    if (lower) {
+        build_etree_parent(n, vb, ve, vd, ConstBiasArray<int>(const_cast<int*>(rp)), diag, ci, stripped.data(),
+                           parent.data(), root.data());
+    } else {
+        build_etree_parent(n, vb, ve, vd, ConstBiasArray<int>(const_cast<int*>(diag), 1), rp + 1, ci, stripped.data(),
+                           parent.data(), root.data());
+    }
+    RefNnzBalancer lb = lower ? RefNnzBalancer{rp, diag, 1, granularity} : RefNnzBalancer{diag, rp + 1, 0, granularity};
+    for (int v = vb; v != ve; v += vd) {
+        weight[static_cast<size_t>(v)] = lb.weight_in_subtree(v);
+        size[static_cast<size_t>(v)] = 1;
+    }
+    weight[static_cast<size_t>(n)] = 0;
+    size[static_cast<size_t>(n)] = 0;
+    init_subtree(vb, ve, vd, stripped.data(), parent.data(), size.data(), weight.data());
+    if (subtree_size) std::copy(size.begin(), size.end(), subtree_size);
+    if (subtree_weight) std::copy(weight.begin(), weight.end(), subtree_weight);
+    return ntasks;
+}
+
 }  // extern "C"

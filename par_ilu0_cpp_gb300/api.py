@@ -71,6 +71,7 @@ ILU_OPT_GRID = 6
 ILU_OPT_GRID_LANE_ELEMS = 7
 ILU_OPT_GRID_TILE_LINES = 8
 ILU_OPT_GRID_TILE_PLANES = 9
+ILU_OPT_TICKET_ORDER = 11
 GMRES_OPT_MODE = 1
 GMRES_OPT_TAU = 2
 GMRES_OPT_USE_GRAPH = 3
@@ -127,6 +128,8 @@ def load() -> ctypes.CDLL:
         "LLJBASH_IluSolverGetInfo": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(IluInfo)]),
         "LLJBASH_IluSolverGetAnalysis": (ctypes.c_int, [ctypes.c_void_p, _I, _I, _I, _I, _I]),
         "LLJBASH_Gb300AnalyzePattern": (ctypes.c_int, [ctypes.c_int, _I, _I, _I, _I, _I, _I, _I, _I]),
+        "LLJBASH_Gb300TreeSchedule": (ctypes.c_int, [ctypes.c_int, _I, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_double, _I, _I, _I, _I, _I, _I]),
         "LLJBASH_GmresSetOption": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
         "LLJBASH_GmresGetReport": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GmresReport)]),
         "LLJBASH_GmresGetKernelTimes": (ctypes.c_int, [ctypes.c_void_p, _D, ctypes.POINTER(ctypes.c_longlong),
@@ -278,6 +281,25 @@ def analyze_pattern(a: Csr):
         raise RuntimeError(f"analysis failed ({rc}): {last_error()}")
     outs["nlev"] = nlev
     return outs
+
+
+def tree_schedule(a: Csr, upper: bool, nproc: int, granularity: int = 1, relax: float = 1.0):
+    """The reference's subtree scheduler on a's pattern: dict(part_ptr, partitions,
+    task_queue, subtree_size, subtree_weight)."""
+    lib = load()
+    n = a.n
+    out = {"part_ptr": np.zeros(nproc + 2, dtype=np.int32), "partitions": np.zeros(n, dtype=np.int32),
+           "task_queue": np.zeros(n + 1, dtype=np.int32), "subtree_size": np.zeros(n + 1, dtype=np.int32),
+           "subtree_weight": np.zeros(n + 1, dtype=np.int32)}
+    nt = ctypes.c_int(0)
+    rc = lib.LLJBASH_Gb300TreeSchedule(n, _ip(_i32(a.row_ptr)), _ip(_i32(a.col_idx)), int(upper), int(nproc),
+                                       int(granularity), float(relax), _ip(out["part_ptr"]), _ip(out["partitions"]),
+                                       _ip(out["task_queue"]), ctypes.byref(nt), _ip(out["subtree_size"]),
+                                       _ip(out["subtree_weight"]))
+    if rc != 0:
+        raise RuntimeError(f"tree schedule failed ({rc}): {last_error()}")
+    out["task_queue"] = out["task_queue"][: nt.value + 1] if nt.value else out["task_queue"][:0]
+    return out
 
 
 class IluSolver:

@@ -4,8 +4,10 @@
 #include <cstring>
 #include <exception>
 #include <string>
+#include <vector>
 
 #include "analysis.hpp"
+#include "tree_schedule.hpp"
 #include "batched_impl.hpp"
 #include "gmres.hpp"
 #include "gmres_c.h"
@@ -156,6 +158,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
             case LLJBASH_ILU_OPT_BLOCK_ROWS:
                 if (value < -1 || value > 1e8) throw std::runtime_error("block rows must be -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);
+                return 0;
+            case LLJBASH_ILU_OPT_TICKET_ORDER:
+                if (value != 0 && value != 1) throw std::runtime_error("ticket order must be 0 or 1");
+                s->impl()->ticket_order = static_cast<int>(value);
                 return 0;
             case LLJBASH_ILU_OPT_GRID:
                 if (value != -1 && value != 0 && value != 1) throw std::runtime_error("grid sweeps must be -1, 0 or 1");
@@ -351,6 +357,33 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
         info->grid_tile_lines = im->GP.jb;
         info->grid_tile_planes = im->GP.kc;
         info->grid_tiles = im->GP.ntile;
+    }
+    return 0;
+}
+
+int LLJBASH_Gb300TreeSchedule(int n, const int* row_ptr, const int* col_idx, int upper, int nproc, int granularity,
+                              double relax, int* part_ptr, int* partitions, int* task_queue, int* ntasks,
+                              int* subtree_size, int* subtree_weight) {
+    try {
+        gb300::validate_csr(n, row_ptr, col_idx, "pattern");
+        if (granularity < 1) throw std::runtime_error("tree schedule granularity must be at least 1");
+        std::vector<int> diag;
+        gb300::diagonal_pointers(n, row_ptr, col_idx, diag);
+        const gb300::DagView g{row_ptr, col_idx, diag.data(), upper == 0};
+        const gb300::RowWeights w = upper ? gb300::RowWeights{diag.data(), row_ptr + 1, 0, 0}
+                                          : gb300::RowWeights{row_ptr, diag.data(), 0, 1};
+        const gb300::TreeScheduleResult r = gb300::tree_schedule(n, g, nproc, granularity, relax, w);
+        auto put = [](int* dst, const std::vector<int>& v) {
+            if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(int));
+        };
+        put(part_ptr, r.part_ptr);
+        put(partitions, r.partitions);
+        put(task_queue, r.task_queue);
+        put(subtree_size, r.subtree_size);
+        put(subtree_weight, r.subtree_weight);
+        if (ntasks) *ntasks = r.ntasks;
+    } catch (const std::exception& e) {
+        return fail(e);
     }
     return 0;
 }

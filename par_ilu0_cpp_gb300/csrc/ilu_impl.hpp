@@ -164,6 +164,8 @@ struct IluSolver::Impl {
     gb300::Analysis an;
 
     gb300::DeviceBuffer<int> rp, ci, diag, order_l;
+    gb300::DeviceBuffer<int> order_fact;  // ticket order of the factorisation (ticket_order = 1)
+    int ticket_order = 0;  // factorisation tickets: 0 level order, 1 the subtree scheduler's order
     gb300::DeviceBuffer<double> lu;
     gb300::DeviceBuffer<double> shift;      // per-row diagonal shift (learned), optional
     gb300::DeviceBuffer<int> done;          // per-row ready stamps of the factorisation

@@ -20,6 +20,7 @@
 #include "ilu_impl.hpp"
 #include "ilu_kernels.cuh"
 #include "mlp.cuh"
+#include "tree_schedule.hpp"
 
 namespace gb300 {
 
@@ -970,6 +971,27 @@ void IluSolver::SetupMatrix() {
     im.ci.upload(ci, static_cast<size_t>(im.nnz), s);
     im.diag.upload(im.an.diag.data(), static_cast<size_t>(n), s);
     im.order_l.upload(im.an.order_l.data(), static_cast<size_t>(n), s);
+    if (im.ticket_order == 1 && n > 0) {
+        // the reference's subtree schedule (one worker per SM): the workers' subtree rows
+        // interleaved round-robin (rows of different subtrees are independent), then the
+        // queue rows; a topological order, as every ticket order must be
+        const TreeScheduleResult ts =
+            tree_schedule(n, gl, std::max(1, im.dev.sms), 1, 1.0, RowWeights{rp, im.an.diag.data(), 0, 1});
+        std::vector<int> ord;
+        ord.reserve(static_cast<size_t>(n));
+        const int np = ts.nproc;
+        int longest = 0;
+        for (int w = 0; w < np; ++w)
+            longest = std::max(longest, ts.part_ptr[static_cast<size_t>(w) + 1] - ts.part_ptr[static_cast<size_t>(w)]);
+        for (int i = 0; i < longest; ++i)
+            for (int w = 0; w < np; ++w)
+                if (ts.part_ptr[static_cast<size_t>(w)] + i < ts.part_ptr[static_cast<size_t>(w) + 1])
+                    ord.push_back(ts.partitions[static_cast<size_t>(ts.part_ptr[static_cast<size_t>(w)] + i)]);
+        for (int k = ts.part_ptr[static_cast<size_t>(np)]; k < n; ++k) ord.push_back(ts.partitions[static_cast<size_t>(k)]);
+        if (static_cast<int>(ord.size()) != n) throw std::runtime_error("tree schedule order is not a permutation");
+        im.order_fact.upload(ord.data(), ord.size(), s);
+        GB_CUDA_CHECK(cudaStreamSynchronize(s));  // ord must outlive the copy
+    }
     im.depth_l.upload(im.an.depth_l.data(), static_cast<size_t>(n), s);
     im.shift.reserve(static_cast<size_t>(std::max(n, 1)));
     im.prepass.ensure(im.dev.sms);
@@ -1147,7 +1169,8 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
             }
             auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
             kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
-                n, im.rp.get(), im.ci.get(), im.diag.get(), im.order_l.get(), im.lu.get(), shift, im.done.get(),
+                n, im.rp.get(), im.ci.get(), im.diag.get(),
+                im.ticket_order == 1 ? im.order_fact.get() : im.order_l.get(), im.lu.get(), shift, im.done.get(),
                 im.stamp, im.counters.get(), im.status.get(), im.fact_cap, im.fact_hcap);
             GB_CUDA_CHECK(cudaGetLastError());
             im.launches += 1;
