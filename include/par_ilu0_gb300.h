@@ -67,7 +67,10 @@ enum {
      *        matrix's plane size when a cost model expects it to beat the level-ordered
      *        kernel (factors with at most 8 entries per row and triangle), else the
      *        level-ordered kernel; LLJBASH_IluInfo reports the choice;
-     *   -1:  the level-ordered sync-free kernel. */
+     *   -1:  the level-ordered sync-free kernel;
+     *   -2:  level-synchronous (the reference's USE_LEVEL variant): the rows of each level
+     *        solved by the whole grid without waits, a grid barrier between levels
+     *        (cooperative launch), for both value types. */
     LLJBASH_ILU_OPT_BLOCK_ROWS = 2,
     /* warps of the level-ordered substitution kernels (0 = automatic: about 48 levels'
      * worth of tasks, 4 levels' worth when a triangle has rows too long for a lane group

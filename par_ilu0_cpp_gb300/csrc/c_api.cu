@@ -156,7 +156,7 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 s->impl()->push_wait_limit();
                 return 0;
             case LLJBASH_ILU_OPT_BLOCK_ROWS:
-                if (value < -1 || value > 1e8) throw std::runtime_error("block rows must be -1, 0 or a row count");
+                if (value < -2 || value > 1e8) throw std::runtime_error("block rows must be -2, -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);
                 return 0;
             case LLJBASH_ILU_OPT_TICKET_ORDER:

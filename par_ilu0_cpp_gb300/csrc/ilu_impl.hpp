@@ -22,6 +22,9 @@ struct LevelPack {
     DeviceBuffer<int> rows, off, len, cols, src, dsrc;
     DeviceBuffer<double> v64, d64;
     DeviceBuffer<float> v32, d32;
+    // level-synchronous packs only: tasks of level l are [ltask[l], ltask[l + 1])
+    DeviceBuffer<int> ltask;
+    int nlev = 0;
 
     template <class T>
     PackedTri<T> view() const;
@@ -176,6 +179,10 @@ struct IluSolver::Impl {
     gb300::BlockPack LB64, UB64, LB32, UB32;
     bool blk64 = false, blk32 = false;
     bool level_packs = false;  // L and U (level-ordered warp layout) are built
+    // level-synchronous schedule (block_rows == -2): level-aligned packs, cooperative grid
+    gb300::LevelPack LS, US;
+    bool levelsync = false;
+    int grid_levelsync = 0;
     // structured-grid sweeps (grid_sweep.cuh) per value type, when the factor is a 7- or
     // 5-point stencil in natural order and grid_mode allows it
     gb300::GridPack GP;
@@ -213,7 +220,8 @@ struct IluSolver::Impl {
     int solve_warps = 0;  // requested warps for the level-ordered kernels (0 = automatic)
     int row_lanes = 0;    // requested lanes per row of the level-ordered kernels (0 = automatic)
     int wait_limit_us = 0;  // device wait limit in microseconds (0 = kWaitLimitUsDefault)
-    int block_rows = 0;  // rows per substitution block (0 = automatic, < 0 = level-ordered kernel)
+    int block_rows = 0;  // rows per substitution block (0 = automatic, -1 = level-ordered kernel,
+                         // -2 = level-synchronous kernel)
     long long launches = 0;  // kernels launched by Factorize / Substitute
 
     ~Impl();

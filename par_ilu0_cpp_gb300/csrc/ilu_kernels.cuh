@@ -979,6 +979,82 @@ __global__ void __launch_bounds__(kBlockWarpsMax * kWarp, 1)
     }
 }
 
+// ---------------------------------------------------------------------------------
+// Level-synchronous substitution (the reference's USE_LEVEL variant,
+// src/ilu_solver.cpp:482-511, src/subtree.hpp:516-575): the rows of one level of the
+// dependency DAG are solved by all warps of the grid at once, without waits, and a grid
+// barrier separates consecutive levels.  Launched cooperatively (all CTAs resident).
+// Packed like PackedTri with one lane per row, but tasks never straddle two levels:
+// ltask[l] .. ltask[l + 1] are the tasks of level l.  Dependencies are read at L2 (ld.cg):
+// they were written by other SMs before the barrier.  Operations per row as the other
+// kernels (L ascending, U descending, FP64 division / FP32 reciprocal): identical results.
+// ---------------------------------------------------------------------------------
+
+// Grid barrier over all CTAs of a cooperative launch: bar[0] arrivals, bar[1] generation.
+// The last CTA to arrive resets the count and advances the generation; the others wait
+// (bounded) for the generation to change.  Returns false when the wait gave up.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* status) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        s_ok = 1;
+        const int gen = ld_acquire(reinterpret_cast<const int*>(bar + 1));
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            st_release(reinterpret_cast<int*>(bar + 1), gen + 1);
+        } else {
+            WaitBudget wb;
+            while (ld_acquire(reinterpret_cast<const int*>(bar + 1)) == gen) {
+                if (wb.expired(status)) {
+                    atomicExch(status + kStatusTimeout, 1);
+                    s_ok = 0;
+                    break;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <class T, bool UPPER>
+__global__ void __launch_bounds__(kSolveWarps * kWarp)
+    sptrsv_levelsync_kernel(PackedTri<T> P, const int* __restrict__ ltask, int nlev, T* in, const double* scale,
+                            T* out, unsigned* bar, int* status, const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    const bool scaled = !UPPER && scale != nullptr;
+    const T sc = scaled ? static_cast<T>(*scale) : T(1);
+    const int lane = threadIdx.x & 31;
+    const int gw = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int l = 0; l < nlev; ++l) {
+        for (int t = ltask[l] + gw; t < ltask[l + 1]; t += nw) {
+            const int row = P.rows[t * kWarp + lane];
+            if (row < 0) continue;
+            T acc = in[row];
+            if (scaled) {
+                acc = acc * sc;
+                in[row] = acc;
+            }
+            const int off = P.off[t];
+            const int K = P.len[t];
+            for (int k = 0; k < K; ++k) {
+                const int c = P.cols[off + k * kWarp + lane];
+                if (c >= 0) acc = fma(-P.vals[off + k * kWarp + lane], __ldcg(out + c), acc);
+            }
+            if (UPPER) {
+                const T d = P.dvals[t * kWarp + lane];
+                acc = sizeof(T) == 8 ? acc / d : acc * d;  // FP32: d holds 1 / u_ii
+            }
+            out[row] = Sentinel<T>::canon(acc);
+        }
+        if (l + 1 < nlev && !grid_barrier(bar, status)) return;
+    }
+}
+
 // Fills n entries with the sentinel.
 template <class T>
 __global__ void fill_sentinel_kernel(long long n, T* p) {

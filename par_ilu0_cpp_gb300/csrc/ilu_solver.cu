@@ -108,6 +108,90 @@ static void build_level_pack(int n, const int* rp, const int* ci, const std::vec
     GB_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
+// Host construction of a level-synchronous pack: rows in level order (order / lptr:
+// the level sets), one lane per row, 32 rows per task, a new task at every level
+// boundary; ltask[l] = first task of level l.  Entry layout as build_level_pack.
+static void build_levelsync_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag,
+                                 const std::vector<int>& order, const std::vector<int>& lptr, int nlev, bool lower,
+                                 LevelPack& P, cudaStream_t s) {
+    std::vector<int> rows, off, len, dsrc, ltask(static_cast<size_t>(nlev) + 1, 0);
+    auto count = [&](int r) { return lower ? diag[r] - rp[r] : rp[r + 1] - diag[r] - 1; };
+    long long slots = 0;
+    for (int l = 0; l < nlev; ++l) {
+        ltask[static_cast<size_t>(l)] = static_cast<int>(off.size());
+        for (int q0 = lptr[static_cast<size_t>(l)]; q0 < lptr[static_cast<size_t>(l) + 1]; q0 += kWarp) {
+            int K = 0;
+            for (int u = 0; u < kWarp; ++u) {
+                const int q = q0 + u;
+                const int r = q < lptr[static_cast<size_t>(l) + 1] ? order[static_cast<size_t>(q)] : -1;
+                rows.push_back(r);
+                if (!lower) dsrc.push_back(r >= 0 ? diag[r] : -1);
+                if (r >= 0) K = std::max(K, count(r));
+            }
+            off.push_back(static_cast<int>(slots));
+            len.push_back(K);
+            slots += static_cast<long long>(K) * kWarp;
+            if (slots > INT_MAX) throw std::runtime_error("triangular factor too large for 32-bit slot offsets");
+        }
+    }
+    ltask[static_cast<size_t>(nlev)] = static_cast<int>(off.size());
+    const int ntask = static_cast<int>(off.size());
+    std::vector<int> cols(static_cast<size_t>(slots), -1), src(static_cast<size_t>(slots), -1);
+    for (int t = 0; t < ntask; ++t)
+        for (int l = 0; l < kWarp; ++l) {
+            const int r = rows[static_cast<size_t>(t) * kWarp + l];
+            if (r < 0) continue;
+            int k = 0;
+            auto put = [&](int p) {
+                const size_t sidx = static_cast<size_t>(off[static_cast<size_t>(t)]) + static_cast<size_t>(k++) * kWarp + l;
+                cols[sidx] = ci[p];
+                src[sidx] = p;
+            };
+            if (lower) {
+                for (int p = rp[r]; p < diag[r]; ++p) put(p);
+            } else {
+                for (int p = rp[r + 1] - 1; p > diag[r]; --p) put(p);
+            }
+        }
+    P.ntask = ntask;
+    P.group = 1;
+    P.slots = slots;
+    P.nlev = nlev;
+    P.rows.upload(rows.data(), rows.size(), s);
+    P.off.upload(off.data(), off.size(), s);
+    P.len.upload(len.data(), len.size(), s);
+    P.cols.upload(cols.data(), cols.size(), s);
+    P.src.upload(src.data(), src.size(), s);
+    P.ltask.upload(ltask.data(), ltask.size(), s);
+    if (!lower) P.dsrc.upload(dsrc.data(), dsrc.size(), s);
+    P.v64.reserve(static_cast<size_t>(std::max<long long>(slots, 1)));
+    P.v32.reserve(static_cast<size_t>(std::max<long long>(slots, 1)));
+    if (!lower) {
+        P.d64.reserve(static_cast<size_t>(std::max(ntask, 1)) * kWarp);
+        P.d32.reserve(static_cast<size_t>(std::max(ntask, 1)) * kWarp);
+    }
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));  // host vectors must outlive the copies
+}
+
+template <class T, bool UPPER>
+static void launch_levelsync(const LevelPack& P, int grid, cudaStream_t s, T* in, const double* scale, T* out,
+                             unsigned* bar, int* status, const int* gate, int step) {
+    if (P.ntask == 0) return;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(grid));
+    cfg.blockDim = dim3(kSolveWarps * kWarp);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, sptrsv_levelsync_kernel<T, UPPER>, P.view<T>(),
+                                     static_cast<const int*>(P.ltask.get()), P.nlev, in, scale, out, bar, status, gate,
+                                     step));
+}
+
 // Level-ordered sweeps, dispatched on the factor's lanes per row.
 template <class T>
 static void launch_level_lower(const LevelPack& L, int grid, int threads, cudaStream_t s, T* b, const double* scale,
@@ -858,6 +942,10 @@ IluSolver::Impl::~Impl() {
 
 template <class T>
 void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T* y, const int* gate, int step) const {
+    if (levelsync) {
+        launch_levelsync<T, false>(LS, grid_levelsync, s, b, scale, y, counters.get() + 4, status.get(), gate, step);
+        return;
+    }
     if (sizeof(T) == 8 ? grid64 : grid32) {
         // b (natural order, rescaled in place) -> layout; the forward sweep's layout output
         // reset to the sentinel in the same pass; `y` is not used
@@ -878,6 +966,10 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
 
 template <class T>
 void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, int step) const {
+    if (levelsync) {
+        launch_levelsync<T, true>(US, grid_levelsync, s, y, nullptr, x, counters.get() + 4, status.get(), gate, step);
+        return;
+    }
     if (sizeof(T) == 8 ? grid64 : grid32) {
         // layout output of the forward sweep -> backward sweep -> x (natural order); the
         // layout output is reset to the sentinel by the scatter; `y` is not used
@@ -898,6 +990,7 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
 
 template <class T>
 const void* IluSolver::Impl::subst_key() const {
+    if (levelsync) return LS.cols.get();
     if (sizeof(T) == 8 ? grid64 : grid32)
         return sizeof(T) == 8 ? static_cast<const void*>(GP.lz64.get()) : static_cast<const void*>(GP.lz32.get());
     if (sizeof(T) == 8 ? blk64 : blk32) return (sizeof(T) == 8 ? LB64 : LB32).codes.get();
@@ -925,6 +1018,8 @@ void IluSolver::Impl::check_status(cudaStream_t s) {
     if (h[kStatusTimeout] != 0) {
         const int zero = 0;
         GB_CUDA_CHECK(cudaMemcpy(status.get() + kStatusTimeout, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        // a kernel that gave up may leave its ticket counters or grid-barrier words set
+        GB_CUDA_CHECK(cudaMemset(counters.get(), 0, sizeof(unsigned) * 8));
         throw std::runtime_error("dependency wait timed out on the device");
     }
 }
@@ -1046,6 +1141,25 @@ void IluSolver::SetupMatrix() {
             if (!ok) continue;
             (elem == 8 ? im.blk64 : im.blk32) = true;
         }
+    }
+    im.levelsync = im.block_rows == -2;
+    if (im.levelsync) {
+        build_levelsync_pack(n, rp, ci, im.an.diag, im.an.order_l, im.an.lptr_l, im.an.nlev_l, true, im.LS, s);
+        build_levelsync_pack(n, rp, ci, im.an.diag, im.an.order_u, im.an.lptr_u, im.an.nlev_u, false, im.US, s);
+        // cooperative launch: every CTA resident (the grid barrier waits for all of them)
+        int per_sm = 0;
+        for (auto kern : {sptrsv_levelsync_kernel<double, false>, sptrsv_levelsync_kernel<double, true>}) {
+            int r = 0;
+            GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, kSolveWarps * kWarp, 0));
+            per_sm = per_sm == 0 ? r : std::min(per_sm, r);
+        }
+        for (auto kern : {sptrsv_levelsync_kernel<float, false>, sptrsv_levelsync_kernel<float, true>}) {
+            int r = 0;
+            GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, kSolveWarps * kWarp, 0));
+            per_sm = std::min(per_sm, r);
+        }
+        if (per_sm < 1) throw std::runtime_error("level-synchronous kernel cannot be resident");
+        im.grid_levelsync = std::min(per_sm, 2) * im.dev.sms;
     }
     im.level_packs = !(im.blk64 && im.blk32);
     if (im.level_packs) {
@@ -1187,6 +1301,11 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
             if (im.level_packs) {
                 gather_level_pack(im.L, true, im.lu.get(), s, im.dev.sms);
                 gather_level_pack(im.U, false, im.lu.get(), s, im.dev.sms);
+                im.launches += 6;
+            }
+            if (im.levelsync) {
+                gather_level_pack(im.LS, true, im.lu.get(), s, im.dev.sms);
+                gather_level_pack(im.US, false, im.lu.get(), s, im.dev.sms);
                 im.launches += 6;
             }
             if (im.grid64) {

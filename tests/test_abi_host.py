@@ -198,10 +198,10 @@ def test_ilu_option_values_checked():
     for v in (-1, 0.5, 3e9):
         with pytest.raises(RuntimeError):
             ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, v)
-    for v in (-1, 0, 16384):
+    for v in (-2, -1, 0, 16384):
         ilu.set_option(api.ILU_OPT_BLOCK_ROWS, v)
     with pytest.raises(RuntimeError):
-        ilu.set_option(api.ILU_OPT_BLOCK_ROWS, -2)
+        ilu.set_option(api.ILU_OPT_BLOCK_ROWS, -3)
     for v in (-1, 0, 1):
         ilu.set_option(api.ILU_OPT_GRID, v)
     for v in (2, -2, 0.5):
@@ -217,5 +217,9 @@ def test_ilu_option_values_checked():
         ilu.set_option(opt, 7)
         with pytest.raises(RuntimeError):
             ilu.set_option(opt, -3)
+    for v in (0, 1):
+        ilu.set_option(api.ILU_OPT_TICKET_ORDER, v)
+    with pytest.raises(RuntimeError):
+        ilu.set_option(api.ILU_OPT_TICKET_ORDER, 2)
     with pytest.raises(RuntimeError):
         ilu.set_option(12345, 1)

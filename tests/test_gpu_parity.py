@@ -426,3 +426,61 @@ def test_ragged_rows_against_oracle(port, lof):
     tol = 1e-8 * float(np.linalg.norm(b))
     res, _, _ = api.ilu_gmres(a, b, lof=lof, tol=tol, restart=30, maxit=1000, mode=1, relative=False)
     assert res.ok and true_residual(a, b, res.x) <= tol * 1.0001
+
+
+LEVELSYNC_CASES = [
+    ("convdiff3d_24", lambda: g.convdiff3d(24), 0),
+    ("lognormal27_12_k2", lambda: g.lognormal27(12, seed=3), 2),
+    ("ragged_3000", lambda: ragged(3000, 40, seed=17), 0),
+    ("banded_150", lambda: banded(1200, 150, 6), 0),
+]
+
+
+@pytest.mark.parametrize("name,make,lof", LEVELSYNC_CASES, ids=[c[0] for c in LEVELSYNC_CASES])
+def test_level_synchronous_schedule(port, name, make, lof):
+    """The level-synchronous sweeps (LLJBASH_ILU_OPT_BLOCK_ROWS = -2: one grid barrier
+    per level, no waits) give the level-ordered kernel's results bit for bit, in FP64
+    substitution and in the mixed-precision solve, and 1e-12 against the oracle."""
+    a = make()
+    f, _ = port.iluk_symbolic(a, lof) if lof else (a, None)
+    _, b = g.random_rhs(a, seed=21)
+    tol = 1e-8 * float(np.linalg.norm(b))
+    out = {}
+    for sched in (-1, -2):
+        ilu = api.IluSolver()
+        ilu.set_option(api.ILU_OPT_BLOCK_ROWS, sched)
+        ilu.set_matrix(f)
+        assert ilu.setup() == 0, api.last_error()
+        assert ilu.factorize() == 0, api.last_error()
+        x = ilu.substitute(b)
+        gm = api.Gmres(tol, 30, 1000)
+        gm.set_preconditioner(ilu)
+        gm.set_option(api.GMRES_OPT_MODE, 1)
+        res = gm.solve(a, b)
+        assert res.ok
+        out[sched] = (x, res.iterations, res.x)
+    assert np.array_equal(out[-2][0], out[-1][0])
+    assert out[-2][1] == out[-1][1] and np.array_equal(out[-2][2], out[-1][2])
+    lu_ref, _ = port.factorize(f)
+    assert rel_err(out[-2][0], port.substitute(f, lu_ref, b)) <= 1e-12
+
+
+def test_level_synchronous_barrier_recovers_after_give_up():
+    """A grid-barrier wait that reaches a 1 us limit gives up and reports the timeout
+    (the barrier words are then reset); with the default limit the next solve is right."""
+    a = banded(1500, 60, 9)
+    _, b = g.random_rhs(a, seed=3)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_BLOCK_ROWS, -2)
+    ilu.set_matrix(a)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    x_ref = ilu.substitute(b)
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 1)
+    try:
+        ilu.substitute(b)
+    except RuntimeError as e:
+        assert "timed out" in str(e)
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 0)
+    for _ in range(2):
+        assert np.array_equal(ilu.substitute(b), x_ref)
