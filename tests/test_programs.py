@@ -44,7 +44,7 @@ def write_mm1(path, a):
         fh.write("%%MatrixMarket matrix coordinate real general\n")
         fh.write(f"{a.n} {a.n} {a.nnz}\n")
         for r, c, v in zip(rows, a.col_idx, a.values):
-            fh.write(f"{r + 1} {c + 1} {v!r}\n")
+            fh.write(f"{int(r) + 1} {int(c) + 1} {float(v)!r}\n")
 
 
 def _field(out, name):
