@@ -62,10 +62,13 @@ void ReadCsrMatrixMM1(CsrMatrix* mat, const char* filename);
 #define CsrMatVec LLJBASH_DECL(CsrMatVec)
 void CsrMatVec(const CsrMatrix* mat, const double* vec, double* sol);
 
-/* Fill-reducing orderings.  The reference delegates them to SuiteSparse AMD/CHOLMOD
- * (src/csr_matrix.cpp:173-225); this library does not ship them: both write the
- * identity permutation and report failure (-1 for AMD, 0 for ND, the reference's
- * failure values).  replaces include/csr_matrix.h:45-49 */
+/* Fill-reducing orderings of the pattern of A + A^T: p[k] = the row placed k-th, ip (may
+ * be NULL) its inverse.  The reference delegates them to SuiteSparse AMD / CHOLMOD nested
+ * dissection (src/csr_matrix.cpp:173-225); this library computes its own (approximate
+ * minimum degree on the quotient graph; recursive bisection at breadth-first level
+ * separators), so the permutations differ from SuiteSparse's.  Return values are the
+ * reference's: CsrAmdOrder 0 on success, -1 on failure; CsrNdOrder 1 on success, 0 on
+ * failure.  replaces include/csr_matrix.h:45-49 */
 #define CsrAmdOrder LLJBASH_DECL(CsrAmdOrder)
 int CsrAmdOrder(const CsrMatrix* mat, int* p, int* ip);
 

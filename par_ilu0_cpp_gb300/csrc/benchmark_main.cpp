@@ -165,8 +165,9 @@ int main(int argc, char* argv[]) {
 
     if (o.amd || o.nd) {
         std::vector<int> p(static_cast<size_t>(n)), ip(static_cast<size_t>(n));
+        // the reference's return conventions: AMD 0 on success, ND 1 on success
         const int rc = o.amd ? CsrAmdOrder(&csr, p.data(), ip.data()) : CsrNdOrder(&csr, p.data(), ip.data());
-        if (rc != 0) {
+        if (rc != (o.amd ? 0 : 1)) {
             std::fprintf(stderr, "%s ordering failed (%d)\n", o.amd ? "AMD" : "ND", rc);
             return 1;
         }

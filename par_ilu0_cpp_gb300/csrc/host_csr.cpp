@@ -14,8 +14,10 @@
 #include <utility>
 #include <vector>
 
+#include "analysis.hpp"
 #include "csr_matrix.h"
 #include "iluk.h"
+#include "orderings.hpp"
 
 namespace {
 
@@ -75,6 +77,31 @@ void realloc_array(T*& arr, long long count) {
     arr = count > 0 ? static_cast<T*>(host_alloc(sizeof(T) * static_cast<size_t>(count))) : nullptr;
 }
 
+}  // namespace
+
+// Fill-reducing orderings (orderings.hpp) of the pattern of A + A^T: p[k] = the row
+// eliminated k-th, ip its inverse.  Return values as the reference's wrappers
+// (src/csr_matrix.cpp:173-225): AMD 0 on success and -1 on failure, ND 1 on success and
+// 0 on failure.
+namespace {
+template <class F>
+int run_ordering(const CsrMatrix* mat, int* p, int* ip, F order_fn) {
+    if (mat == nullptr || mat->size < 0 || p == nullptr || (mat->size > 0 && mat->row_ptr == nullptr)) return -1;
+    const int n = mat->size;
+    try {
+        gb300::validate_csr(n, mat->row_ptr, mat->col_idx, "ordering input");
+        std::vector<int> xadj, adj;
+        gb300::symmetric_graph(n, mat->row_ptr, mat->col_idx, xadj, adj);
+        const std::vector<int> order = order_fn(n, xadj, adj);
+        if (static_cast<int>(order.size()) != n) return -1;
+        std::copy(order.begin(), order.end(), p);
+        if (ip)
+            for (int i = 0; i < n; ++i) ip[p[i]] = i;
+    } catch (const std::exception&) {
+        return -1;
+    }
+    return 0;
+}
 }  // namespace
 
 extern "C" {
@@ -230,19 +257,11 @@ void ReadCsrMatrixMM1(CsrMatrix* mat, const char* filename) {
 }
 
 int CsrAmdOrder(const CsrMatrix* mat, int* p, int* ip) {
-    for (int i = 0; i < mat->size; ++i) {
-        p[i] = i;
-        if (ip) ip[i] = i;
-    }
-    return -1;
+    return run_ordering(mat, p, ip, gb300::minimum_degree_order);
 }
 
 int CsrNdOrder(const CsrMatrix* mat, int* p, int* ip) {
-    for (int i = 0; i < mat->size; ++i) {
-        p[i] = i;
-        if (ip) ip[i] = i;
-    }
-    return 0;
+    return run_ordering(mat, p, ip, gb300::nested_dissection_order) == 0 ? 1 : 0;
 }
 
 // Symbolic ILU(k) (reference behaviour: src/iluk.cpp:5-54).  Row i starts from A's

@@ -114,15 +114,48 @@ def test_csr_lifecycle():
     assert dst.size == -1 and not dst.row_ptr and not dst.value
 
 
-def test_orderings_report_unavailable():
+def _order(a, nd):
     lib = api.load()
-    a = Csr(3, [0, 1, 2, 3], [0, 1, 2], [1.0, 1.0, 1.0])
-    p = np.zeros(3, np.int32)
-    ip = np.zeros(3, np.int32)
+    p = np.zeros(a.n, np.int32)
+    ip = np.zeros(a.n, np.int32)
     ptr = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
-    assert lib.LLJBASH_CsrAmdOrder(api.HostCsrView(a).ref, ptr(p), ptr(ip)) == -1
-    assert list(p) == [0, 1, 2]
-    assert lib.LLJBASH_CsrNdOrder(api.HostCsrView(a).ref, ptr(p), ptr(ip)) == 0
+    f = lib.LLJBASH_CsrNdOrder if nd else lib.LLJBASH_CsrAmdOrder
+    return f(api.HostCsrView(a).ref, ptr(p), ptr(ip)), p, ip
+
+
+@pytest.mark.parametrize("make", [lambda: Csr(3, [0, 1, 2, 3], [0, 1, 2], [1.0, 1.0, 1.0]),
+                                  lambda: __import__("par_ilu0_cpp_gb300.generators").generators.laplace2d(40),
+                                  lambda: __import__("par_ilu0_cpp_gb300.generators").generators.convdiff3d(14)],
+                         ids=["diagonal", "laplace2d_40", "convdiff3d_14"])
+def test_fill_reducing_orderings(make):
+    """CsrAmdOrder / CsrNdOrder (the library's own AMD and nested dissection): valid
+    permutations with the reference's return codes (AMD 0, ND 1 on success), p[k] the
+    row placed k-th and ip its inverse, and far less LU fill than the natural order."""
+    import scipy.sparse.linalg as sla
+
+    a = make()
+    m = a.to_scipy()
+
+    def fill(perm):
+        lu = sla.splu(m[perm][:, perm].tocsc(), permc_spec="NATURAL", diag_pivot_thresh=0.0,
+                      options=dict(SymmetricMode=True))
+        return lu.L.nnz + lu.U.nnz
+
+    natural = fill(np.arange(a.n))
+    for nd in (False, True):
+        rc, p, ip = _order(a, nd)
+        assert rc == (1 if nd else 0)
+        assert np.array_equal(np.sort(p), np.arange(a.n)) and np.array_equal(ip[p], np.arange(a.n))
+        if a.n > 100:
+            assert fill(p) < 0.5 * natural, (nd, fill(p), natural)
+
+
+def test_ordering_rejects_invalid_input():
+    bad = Csr(3, [0, 1, 3, 3], [0, 5, 1], [1.0, 1.0, 1.0])
+    rc, _, _ = _order(bad, False)
+    assert rc == -1
+    rc, _, _ = _order(bad, True)
+    assert rc == 0
 
 
 def _write_mm(path, n, entries):

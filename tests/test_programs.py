@@ -115,3 +115,25 @@ def test_benchmark_cli_isolation_modes(tmp_path, mode):
         assert float(_field(res.stdout, "total factorize time (s)")) > 0
     else:
         assert float(_field(res.stdout, "total precon time (s)")) > 0
+
+
+def test_reference_amd_test_runs_on_the_host(tmp_path):
+    """The reference's test/amd_test.c (unchanged) prints the pattern of a 5x5 matrix in
+    its AMD order; CsrAmdOrder returns 0 and a permutation."""
+    exe = _compile_reference_program("test/amd_test.c", str(tmp_path))
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert "ret: 0" in res.stdout
+    perm = re.search(r"P:\n((?: \d+)+)", res.stdout).group(1).split()
+    assert sorted(int(v) for v in perm) == list(range(5))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flag", ["--amd", "--nd"])
+def test_benchmark_cli_reordered(tmp_path, flag):
+    mm = str(tmp_path / "a.mtx")
+    write_mm1(mm, g.convdiff3d(16))
+    res = subprocess.run([BENCH, "-m", mm, flag, "-k", "1"], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert float(_field(res.stdout, "max_err")) < 1e-5
+    assert int(_field(res.stdout, "iter")) > 0
