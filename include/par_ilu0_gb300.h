@@ -109,7 +109,13 @@ enum {
      * reference's subtree scheduler (src/subtree.hpp tree_schedule, one worker per SM):
      * the workers' independent subtrees interleaved row by row, then the remaining
      * (separator) rows in elimination-tree post order.  Next IluSolverSetup. */
-    LLJBASH_ILU_OPT_TICKET_ORDER = 11
+    LLJBASH_ILU_OPT_TICKET_ORDER = 11,
+    /* factorisation kernel (results are the same for every choice): 0 (default)
+     * automatic: one lane per row when no row has more than 16 entries (each finished row
+     * publishes u_kk and its upper entries, rows waiting for it poll exactly those
+     * values), else one warp per row; 1 warp per row; 2 lane per row where the rows
+     * qualify.  Next IluSolverSetup. */
+    LLJBASH_ILU_OPT_FACTOR_KERNEL = 12
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 
@@ -167,6 +173,7 @@ typedef struct LLJBASH_IluInfo {
     int block_cluster_fp32; /* the same for the FP32 sweeps */
     int row_lanes_lower;  /* lanes per row of the level-ordered lower / upper sweeps */
     int row_lanes_upper;
+    int factor_lane;      /* 1: the factorisation runs one lane per row (else one warp per row) */
     int grid_fp64;        /* 1: the FP64 / FP32 sweeps use the structured-grid schedule */
     int grid_fp32;
     int grid_nx, grid_ny, grid_nz;  /* its grid (2-D: grid_ny = 1) */

@@ -51,7 +51,8 @@ class IluInfo(ctypes.Structure):
                 ("block_rows_fp64", ctypes.c_int), ("block_rows_fp32", ctypes.c_int),
                 ("block_cluster_fp64", ctypes.c_int), ("block_cluster_fp32", ctypes.c_int),
                 ("row_lanes_lower", ctypes.c_int), ("row_lanes_upper", ctypes.c_int),
-                ("grid_fp64", ctypes.c_int), ("grid_fp32", ctypes.c_int), ("grid_nx", ctypes.c_int),
+                ("factor_lane", ctypes.c_int), ("grid_fp64", ctypes.c_int), ("grid_fp32", ctypes.c_int),
+                ("grid_nx", ctypes.c_int),
                 ("grid_ny", ctypes.c_int), ("grid_nz", ctypes.c_int), ("grid_lane_elems", ctypes.c_int),
                 ("grid_tile_lines", ctypes.c_int), ("grid_tile_planes", ctypes.c_int), ("grid_tiles", ctypes.c_int)]
 
@@ -72,6 +73,7 @@ ILU_OPT_GRID_LANE_ELEMS = 7
 ILU_OPT_GRID_TILE_LINES = 8
 ILU_OPT_GRID_TILE_PLANES = 9
 ILU_OPT_TICKET_ORDER = 11
+ILU_OPT_FACTOR_KERNEL = 12
 GMRES_OPT_MODE = 1
 GMRES_OPT_TAU = 2
 GMRES_OPT_USE_GRAPH = 3

@@ -159,6 +159,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 if (value < -2 || value > 1e8) throw std::runtime_error("block rows must be -2, -1, 0 or a row count");
                 s->impl()->block_rows = static_cast<int>(value);
                 return 0;
+            case LLJBASH_ILU_OPT_FACTOR_KERNEL:
+                if (value != 0 && value != 1 && value != 2) throw std::runtime_error("factor kernel must be 0, 1 or 2");
+                s->impl()->factor_kernel = static_cast<int>(value);
+                return 0;
             case LLJBASH_ILU_OPT_TICKET_ORDER:
                 if (value != 0 && value != 1) throw std::runtime_error("ticket order must be 0 or 1");
                 s->impl()->ticket_order = static_cast<int>(value);
@@ -347,6 +351,7 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->block_cluster_fp32 = im->blk32 ? im->LB32.cl : 0;
     info->row_lanes_lower = im->level_packs ? im->L.group : 0;
     info->row_lanes_upper = im->level_packs ? im->U.group : 0;
+    info->factor_lane = im->fact_lane ? 1 : 0;
     info->grid_fp64 = im->grid64 ? 1 : 0;
     info->grid_fp32 = im->grid32 ? 1 : 0;
     if (im->grid64 || im->grid32) {

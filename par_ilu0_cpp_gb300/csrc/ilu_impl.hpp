@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "device_util.hpp"
+#include "factor_lane.cuh"
 #include "grid_sweep.cuh"
 #include "ilu_kernels.cuh"
 #include "ilu_solver.hpp"
@@ -169,6 +170,14 @@ struct IluSolver::Impl {
     gb300::DeviceBuffer<int> rp, ci, diag, order_l;
     gb300::DeviceBuffer<int> order_fact;  // ticket order of the factorisation (ticket_order = 1)
     int ticket_order = 0;  // factorisation tickets: 0 level order, 1 the subtree scheduler's order
+    // lane-per-row factorisation (factor_lane.cuh) for factors with short rows
+    int factor_kernel = 0;  // 0 automatic, 1 warp per row, 2 lane per row (when the rows qualify)
+    bool fact_lane = false;
+    gb300::DeviceBuffer<int> lf_rows, lf_pub_off, lf_upd_ptr;
+    gb300::DeviceBuffer<int2> lf_upd;
+    gb300::DeviceBuffer<double> lf_pub;
+    long long lf_pub_len = 0;
+    int lf_ntask = 0, grid_lane_fact = 0;
     gb300::DeviceBuffer<double> lu;
     gb300::DeviceBuffer<double> shift;      // per-row diagonal shift (learned), optional
     gb300::DeviceBuffer<int> done;          // per-row ready stamps of the factorisation

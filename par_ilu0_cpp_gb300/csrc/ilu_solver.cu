@@ -38,6 +38,12 @@ static int row_lanes_for(int kmax, int requested) {
     return g;
 }
 
+// Position of column c in the sorted ci[lo, hi), -1 if absent.
+static int find_sorted_host(const int* ci, int lo, int hi, int c) {
+    const int* it = std::lower_bound(ci + lo, ci + hi, c);
+    return (it != ci + hi && *it == c) ? static_cast<int>(it - ci) : -1;
+}
+
 // Host construction of a packed factor from a schedule `order` (rows in level order),
 // `group` lanes per row (PackedTri layout).  lower: entries [rp[r], diag[r]) ascending;
 // upper: entries (diag[r], rp[r+1]) descending plus the diagonal position.
@@ -190,6 +196,56 @@ static void launch_levelsync(const LevelPack& P, int grid, cudaStream_t s, T* in
     GB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, sptrsv_levelsync_kernel<T, UPPER>, P.view<T>(),
                                      static_cast<const int*>(P.ltask.get()), P.nlev, in, scale, out, bar, status, gate,
                                      step));
+}
+
+// Host construction of the lane-per-row factorisation (factor_lane.cuh): 32-row tasks in
+// the order `order` (level order: topological), every row's pub slots (u_kk, then its
+// strict-upper entries), and for every strict-lower entry p of row j (pivot k) the
+// updates (offset of c in row j, pub slot of u_kc) for c in row k's strict-upper part and
+// in row j's pattern, ascending c.  False when a row is longer than kLaneRowMax.
+static bool build_lane_factor(int n, const int* rp, const int* ci, const std::vector<int>& diag,
+                              const std::vector<int>& order, lljbash::IluSolver::Impl& im, cudaStream_t s) {
+    for (int r = 0; r < n; ++r)
+        if (rp[r + 1] - rp[r] > kLaneRowMax) return false;
+    const long long nnz = rp[n];
+    std::vector<int> pub_off(static_cast<size_t>(n));
+    long long slots = 0;
+    for (int r = 0; r < n; ++r) {
+        pub_off[static_cast<size_t>(r)] = static_cast<int>(slots);
+        slots += rp[r + 1] - diag[static_cast<size_t>(r)];  // u_rr and the strict-upper entries
+    }
+    if (slots > INT_MAX) return false;
+    std::vector<int> upd_ptr(static_cast<size_t>(nnz) + 1, 0);
+    std::vector<int2> upd;
+    for (int j = 0; j < n; ++j) {
+        for (int p = rp[j]; p < rp[j + 1]; ++p) {
+            upd_ptr[static_cast<size_t>(p)] = static_cast<int>(upd.size());
+            if (p >= diag[static_cast<size_t>(j)]) continue;
+            const int k = ci[p];
+            for (int qk = diag[static_cast<size_t>(k)] + 1; qk < rp[k + 1]; ++qk) {
+                const int pos = find_sorted_host(ci, rp[j], rp[j + 1], ci[qk]);
+                if (pos >= 0)
+                    upd.push_back(make_int2(pos - rp[j], pub_off[static_cast<size_t>(k)] + (qk - diag[static_cast<size_t>(k)])));
+            }
+        }
+    }
+    upd_ptr[static_cast<size_t>(nnz)] = static_cast<int>(upd.size());
+    const int ntask = ceil_div(n, kWarp);
+    std::vector<int> rows(static_cast<size_t>(ntask) * kWarp, -1);
+    for (int q = 0; q < n; ++q) rows[static_cast<size_t>(q)] = order[static_cast<size_t>(q)];
+    im.lf_rows.upload(rows.data(), rows.size(), s);
+    im.lf_pub_off.upload(pub_off.data(), pub_off.size(), s);
+    im.lf_upd_ptr.upload(upd_ptr.data(), upd_ptr.size(), s);
+    if (upd.empty()) upd.push_back(make_int2(0, 0));
+    im.lf_upd.upload(upd.data(), upd.size(), s);
+    im.lf_pub.reserve(static_cast<size_t>(std::max<long long>(slots, 1)));
+    im.lf_pub_len = slots;
+    im.lf_ntask = ntask;
+    int per_sm = 0;
+    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ilu_factor_lane_kernel, kLaneFactWarps * kWarp, 0));
+    im.grid_lane_fact = std::max(1, per_sm) * im.dev.sms;
+    GB_CUDA_CHECK(cudaStreamSynchronize(s));  // host vectors must outlive the copies
+    return true;
 }
 
 // Level-ordered sweeps, dispatched on the factor's lanes per row.
@@ -1066,6 +1122,7 @@ void IluSolver::SetupMatrix() {
     im.ci.upload(ci, static_cast<size_t>(im.nnz), s);
     im.diag.upload(im.an.diag.data(), static_cast<size_t>(n), s);
     im.order_l.upload(im.an.order_l.data(), static_cast<size_t>(n), s);
+    std::vector<int> tree_order;  // the factorisation's ticket order when ticket_order == 1
     if (im.ticket_order == 1 && n > 0) {
         // the reference's subtree schedule (one worker per SM): the workers' subtree rows
         // interleaved round-robin (rows of different subtrees are independent), then the
@@ -1086,6 +1143,7 @@ void IluSolver::SetupMatrix() {
         if (static_cast<int>(ord.size()) != n) throw std::runtime_error("tree schedule order is not a permutation");
         im.order_fact.upload(ord.data(), ord.size(), s);
         GB_CUDA_CHECK(cudaStreamSynchronize(s));  // ord must outlive the copy
+        tree_order.swap(ord);
     }
     im.depth_l.upload(im.an.depth_l.data(), static_cast<size_t>(n), s);
     im.shift.reserve(static_cast<size_t>(std::max(n, 1)));
@@ -1192,6 +1250,12 @@ void IluSolver::SetupMatrix() {
     im.sy32.reserve(nv);
     fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
     fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
+    // Factorisation kernel: lane per row for short rows (automatic or requested), else
+    // warp per row
+    im.fact_lane = false;
+    if (im.factor_kernel != 1 && n > 0)
+        im.fact_lane = build_lane_factor(n, rp, ci, im.an.diag,
+                                         im.ticket_order == 1 ? tree_order : im.an.order_l, im, s);
     // Factorisation launch: rows staged in shared memory up to the longest row where a
     // warp's share fits (fewer warps per block for long rows), a wider register window
     // of the next pivot row when pivot rows are long.
@@ -1281,13 +1345,30 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
             } else if (shift_kind == 1) {
                 shift = im.shift.get();
             }
+            if (im.fact_lane) {
+                fill_sentinel(im.lf_pub.get(), im.lf_pub_len, s, im.dev.sms);
+                LaneFactor F;
+                F.n = n;
+                F.ntask = im.lf_ntask;
+                F.rows = im.lf_rows.get();
+                F.rp = im.rp.get();
+                F.ci = im.ci.get();
+                F.diag = im.diag.get();
+                F.pub_off = im.lf_pub_off.get();
+                F.upd_ptr = im.lf_upd_ptr.get();
+                F.upd = im.lf_upd.get();
+                ilu_factor_lane_kernel<<<im.grid_lane_fact, kLaneFactWarps * kWarp, 0, s>>>(
+                    F, im.lu.get(), shift, im.lf_pub.get(), im.counters.get(), im.status.get());
+                GB_CUDA_CHECK(cudaGetLastError());
+                im.launches += 2;
+            }
             auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
-            kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
+            if (!im.fact_lane) kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
                 n, im.rp.get(), im.ci.get(), im.diag.get(),
                 im.ticket_order == 1 ? im.order_fact.get() : im.order_l.get(), im.lu.get(), shift, im.done.get(),
                 im.stamp, im.counters.get(), im.status.get(), im.fact_cap, im.fact_hcap);
             GB_CUDA_CHECK(cudaGetLastError());
-            im.launches += 1;
+            if (!im.fact_lane) im.launches += 1;
             if (im.blk64) {
                 gather_block(im.LB64, true, im.lu.get(), s, im.dev.sms);
                 gather_block(im.UB64, false, im.lu.get(), s, im.dev.sms);

@@ -484,3 +484,67 @@ def test_level_synchronous_barrier_recovers_after_give_up():
     ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 0)
     for _ in range(2):
         assert np.array_equal(ilu.substitute(b), x_ref)
+
+
+LANE_FACTOR_CASES = [
+    ("convdiff3d_32", lambda: g.convdiff3d(32), 0),
+    ("laplace2d_128_ilu2", lambda: g.laplace2d(128), 2),
+    ("ragged_4000", lambda: ragged(4000, 6, seed=31), 0),
+    ("ragged_2000_ilu1", lambda: ragged(2000, 3, seed=32), 1),
+    ("banded_5", lambda: banded(3000, 5, 7), 0),
+]
+
+
+@pytest.mark.parametrize("name,make,lof", LANE_FACTOR_CASES, ids=[c[0] for c in LANE_FACTOR_CASES])
+def test_lane_factorisation_matches_warp_kernel(port, name, make, lof):
+    """The lane-per-row factorisation (LLJBASH_ILU_OPT_FACTOR_KERNEL = 2) gives the
+    warp-per-row kernel's factors bit for bit, with and without a diagonal shift, and the
+    oracle's to 1e-12."""
+    a = make()
+    f, _ = port.iluk_symbolic(a, lof) if lof else (a, None)
+    shift = np.random.default_rng(5).uniform(0.0, 0.5, a.n)
+    vals = {}
+    for kern in (1, 2):
+        ilu = api.IluSolver()
+        ilu.set_option(api.ILU_OPT_FACTOR_KERNEL, kern)
+        ilu.set_matrix(f)
+        assert ilu.setup() == 0, api.last_error()
+        assert ilu.info().factor_lane == (1 if kern == 2 else 0)
+        assert ilu.factorize() == 0, api.last_error()
+        plain = ilu.values()
+        ilu.set_values(f.values)
+        ilu.set_shift(shift)
+        assert ilu.factorize() == 0, api.last_error()
+        vals[kern] = (plain, ilu.values())
+    assert np.array_equal(vals[1][0], vals[2][0]) and np.array_equal(vals[1][1], vals[2][1])
+    lu_ref, _ = port.factorize(f)
+    assert rel_err(vals[2][0], lu_ref, floor=1e-300) <= 1e-12
+
+
+def test_lane_factorisation_zero_pivot_and_recovery():
+    """A zero pivot is reported as with the warp kernel; a wait cut short by a 1 us limit
+    reports the timeout and the next factorisation is right."""
+    z = g.Csr(2, [0, 2, 4], [0, 1, 0, 1], [0.0, 1.0, 1.0, 1.0])
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_FACTOR_KERNEL, 2)
+    ilu.set_matrix(z)
+    assert ilu.setup() == 0 and ilu.info().factor_lane == 1
+    assert ilu.factorize() == 0
+    assert ilu.info().breakdowns >= 1 and ilu.info().first_breakdown == 0
+    a = banded(4000, 6, 3)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_FACTOR_KERNEL, 2)
+    ilu.set_matrix(a)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0
+    ref = ilu.values()
+    ilu.set_values(a.values)
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 1)
+    rc = ilu.factorize()
+    assert rc in (0, -1)
+    if rc == -1:
+        assert "timed out" in api.last_error()
+    ilu.set_option(api.ILU_OPT_WAIT_LIMIT_US, 0)
+    ilu.set_values(a.values)
+    assert ilu.factorize() == 0, api.last_error()
+    assert np.array_equal(ilu.values(), ref)
