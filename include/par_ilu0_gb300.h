@@ -110,11 +110,10 @@ enum {
      * the workers' independent subtrees interleaved row by row, then the remaining
      * (separator) rows in elimination-tree post order.  Next IluSolverSetup. */
     LLJBASH_ILU_OPT_TICKET_ORDER = 11,
-    /* factorisation kernel (results are the same for every choice): 0 (default)
-     * automatic: one lane per row when no row has more than 16 entries (each finished row
-     * publishes u_kk and its upper entries, rows waiting for it poll exactly those
-     * values), else one warp per row; 1 warp per row; 2 lane per row where the rows
-     * qualify.  Next IluSolverSetup. */
+    /* factorisation kernel (results are the same for every choice): 0 (default,
+     * automatic) and 1: one warp per row; 2: one lane per row when no row has more than
+     * 16 entries (each finished row publishes u_kk and its upper entries, rows waiting for
+     * it poll exactly those values), else one warp per row.  Next IluSolverSetup. */
     LLJBASH_ILU_OPT_FACTOR_KERNEL = 12
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);

@@ -241,9 +241,9 @@ static bool build_lane_factor(int n, const int* rp, const int* ci, const std::ve
     im.lf_pub.reserve(static_cast<size_t>(std::max<long long>(slots, 1)));
     im.lf_pub_len = slots;
     im.lf_ntask = ntask;
-    int per_sm = 0;
-    GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ilu_factor_lane_kernel, kLaneFactWarps * kWarp, 0));
-    im.grid_lane_fact = std::max(1, per_sm) * im.dev.sms;
+    // one CTA (8 warps) per SM, as the level-ordered sweeps: more warps only poll further
+    // ahead of the dependency chain and slow its L2 handoffs
+    im.grid_lane_fact = std::max(1, std::min(im.dev.sms, ntask));
     GB_CUDA_CHECK(cudaStreamSynchronize(s));  // host vectors must outlive the copies
     return true;
 }
@@ -1250,10 +1250,10 @@ void IluSolver::SetupMatrix() {
     im.sy32.reserve(nv);
     fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
     fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
-    // Factorisation kernel: lane per row for short rows (automatic or requested), else
-    // warp per row
+    // Factorisation kernel: warp per row (automatic), or lane per row for short rows when
+    // requested
     im.fact_lane = false;
-    if (im.factor_kernel != 1 && n > 0)
+    if (im.factor_kernel == 2 && n > 0)
         im.fact_lane = build_lane_factor(n, rp, ci, im.an.diag,
                                          im.ticket_order == 1 ? tree_order : im.an.order_l, im, s);
     // Factorisation launch: rows staged in shared memory up to the longest row where a
