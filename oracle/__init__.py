@@ -254,6 +254,23 @@ class Ref(_Lib):
         out["task_queue"] = out["task_queue"][: nt + 1] if nt else out["task_queue"][:0]
         return out
 
+    def solve_system(self, a, rhs, lof, rtol, restart, maxit, nthreads: int = 1):
+        """One system of a batch: symbolic + setup, one Factorize, then a GMRES solve
+        from x0 = 0 per row of rhs (nrhs x n) to rtol * ||b_r||_2, all on the calling
+        thread (ctypes releases the GIL, so a thread pool runs systems side by side).
+        The reference prints to stdout: wrap calls in c_stdout_to_stderr.  Returns
+        dict(converged, iters, x, times = [symbolic + setup, factorize, solves] in s)."""
+        rhs = np.ascontiguousarray(np.atleast_2d(rhs), dtype=np.float64)
+        nrhs = rhs.shape[0]
+        x = np.empty_like(rhs)
+        its = np.zeros(nrhs, dtype=np.int32)
+        times = np.zeros(3)
+        f = self.lib.ref_solve_system
+        f.restype = ctypes.c_int
+        conv = f(a.n, _ip(_i32(a.row_ptr)), _ip(_i32(a.col_idx)), _dp(_f64(a.values)), int(lof), int(restart),
+                 int(maxit), ctypes.c_double(rtol), int(nthreads), int(nrhs), _dp(rhs), _dp(x), _ip(its), _dp(times))
+        return dict(converged=int(conv), iters=its, x=x, times=times)
+
     def session(self, a, lof, tol, restart, maxit, nthreads):
         """The test/benchmark.cpp repetition loop: symbolic + first setup now, then
         RefSession.step() = one repetition (Factorize + GMRES timed)."""

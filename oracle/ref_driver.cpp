@@ -19,6 +19,7 @@
  */
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -286,6 +287,44 @@ void ref_session_destroy(void* hdl) {
     auto* s = static_cast<RefSession*>(hdl);
     DestroyCsrMatrix(&s->a);
     delete s;
+}
+
+/* ---- one system of a batch of independent systems: IlukSymbolic + SetupMatrix, one
+ * Factorize, then for each of nrhs right-hand sides (rhs / x: nrhs vectors of n) a
+ * GMRES solve from x0 = 0 to the reference's absolute criterion rtol * ||b_r||_2, all on
+ * the calling thread with nthreads OpenMP threads (SetupMatrix sets the calling thread's
+ * OpenMP thread count).  times[0] symbolic + setup, times[1] Factorize, times[2] all
+ * solves (s, steady_clock); iters[r] per right-hand side.  Returns the number of
+ * converged right-hand sides. */
+int ref_solve_system(int n, const int* rp, const int* ci, const double* val, int lof, int restart, int maxit,
+                     double rtol, int nthreads, int nrhs, const double* rhs, double* x, int* iters, double* times) {
+    double t[2] = {0.0, 0.0};
+    auto* s = static_cast<RefSession*>(ref_session_create(n, rp, ci, val, lof, restart, maxit, 0.0, nthreads, t));
+    double t0 = now_s();
+    s->ilu.Factorize();
+    double t1 = now_s();
+    int converged = 0;
+    std::vector<double> b(static_cast<size_t>(n));
+    for (int r = 0; r < nrhs; ++r) {
+        const double* br = rhs + static_cast<size_t>(r) * n;
+        double nb = 0.0;
+        for (int i = 0; i < n; ++i) nb += br[i] * br[i];
+        s->gmres.param().tolerance = rtol * std::sqrt(nb);
+        std::copy_n(br, n, b.data());
+        double* xr = x + static_cast<size_t>(r) * n;
+        std::fill_n(xr, n, 0.0);
+        auto ret = s->gmres.Solve(&s->a, b.data(), xr);
+        if (iters) iters[r] = ret.second;
+        converged += ret.first ? 1 : 0;
+    }
+    double t2 = now_s();
+    if (times) {
+        times[0] = t[0] + t[1];
+        times[1] = t1 - t0;
+        times[2] = t2 - t1;
+    }
+    ref_session_destroy(s);
+    return converged;
 }
 
 /* ---- subtree scheduler (src/subtree.hpp tree_schedule) ------------------------------

@@ -93,3 +93,27 @@ def test_host_analysis_bit_exact_at_benchmark_sizes(ref_fast, name, make, lof):
     depth_u, nu = ref_fast.levels(f_ref, False)
     assert np.array_equal(an["depth_l"], depth_l) and np.array_equal(an["depth_u"], depth_u)
     assert list(an["nlev"]) == [nl, nu]
+
+
+def test_reference_batch_entry_matches_single_solves():
+    """ref_solve_system (one factorisation, a GMRES solve per right-hand side, the batched
+    CPU baseline's unit of work) gives the same iterations and solutions as the
+    benchmark sequence run once per right-hand side, also from several threads at once."""
+    import concurrent.futures
+
+    try:
+        ref = oracle.Ref(oracle.REF_OMP_SO)
+    except OSError as e:
+        pytest.skip(f"reference timing build not loadable here: {e}")
+    systems = g.batched_systems(4, 7)
+    rhs = [np.atleast_2d(g.random_rhs(a, seed=40 + k, nrhs=3)[1]) for k, a in enumerate(systems)]
+    with oracle.c_stdout_to_stderr():
+        with concurrent.futures.ThreadPoolExecutor(max_workers=4) as ex:
+            out = list(ex.map(lambda k: ref.solve_system(systems[k], rhs[k], 0, 1e-8, 30, 1000, 1), range(4)))
+        for k, a in enumerate(systems):
+            assert out[k]["converged"] == 3
+            for r in range(3):
+                b = rhs[k][r]
+                one = ref.ilu_gmres(a, b, 0, 1e-8 * float(np.linalg.norm(b)), 30, 1000, nthreads=1)
+                assert one["ok"] and one["iters"] == out[k]["iters"][r]
+                assert rel_err(out[k]["x"][r], one["x"]) <= 1e-12
