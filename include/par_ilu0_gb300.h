@@ -91,19 +91,23 @@ enum {
      * -1 ("dependency wait timed out on the device") and the solver stays usable.  Takes
      * effect at the next launch. */
     LLJBASH_ILU_OPT_WAIT_LIMIT_US = 5,
-    /* structured-grid sweeps (results are the same as with every other schedule): for
-     * factors that are a full 7-point (3-D) or 5-point (2-D) stencil in natural order, the
-     * triangular sweeps run on a fixed wavefront schedule (a lane walks a grid line in
-     * registers, neighbours arrive by warp shuffles and shared memory), taking precedence
-     * over LLJBASH_ILU_OPT_BLOCK_ROWS.  1: on when the pattern qualifies; 0 (default,
-     * automatic): off, the block-local kernels being faster on the grids measured;
+    /* structured-grid line-pipeline sweeps (results are the same as with every other
+     * schedule): for factors that are a full 7-point (3-D) or 5-point (2-D) stencil in
+     * natural order, a lane walks one grid line in registers, the other two neighbours
+     * arrive by warp shuffles (lanes skewed by one step each), shared memory between the
+     * warps of a CTA and L2 between CTAs.  1: both sweeps of both precisions when the
+     * pattern qualifies, whatever LLJBASH_ILU_OPT_BLOCK_ROWS says; 0 (default, automatic):
+     * when the pattern qualifies and LLJBASH_ILU_OPT_BLOCK_ROWS is automatic (0), each
+     * sweep of each precision is timed at the first Factorize against the block-local /
+     * level-ordered kernel and the faster kept (LLJBASH_IluInfo grid_fp64 / grid_fp32);
      * -1: off.  Takes effect at the next IluSolverSetup. */
     LLJBASH_ILU_OPT_GRID = 6,
-    /* tuning of the structured-grid sweeps (0 = automatic), next IluSolverSetup:
-     * elements per lane along x (1, 2, 4), grid lines per tile, grid planes per tile. */
-    LLJBASH_ILU_OPT_GRID_LANE_ELEMS = 7,
-    LLJBASH_ILU_OPT_GRID_TILE_LINES = 8,
-    LLJBASH_ILU_OPT_GRID_TILE_PLANES = 9,
+    /* shape of the line-pipeline sweeps (0 = automatic), next IluSolverSetup: lanes of a
+     * warp along y (1, 4, 8; the rest along z; 2-D grids use 1), warps of a CTA along y
+     * and along z (at most 8 warps in all). */
+    LLJBASH_ILU_OPT_GRID_WARP_Y = 7,
+    LLJBASH_ILU_OPT_GRID_CTA_Y = 8,
+    LLJBASH_ILU_OPT_GRID_CTA_Z = 9,
     /* order in which the factorisation kernel's warps take rows (results are the same
      * for every order): 0 (default) level order (the reference's Levelization); 1 the
      * reference's subtree scheduler (src/subtree.hpp tree_schedule, one worker per SM):
@@ -173,13 +177,15 @@ typedef struct LLJBASH_IluInfo {
     int row_lanes_lower;  /* lanes per row of the level-ordered lower / upper sweeps */
     int row_lanes_upper;
     int factor_lane;      /* 1: the factorisation runs one lane per row (else one warp per row) */
-    int grid_fp64;        /* 1: the FP64 / FP32 sweeps use the structured-grid schedule */
+    int grid_fp64;        /* FP64 / FP32 sweeps on the line-pipeline schedule: bit 0 the
+                           * forward, bit 1 the backward sweep */
     int grid_fp32;
     int grid_nx, grid_ny, grid_nz;  /* its grid (2-D: grid_ny = 1) */
-    int grid_lane_elems;  /* elements per lane, lines and planes per tile, tiles */
-    int grid_tile_lines;
-    int grid_tile_planes;
-    int grid_tiles;
+    int grid_warp_y;      /* lanes of a warp along y and z */
+    int grid_warp_z;
+    int grid_cta_y;       /* warps of a CTA along y and z */
+    int grid_cta_z;
+    int grid_blocks;      /* CTA-sized blocks of grid lines */
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

@@ -53,8 +53,9 @@ class IluInfo(ctypes.Structure):
                 ("row_lanes_lower", ctypes.c_int), ("row_lanes_upper", ctypes.c_int),
                 ("factor_lane", ctypes.c_int), ("grid_fp64", ctypes.c_int), ("grid_fp32", ctypes.c_int),
                 ("grid_nx", ctypes.c_int),
-                ("grid_ny", ctypes.c_int), ("grid_nz", ctypes.c_int), ("grid_lane_elems", ctypes.c_int),
-                ("grid_tile_lines", ctypes.c_int), ("grid_tile_planes", ctypes.c_int), ("grid_tiles", ctypes.c_int)]
+                ("grid_ny", ctypes.c_int), ("grid_nz", ctypes.c_int), ("grid_warp_y", ctypes.c_int),
+                ("grid_warp_z", ctypes.c_int), ("grid_cta_y", ctypes.c_int), ("grid_cta_z", ctypes.c_int),
+                ("grid_blocks", ctypes.c_int)]
 
 
 class GmresReport(ctypes.Structure):
@@ -69,9 +70,9 @@ ILU_OPT_SOLVE_WARPS = 3
 ILU_OPT_ROW_LANES = 4
 ILU_OPT_WAIT_LIMIT_US = 5
 ILU_OPT_GRID = 6
-ILU_OPT_GRID_LANE_ELEMS = 7
-ILU_OPT_GRID_TILE_LINES = 8
-ILU_OPT_GRID_TILE_PLANES = 9
+ILU_OPT_GRID_WARP_Y = 7
+ILU_OPT_GRID_CTA_Y = 8
+ILU_OPT_GRID_CTA_Z = 9
 ILU_OPT_TICKET_ORDER = 11
 ILU_OPT_FACTOR_KERNEL = 12
 GMRES_OPT_MODE = 1

@@ -171,16 +171,16 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 if (value != -1 && value != 0 && value != 1) throw std::runtime_error("grid sweeps must be -1, 0 or 1");
                 s->impl()->grid_mode = static_cast<int>(value);
                 return 0;
-            case LLJBASH_ILU_OPT_GRID_LANE_ELEMS:
-                if (value != 0 && value != 1 && value != 2 && value != 4)
-                    throw std::runtime_error("grid elements per lane must be 0 (automatic), 1, 2 or 4");
-                s->impl()->grid_elems = static_cast<int>(value);
+            case LLJBASH_ILU_OPT_GRID_WARP_Y:
+                if (value != 0 && value != 1 && value != 4 && value != 8)
+                    throw std::runtime_error("grid lanes of a warp along y must be 0 (automatic), 1, 4 or 8");
+                s->impl()->grid_wy = static_cast<int>(value);
                 return 0;
-            case LLJBASH_ILU_OPT_GRID_TILE_LINES:
-            case LLJBASH_ILU_OPT_GRID_TILE_PLANES:
-                if (value < 0 || value > 1e6 || value != static_cast<int>(value))
-                    throw std::runtime_error("grid tile size must be 0 (automatic) or a positive count");
-                (option == LLJBASH_ILU_OPT_GRID_TILE_LINES ? s->impl()->grid_lines : s->impl()->grid_planes) =
+            case LLJBASH_ILU_OPT_GRID_CTA_Y:
+            case LLJBASH_ILU_OPT_GRID_CTA_Z:
+                if (value < 0 || value > 8 || value != static_cast<int>(value))
+                    throw std::runtime_error("grid warps of a CTA must be 0 (automatic) or 1 .. 8");
+                (option == LLJBASH_ILU_OPT_GRID_CTA_Y ? s->impl()->grid_by : s->impl()->grid_bz) =
                     static_cast<int>(value);
                 return 0;
             default:
@@ -352,16 +352,17 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->row_lanes_lower = im->level_packs ? im->L.group : 0;
     info->row_lanes_upper = im->level_packs ? im->U.group : 0;
     info->factor_lane = im->fact_lane ? 1 : 0;
-    info->grid_fp64 = im->grid64 ? 1 : 0;
-    info->grid_fp32 = im->grid32 ? 1 : 0;
+    info->grid_fp64 = im->line_use64;
+    info->grid_fp32 = im->line_use32;
     if (im->grid64 || im->grid32) {
         info->grid_nx = im->GP.g.nx;
         info->grid_ny = im->GP.g.ny;
         info->grid_nz = im->GP.g.nz;
-        info->grid_lane_elems = im->GP.g.E;
-        info->grid_tile_lines = im->GP.jb;
-        info->grid_tile_planes = im->GP.kc;
-        info->grid_tiles = im->GP.ntile;
+        info->grid_warp_y = im->GP.g.wy;
+        info->grid_warp_z = im->GP.g.wz;
+        info->grid_cta_y = im->GP.g.by;
+        info->grid_cta_z = im->GP.g.bz;
+        info->grid_blocks = im->GP.g.nblk;
     }
     return 0;
 }

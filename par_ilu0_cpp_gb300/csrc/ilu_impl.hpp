@@ -7,7 +7,7 @@
 
 #include "device_util.hpp"
 #include "factor_lane.cuh"
-#include "grid_sweep.cuh"
+#include "line_sweep.cuh"
 #include "ilu_kernels.cuh"
 #include "ilu_solver.hpp"
 #include "mlp_impl.hpp"
@@ -104,42 +104,26 @@ struct BlockPack {
     }
 };
 
-// Structured-grid factor (wavefront-lanes sweeps, grid_sweep.cuh): the sweep layout,
-// the coefficient sources (positions in the factor's value array, -1 where absent) and
-// the gathered coefficients and work vectors per value type.
-struct GridPack {
-    GridLayout g;
-    int jb = 1, kc = 1;       // tile shape
-    int ntile = 0;
-    int threads = 0;          // CTA size: nic * jb warps
-    int grid = 0;             // CTAs to launch
-    size_t smem = 0;          // dynamic shared memory of one CTA (type-dependent)
-    DeviceBuffer<long long> pos;                       // [n] layout position of each row
-    DeviceBuffer<int2> tiles_l, tiles_u;               // tickets -> (tile line, tile plane)
-    DeviceBuffer<int> src_lz, src_ly, src_lx, src_uz, src_uy, src_ux, src_ud;  // [len]
-    DeviceBuffer<double> lz64, ly64, lx64, uz64, uy64, ux64, ud64;
-    DeviceBuffer<float> lz32, ly32, lx32, uz32, uy32, ux32, ud32;
-    DeviceBuffer<double> b64, y64, z64;                 // layout work vectors
-    DeviceBuffer<float> b32, y32, z32;
+// Structured-grid factor (line-pipeline sweeps, line_sweep.cuh): block geometry, ticket
+// order and the packed operand streams of L and U per value type (rebuilt from the factor
+// values after every factorisation).
+struct LinePack {
+    LineGeom g;
+    int threads = 0;  // CTA size: nw warps
+    int grid = 0;     // CTAs launched
+    DeviceBuffer<int> order;        // [nblk] block of each ticket
+    DeviceBuffer<double> l64, u64;  // [4 slots]
+    DeviceBuffer<float> l32, u32;
 
     template <class T>
-    GridTri<T> view(bool upper) const {
-        GridTri<T> p;
+    LineTri<T> view(bool upper) const {
+        LineTri<T> p;
         p.g = g;
-        p.jb = jb;
-        p.kc = kc;
-        p.ntile = ntile;
-        p.tiles = upper ? tiles_u.get() : tiles_l.get();
+        p.order = order.get();
         if constexpr (sizeof(T) == 8) {
-            p.cz = upper ? uz64.get() : lz64.get();
-            p.cy = upper ? uy64.get() : ly64.get();
-            p.cx = upper ? ux64.get() : lx64.get();
-            p.d = upper ? ud64.get() : nullptr;
+            p.coef = upper ? u64.get() : l64.get();
         } else {
-            p.cz = upper ? uz32.get() : lz32.get();
-            p.cy = upper ? uy32.get() : ly32.get();
-            p.cx = upper ? ux32.get() : lx32.get();
-            p.d = upper ? ud32.get() : nullptr;
+            p.coef = upper ? u32.get() : l32.get();
         }
         return p;
     }
@@ -192,14 +176,19 @@ struct IluSolver::Impl {
     gb300::LevelPack LS, US;
     bool levelsync = false;
     int grid_levelsync = 0;
-    // structured-grid sweeps (grid_sweep.cuh) per value type, when the factor is a 7- or
-    // 5-point stencil in natural order and grid_mode allows it
-    gb300::GridPack GP;
+    // structured-grid line-pipeline sweeps (line_sweep.cuh) per value type, when the
+    // factor is a 7- or 5-point stencil in natural order and grid_mode allows it
+    gb300::LinePack GP;
     bool grid64 = false, grid32 = false;
-    int grid_mode = 0;       // 1: on when the pattern qualifies; 0 (automatic) and -1: off
-    int grid_elems = 0;      // requested elements per lane (0 automatic: 1)
-    int grid_lines = 0;      // requested lines per tile (0 automatic)
-    int grid_planes = 0;     // requested planes per tile (0 automatic)
+    int grid_mode = 0;  // 1 or 0 (automatic): on when the pattern qualifies; -1: off
+    int grid_wy = 0;    // requested lanes of a warp along y (0 automatic)
+    int grid_by = 0;    // requested warps of a CTA along y (0 automatic)
+    int grid_bz = 0;    // requested warps of a CTA along z (0 automatic)
+    // line-pipeline sweeps in use per value type (bit 0: forward, bit 1: backward); in
+    // automatic mode chosen at the first Factorize after SetupMatrix by timing each sweep
+    // against the block-local / level-ordered kernel
+    int line_use64 = 0, line_use32 = 0;
+    bool line_tuned = true;
     unsigned setup_gen = 0;    // incremented by every SetupMatrix
     gb300::DeviceBuffer<double> sb64, sy64, sx64;  // Substitute() work vectors
     gb300::DeviceBuffer<float> sy32;               // FP32 forward-sweep intermediate

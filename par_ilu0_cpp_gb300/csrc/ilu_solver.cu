@@ -766,7 +766,7 @@ static void fill_sentinel(T* p, long long n, cudaStream_t s, int sms) {
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
-// ---- structured-grid sweeps (grid_sweep.cuh) ------------------------------------
+// ---- structured-grid line-pipeline sweeps (line_sweep.cuh) ----------------------
 // Grid shape of a factor pattern that is a full 7-point (3-D) or 5-point (2-D) stencil
 // in natural order: strict-lower columns of row r = i + nx j + nx ny k exactly
 // {r - nx ny (k > 0), r - nx (j > 0), r - 1 (i > 0)} and strict-upper columns exactly
@@ -817,178 +817,166 @@ static bool detect_grid(int n, const int* rp, const int* ci, const std::vector<i
     return true;
 }
 
-// Tickets of the tile grid in dependency order: anti-diagonals d = tile line + tile
-// plane ascending (lower) or descending with each diagonal reversed (upper).
-static std::vector<int2> grid_tile_order(int tj, int tk, bool upper) {
-    std::vector<int2> t;
-    t.reserve(static_cast<size_t>(tj) * tk);
-    for (int d = 0; d < tj + tk - 1; ++d)
-        for (int a = 0; a < tj; ++a) {
-            const int b = d - a;
-            if (b >= 0 && b < tk) t.push_back(make_int2(a, b));
-        }
-    if (upper) std::reverse(t.begin(), t.end());
-    return t;
-}
-
-// Builds the sweep layout, the coefficient sources and the tile schedule of a factor
-// that detect_grid accepted.  Tile shape: lines per tile (nic warps each, at most
-// kGridMaxWarps warps per CTA) and planes per tile such that there are about as many
-// tiles as SMs; `elems`, `lines`, `planes` override (0 = automatic).
-static void build_grid_pack(int n, const int* rp, const int* ci, const std::vector<int>& diag, int nx, int ny, int nz,
-                            int elems, int lines, int planes, int sms, GridPack& G, cudaStream_t s) {
-    GridLayout& g = G.g;
+// Block geometry of the line-pipeline sweeps: lanes of a warp along y (wy, and
+// wz = 32 / wy along z; a 2-D grid, ny = 1, has wy = 1) and warps of a CTA along y and z
+// (by, bz).  Requested values (0 = automatic) are clamped to what the grid allows.
+static LineGeom line_geometry(int nx, int ny, int nz, int wy_req, int by_req, int bz_req) {
+    LineGeom g;
     g.nx = nx;
     g.ny = ny;
     g.nz = nz;
-    g.E = elems > 0 ? elems : 1;
-    g.nic = ceil_div(nx, 32 * g.E);
-    g.len = (static_cast<long long>(ny) * g.nic * nz + 31) * 32 * g.E;
-    const int max_lines = std::max(1, kGridMaxWarps / g.nic);
-    G.jb = lines > 0 ? std::min(lines, max_lines) : std::min(ny, max_lines);
-    G.jb = std::max(1, std::min(G.jb, ny));
-    const int tj = ceil_div(ny, G.jb);
-    int tk = std::max(1, std::min(nz, (sms + tj / 2) / std::max(1, tj)));
-    G.kc = planes > 0 ? std::min(planes, nz) : ceil_div(nz, tk);
-    tk = ceil_div(nz, G.kc);
-    G.ntile = tj * tk;
-    G.threads = g.nic * G.jb * kWarp;
-    std::vector<long long> pos(static_cast<size_t>(n));
-    const long long len = g.len;
-    std::vector<int> lz(len, -1), ly(len, -1), lx(len, -1), uz(len, -1), uy(len, -1), ux(len, -1), ud(len, -1);
-    const int P = nx * ny;
-    for (int r = 0; r < n; ++r) {
-        const int i = r % nx, j = (r / nx) % ny, k = r / P;
-        const long long p = g.pos(i, j, k);
-        pos[static_cast<size_t>(r)] = p;
-        int t = rp[r];
-        if (k > 0) lz[p] = t++;
-        if (ny > 1 && j > 0) ly[p] = t++;
-        if (i > 0) lx[p] = t++;
-        t = diag[r];
-        ud[p] = t++;
-        if (i < nx - 1) ux[p] = t++;
-        if (ny > 1 && j < ny - 1) uy[p] = t++;
-        if (k < nz - 1) uz[p] = t++;
+    // lanes along y: 8 (default) or the requested 1 / 4; a 2-D grid has 1
+    int wy = 1;
+    if (ny > 1) {
+        wy = wy_req > 0 ? wy_req : (ny > 4 ? 8 : 4);
+        if (wy != 1 && wy != 4 && wy != 8) wy = 8;
     }
-    G.pos.upload(pos.data(), pos.size(), s);
-    G.src_lz.upload(lz.data(), lz.size(), s);
-    G.src_ly.upload(ly.data(), ly.size(), s);
-    G.src_lx.upload(lx.data(), lx.size(), s);
-    G.src_uz.upload(uz.data(), uz.size(), s);
-    G.src_uy.upload(uy.data(), uy.size(), s);
-    G.src_ux.upload(ux.data(), ux.size(), s);
-    G.src_ud.upload(ud.data(), ud.size(), s);
-    const std::vector<int2> tl = grid_tile_order(tj, tk, false), tu = grid_tile_order(tj, tk, true);
-    G.tiles_l.upload(tl.data(), tl.size(), s);
-    G.tiles_u.upload(tu.data(), tu.size(), s);
-    // host vectors must outlive the asynchronous copies
-    GB_CUDA_CHECK(cudaStreamSynchronize(s));
-}
-
-template <class T>
-static size_t grid_smem_bytes(const GridPack& G) {
-    const size_t nw = static_cast<size_t>(G.threads / kWarp);
-    return nw * (static_cast<size_t>(kGridRingY) * 32 * G.g.E + kGridRingX) * sizeof(T) + nw * sizeof(int);
-}
-
-template <class T, bool UPPER>
-static auto grid_kernel_for(int E) {
-    switch (E) {
-        case 1: return sptrsv_grid_kernel<T, UPPER, 1>;
-        case 2: return sptrsv_grid_kernel<T, UPPER, 2>;
-        case 4: return sptrsv_grid_kernel<T, UPPER, 4>;
-        default: throw std::runtime_error("grid sweep: elements per lane must be 1, 2 or 4");
+    g.wy = wy;
+    g.wz = 32 / wy;
+    const int wly = ceil_div(ny, g.wy), wlz = ceil_div(nz, g.wz);  // warps along y / z
+    int by = ny > 1 ? (by_req > 0 ? by_req : 2) : 1;
+    int bz = bz_req > 0 ? bz_req : (ny > 1 ? 2 : 8);
+    by = std::max(1, std::min(by, wly));
+    bz = std::max(1, std::min(bz, wlz));
+    if (ny > 1) {  // the halo warp holds one line of each incoming face per lane
+        by = std::min(by, std::max(1, 32 / g.wy));
+        bz = std::min(bz, std::max(1, 32 / g.wz));
     }
+    while (by * bz > kLineMaxWarps) (bz > by ? bz : by) /= 2;
+    g.by = by;
+    g.bz = bz;
+    g.nby = ceil_div(wly, by);
+    g.nbz = ceil_div(wlz, bz);
+    g.nblk = g.nby * g.nbz;
+    g.steps = nx + g.wy + g.wz - 2;
+    return g;
 }
 
-// Allocates the coefficient arrays and work vectors of value type T, raises the
-// kernels' shared-memory limit and sizes the grid; false when a CTA cannot be resident.
+// Tickets of the block grid in dependency order: anti-diagonals iy + iz ascending (the
+// same in the sweep coordinates of L and U).
+static std::vector<int> line_block_order(const LineGeom& g) {
+    std::vector<int> o;
+    o.reserve(static_cast<size_t>(g.nblk));
+    for (int d = 0; d < g.nby + g.nbz - 1; ++d)
+        for (int iz = 0; iz < g.nbz; ++iz) {
+            const int iy = d - iz;
+            if (iy >= 0 && iy < g.nby) o.push_back(iy + g.nby * iz);
+        }
+    return o;
+}
+
+// Raises the kernels' shared-memory limit, sizes the grid and allocates the packed
+// operands of value type T; false when a CTA cannot be resident.
 template <class T>
-static bool configure_grid(GridPack& G, int sms, size_t smem_optin, cudaStream_t s) {
-    const size_t smem = grid_smem_bytes<T>(G);
-    if (smem > smem_optin) return false;
+static bool configure_line(LinePack& G, const DeviceInfo& dev) {
+    const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
+    if (smem + 1024 > static_cast<size_t>(dev.smem_optin)) return false;
     int per_sm = 0;
     for (bool upper : {false, true}) {
-        auto kern = upper ? grid_kernel_for<T, true>(G.g.E) : grid_kernel_for<T, false>(G.g.E);
+        const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_kernel<T, true>)
+                                 : reinterpret_cast<const void*>(sptrsv_line_kernel<T, false>);
         GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
         int r = 0;
         GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, G.threads, smem));
         if (r < 1) return false;
         per_sm = per_sm == 0 ? r : std::min(per_sm, r);
     }
-    G.grid = std::min(G.ntile, per_sm * sms);
-    const size_t len = static_cast<size_t>(G.g.len);
+    G.grid = std::min(G.g.nblk, per_sm * dev.sms);
+    const size_t len = static_cast<size_t>(G.g.slots()) * 4;
     if constexpr (sizeof(T) == 8) {
-        for (auto* b : {&G.lz64, &G.ly64, &G.lx64, &G.uz64, &G.uy64, &G.ux64, &G.ud64, &G.b64}) b->reserve(len);
-        G.y64.reserve(len);
-        G.z64.reserve(len);
-        fill_sentinel(G.y64.get(), static_cast<long long>(len), s, sms);
-        fill_sentinel(G.z64.get(), static_cast<long long>(len), s, sms);
+        G.l64.reserve(len);
+        G.u64.reserve(len);
     } else {
-        for (auto* b : {&G.lz32, &G.ly32, &G.lx32, &G.uz32, &G.uy32, &G.ux32, &G.ud32, &G.b32}) b->reserve(len);
-        G.y32.reserve(len);
-        G.z32.reserve(len);
-        fill_sentinel(G.y32.get(), static_cast<long long>(len), s, sms);
-        fill_sentinel(G.z32.get(), static_cast<long long>(len), s, sms);
+        G.l32.reserve(len);
+        G.u32.reserve(len);
     }
     return true;
 }
 
-// Gathers the factor values into the coefficient arrays of type T.
+// Packs the factor values into the operand streams of type T.
 template <class T>
-static void gather_grid(GridPack& G, const double* lu, cudaStream_t s, int sms) {
-    const long long len = G.g.len;
+static void pack_line(LinePack& G, const int* rp, const int* diag, const double* lu, cudaStream_t s, int sms) {
+    const long long slots = G.g.slots();
     const int threads = 256;
-    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(len, threads), 8LL * sms)));
-    const bool f64 = sizeof(T) == 8;
-    T* dst[7];
-    if constexpr (sizeof(T) == 8) {
-        T* d[7] = {G.lz64.get(), G.ly64.get(), G.lx64.get(), G.uz64.get(), G.uy64.get(), G.ux64.get(), G.ud64.get()};
-        std::copy(d, d + 7, dst);
-    } else {
-        T* d[7] = {G.lz32.get(), G.ly32.get(), G.lx32.get(), G.uz32.get(), G.uy32.get(), G.ux32.get(), G.ud32.get()};
-        std::copy(d, d + 7, dst);
-    }
-    const int* src[7] = {G.src_lz.get(), G.src_ly.get(), G.src_lx.get(), G.src_uz.get(),
-                         G.src_uy.get(), G.src_ux.get(), G.src_ud.get()};
-    for (int a = 0; a < 7; ++a)
-        grid_coef_kernel<T><<<grid, threads, 0, s>>>(len, src[a], lu, dst[a], a == 6 && !f64);
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(slots, threads), 8LL * sms)));
+    T* l = sizeof(T) == 8 ? reinterpret_cast<T*>(G.l64.get()) : reinterpret_cast<T*>(G.l32.get());
+    T* u = sizeof(T) == 8 ? reinterpret_cast<T*>(G.u64.get()) : reinterpret_cast<T*>(G.u32.get());
+    line_pack_kernel<T, false><<<grid, threads, 0, s>>>(G.g, rp, diag, lu, l);
+    line_pack_kernel<T, true><<<grid, threads, 0, s>>>(G.g, rp, diag, lu, u);
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
 template <class T, bool UPPER>
-static void launch_grid(const GridPack& G, cudaStream_t s, const T* in, T* out, unsigned* counter, int* status,
-                        const int* gate, int step) {
-    auto kern = grid_kernel_for<T, UPPER>(G.g.E);
-    kern<<<G.grid, G.threads, grid_smem_bytes<T>(G), s>>>(G.view<T>(UPPER), in, out, counter, status, gate, step);
+static void launch_line(const LinePack& G, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
+                        int* status, const int* gate, int step) {
+    const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
+    sptrsv_line_kernel<T, UPPER><<<G.grid, G.threads, smem, s>>>(G.view<T>(UPPER), in, scale, out, counter, status,
+                                                                  gate, step);
     GB_CUDA_CHECK(cudaGetLastError());
 }
-
-template <class T>
-static void launch_grid_gather(const GridPack& G, int n, cudaStream_t s, T* in, const double* scale, T* lay, T* reset,
-                               const int* gate, int step, int sms) {
-    const int threads = 256;
-    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(n, threads), 8LL * sms)));
-    grid_gather_kernel<T><<<grid, threads, 0, s>>>(n, G.pos.get(), in, scale, lay, reset, gate, step);
-    GB_CUDA_CHECK(cudaGetLastError());
-}
-
-template <class T>
-static void launch_grid_scatter(const GridPack& G, int n, cudaStream_t s, T* lay, T* out, const int* gate, int step,
-                                int sms) {
-    const int threads = 256;
-    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(n, threads), 8LL * sms)));
-    grid_scatter_kernel<T><<<grid, threads, 0, s>>>(n, G.pos.get(), lay, out, gate, step);
-    GB_CUDA_CHECK(cudaGetLastError());
-}
-
 
 }  // namespace gb300
 
 namespace lljbash {
 
 using namespace gb300;
+
+// Automatic choice of the line-pipeline sweeps (structured-grid factors): each sweep of
+// each value type is timed (CUDA events, second of two runs, right-hand side of ones, the
+// factors just computed) with the line kernel and with the block-local / level-ordered
+// kernel, and the faster is kept.  Both give the same results; only the time differs.
+template <class T>
+static int tune_line_sweeps(IluSolver::Impl& im, int& use, T* b, T* y, T* x, cudaStream_t s) {
+    const int n = im.n;
+    const int threads = 256;
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div<long long>(n, threads), 8LL * im.dev.sms)));
+    line_fill_kernel<T><<<grid, threads, 0, s>>>(n, b, T(1));
+    cudaEvent_t e0, e1;
+    GB_CUDA_CHECK(cudaEventCreate(&e0));
+    GB_CUDA_CHECK(cudaEventCreate(&e1));
+    int launches = 1;
+    float best[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [sweep][0: other, 1: line]
+    for (int sweep = 0; sweep < 2; ++sweep)
+        for (int cand = 0; cand < 2; ++cand) {
+            use = cand ? (sweep ? 2 : 1) : 0;
+            for (int rep = 0; rep < 2; ++rep) {
+                if (sweep == 0) {
+                    fill_sentinel(y, n, s, im.dev.sms);
+                    GB_CUDA_CHECK(cudaEventRecord(e0, s));
+                    im.launch_lower<T>(s, b, nullptr, y, nullptr, 0);
+                } else {
+                    fill_sentinel(x, n, s, im.dev.sms);
+                    GB_CUDA_CHECK(cudaEventRecord(e0, s));
+                    im.launch_upper<T>(s, y, x, nullptr, 0);
+                }
+                GB_CUDA_CHECK(cudaEventRecord(e1, s));
+                GB_CUDA_CHECK(cudaEventSynchronize(e1));
+                GB_CUDA_CHECK(cudaEventElapsedTime(&best[sweep][cand], e0, e1));
+                launches += 2;
+            }
+        }
+    GB_CUDA_CHECK(cudaEventDestroy(e0));
+    GB_CUDA_CHECK(cudaEventDestroy(e1));
+    use = (best[0][1] < best[0][0] ? 1 : 0) | (best[1][1] < best[1][0] ? 2 : 0);
+    return launches;
+}
+
+static void tune_line(IluSolver::Impl& im, cudaStream_t s) {
+    const size_t nv = static_cast<size_t>(std::max(im.n, 1));
+    if (im.grid64) im.launches += tune_line_sweeps<double>(im, im.line_use64, im.sb64.get(), im.sy64.get(), im.sx64.get(), s);
+    if (im.grid32) {
+        DeviceBuffer<float> b32, x32;
+        b32.reserve(nv);
+        x32.reserve(nv);
+        im.launches += tune_line_sweeps<float>(im, im.line_use32, b32.get(), im.sy32.get(), x32.get(), s);
+        // the FP32 forward-sweep vector is back at the sentinel for its next user
+        fill_sentinel(im.sy32.get(), static_cast<long long>(nv), s, im.dev.sms);
+        GB_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
+    fill_sentinel(im.sy64.get(), static_cast<long long>(nv), s, im.dev.sms);
+    im.line_tuned = true;
+    im.check_status(s);
+}
 
 IluSolver::Impl::~Impl() {
     if (ev0) cudaEventDestroy(ev0);
@@ -1002,13 +990,8 @@ void IluSolver::Impl::launch_lower(cudaStream_t s, T* b, const double* scale, T*
         launch_levelsync<T, false>(LS, grid_levelsync, s, b, scale, y, counters.get() + 4, status.get(), gate, step);
         return;
     }
-    if (sizeof(T) == 8 ? grid64 : grid32) {
-        // b (natural order, rescaled in place) -> layout; the forward sweep's layout output
-        // reset to the sentinel in the same pass; `y` is not used
-        T* lb = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.b64.get()) : reinterpret_cast<T*>(GP.b32.get());
-        T* ly = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.y64.get()) : reinterpret_cast<T*>(GP.y32.get());
-        launch_grid_gather<T>(GP, n, s, b, scale, lb, ly, gate, step, dev.sms);
-        launch_grid<T, false>(GP, s, lb, ly, counters.get() + 1, status.get(), gate, step);
+    if ((sizeof(T) == 8 ? line_use64 : line_use32) & 1) {
+        launch_line<T, false>(GP, s, b, scale, y, counters.get() + 1, status.get(), gate, step);
         return;
     }
     if (sizeof(T) == 8 ? blk64 : blk32) {
@@ -1026,13 +1009,8 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
         launch_levelsync<T, true>(US, grid_levelsync, s, y, nullptr, x, counters.get() + 4, status.get(), gate, step);
         return;
     }
-    if (sizeof(T) == 8 ? grid64 : grid32) {
-        // layout output of the forward sweep -> backward sweep -> x (natural order); the
-        // layout output is reset to the sentinel by the scatter; `y` is not used
-        T* ly = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.y64.get()) : reinterpret_cast<T*>(GP.y32.get());
-        T* lz = sizeof(T) == 8 ? reinterpret_cast<T*>(GP.z64.get()) : reinterpret_cast<T*>(GP.z32.get());
-        launch_grid<T, true>(GP, s, ly, lz, counters.get() + 2, status.get(), gate, step);
-        launch_grid_scatter<T>(GP, n, s, lz, x, gate, step, dev.sms);
+    if ((sizeof(T) == 8 ? line_use64 : line_use32) & 2) {
+        launch_line<T, true>(GP, s, y, nullptr, x, counters.get() + 2, status.get(), gate, step);
         return;
     }
     if (sizeof(T) == 8 ? blk64 : blk32) {
@@ -1047,8 +1025,8 @@ void IluSolver::Impl::launch_upper(cudaStream_t s, T* y, T* x, const int* gate, 
 template <class T>
 const void* IluSolver::Impl::subst_key() const {
     if (levelsync) return LS.cols.get();
-    if (sizeof(T) == 8 ? grid64 : grid32)
-        return sizeof(T) == 8 ? static_cast<const void*>(GP.lz64.get()) : static_cast<const void*>(GP.lz32.get());
+    if (const int bits = sizeof(T) == 8 ? line_use64 : line_use32; bits != 0)  // the schedule is part of the key
+        return (sizeof(T) == 8 ? reinterpret_cast<const char*>(GP.l64.get()) : reinterpret_cast<const char*>(GP.l32.get())) + bits;
     if (sizeof(T) == 8 ? blk64 : blk32) return (sizeof(T) == 8 ? LB64 : LB32).codes.get();
     return L.cols.get();
 }
@@ -1158,8 +1136,39 @@ void IluSolver::SetupMatrix() {
     GB_CUDA_CHECK(cudaMemsetAsync(im.status.get(), 0, sizeof(int) * kStatusWords, s));
     im.push_wait_limit();
     ++im.setup_gen;
+    // structured-grid line-pipeline sweeps: 7- / 5-point stencil factors in natural order
+    // (automatic, grid_mode 0: when the other schedules are automatic too; 1: always)
+    im.grid64 = im.grid32 = false;
+    if (im.grid_mode == 1 || (im.grid_mode == 0 && im.block_rows == 0)) {
+        int gx = 0, gy = 0, gz = 0;
+        if (detect_grid(n, rp, ci, im.an.diag, gx, gy, gz)) {
+            // the requested (or automatic) CTA shape, halved along its longer side until
+            // the FP64 kernels' shared memory fits
+            int by = im.grid_by, bz = im.grid_bz;
+            for (int attempt = 0; attempt < 8; ++attempt) {
+                im.GP.g = line_geometry(gx, gy, gz, im.grid_wy, by, bz);
+                im.GP.threads = (im.GP.g.nw() + 1) * kWarp;  // compute warps + the halo warp
+                im.grid64 = configure_line<double>(im.GP, im.dev);
+                if (im.grid64 || im.GP.g.nw() == 1) break;
+                by = im.GP.g.by;
+                bz = im.GP.g.bz;
+                (bz >= by ? bz : by) = std::max(1, (bz >= by ? bz : by) / 2);
+            }
+            im.grid32 = configure_line<float>(im.GP, im.dev);
+            const std::vector<int> order = line_block_order(im.GP.g);
+            im.GP.order.upload(order.data(), order.size(), s);
+            GB_CUDA_CHECK(cudaStreamSynchronize(s));  // `order` must outlive the copy
+        }
+    }
+    // forced (grid_mode 1): every sweep of a configured type; automatic: timed against the
+    // other schedules at the first Factorize (tune_line_sweeps)
+    const bool line_forced = im.grid_mode == 1;
+    im.line_use64 = line_forced && im.grid64 ? 3 : 0;
+    im.line_use32 = line_forced && im.grid32 ? 3 : 0;
+    im.line_tuned = line_forced || !(im.grid64 || im.grid32);
+    const bool grid_both = line_forced && im.grid64 && im.grid32;
     im.blk64 = im.blk32 = false;
-    if (im.block_rows >= 0) {
+    if (im.block_rows >= 0 && !grid_both) {
         // block-local schedule: an explicit block size, or (0) the one the cost model
         // picks per value type; a type whose block does not fit in shared memory, or for
         // which the model prefers the level-ordered kernel, keeps the level kernel
@@ -1200,7 +1209,7 @@ void IluSolver::SetupMatrix() {
             (elem == 8 ? im.blk64 : im.blk32) = true;
         }
     }
-    im.levelsync = im.block_rows == -2;
+    im.levelsync = im.block_rows == -2 && !grid_both;
     if (im.levelsync) {
         build_levelsync_pack(n, rp, ci, im.an.diag, im.an.order_l, im.an.lptr_l, im.an.nlev_l, true, im.LS, s);
         build_levelsync_pack(n, rp, ci, im.an.diag, im.an.order_u, im.an.lptr_u, im.an.nlev_u, false, im.US, s);
@@ -1219,7 +1228,7 @@ void IluSolver::SetupMatrix() {
         if (per_sm < 1) throw std::runtime_error("level-synchronous kernel cannot be resident");
         im.grid_levelsync = std::min(per_sm, 2) * im.dev.sms;
     }
-    im.level_packs = !(im.blk64 && im.blk32);
+    im.level_packs = !((im.blk64 || (line_forced && im.grid64)) && (im.blk32 || (line_forced && im.grid32)));
     if (im.level_packs) {
         int kl = 0, ku = 0;
         for (int r = 0; r < n; ++r) {
@@ -1228,20 +1237,6 @@ void IluSolver::SetupMatrix() {
         }
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_l, true, row_lanes_for(kl, im.row_lanes), im.L, s);
         build_level_pack(n, rp, ci, im.an.diag, im.an.order_u, false, row_lanes_for(ku, im.row_lanes), im.U, s);
-    }
-    // structured-grid sweeps: 7- / 5-point stencil factors in natural order
-    im.grid64 = im.grid32 = false;
-    // (automatic = off: on GB300 the block-local / cluster kernels measure faster on the
-    // stencil grids tried so far; the grid schedule runs when requested)
-    if (im.grid_mode > 0) {
-        int gx = 0, gy = 0, gz = 0;
-        if (detect_grid(n, rp, ci, im.an.diag, gx, gy, gz)) {
-            build_grid_pack(n, rp, ci, im.an.diag, gx, gy, gz, im.grid_elems, im.grid_lines, im.grid_planes,
-                            im.dev.sms, im.GP, s);
-            const size_t optin = static_cast<size_t>(im.dev.smem_optin);
-            im.grid64 = configure_grid<double>(im.GP, im.dev.sms, optin, s);
-            im.grid32 = configure_grid<float>(im.GP, im.dev.sms, optin, s);
-        }
     }
     const size_t nv = static_cast<size_t>(std::max(n, 1));
     im.sb64.reserve(nv);
@@ -1390,12 +1385,12 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
                 im.launches += 6;
             }
             if (im.grid64) {
-                gather_grid<double>(im.GP, im.lu.get(), s, im.dev.sms);
-                im.launches += 7;
+                pack_line<double>(im.GP, im.rp.get(), im.diag.get(), im.lu.get(), s, im.dev.sms);
+                im.launches += 2;
             }
             if (im.grid32) {
-                gather_grid<float>(im.GP, im.lu.get(), s, im.dev.sms);
-                im.launches += 7;
+                pack_line<float>(im.GP, im.rp.get(), im.diag.get(), im.lu.get(), s, im.dev.sms);
+                im.launches += 2;
             }
         }
         GB_CUDA_CHECK(cudaEventRecord(im.ev1, s));
@@ -1420,6 +1415,7 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
         h = factor_once(0);
         im.shift_applied = false;
     }
+    if (!im.line_tuned) tune_line(im, s);
     if (!on_device && im.copy_back && im.nnz > 0) {
         GB_CUDA_CHECK(cudaMemcpyAsync(aMatrix_.value, im.lu.get(), sizeof(double) * static_cast<size_t>(im.nnz),
                                       cudaMemcpyDeviceToHost, s));

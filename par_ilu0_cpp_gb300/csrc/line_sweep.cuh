@@ -1,0 +1,482 @@
+// Structured-grid triangular substitution: the line pipeline.
+//
+// For factors whose strict-lower part couples row r = X + nx (Y + ny Z) only to rows
+// r - 1 (X > 0), r - nx (Y > 0) and r - nx ny (Z > 0) — a 7-point (3-D) or 5-point (2-D:
+// ny = 1, the second offset taken as the plane offset) stencil in natural order, ILU(0) —
+// and whose strict-upper part is the mirror image, every row depends on its three
+// predecessors along x, y and z.  The sweeps then run on a fixed software pipeline
+// instead of level sets:
+//
+// * in sweep coordinates (x', y', z') — the natural ones for L, mirrored for U — a lane
+//   owns one grid line (y', z') and walks it in x', so the x-dependency is the lane's
+//   own previous result, in a register;
+// * a warp holds wy x wz lines (lane = zz wy + yy) and lane (yy, zz) works on
+//   x' = s - (yy + zz) at step s: its y- and z-predecessors at the same x' were computed
+//   by lanes (yy - 1, zz) and (yy, zz - 1) one step earlier and arrive by warp shuffles;
+// * a CTA holds by x bz warps; a warp's first lanes along y / z take their predecessors
+//   from the previous warp's face in shared memory ([nx][wz] / [nx][wy] values per
+//   warp, written once per block, value-as-flag: reset to the sentinel with the block);
+// * a block's first warps take them from the previous block through `out` in L2,
+//   loaded PF steps ahead and polled only while they still hold the sentinel.
+//
+// The per-step work of a lane is one row: three FMAs (z, y, x terms in the reference's
+// order) and, for U, the division by u_ii (FP64) or the product with the rounded
+// reciprocal (FP32, as the other FP32 kernels).  The operands of each step (coefficients
+// in a packed stream per warp, right-hand side) are loaded PF steps before use.  The
+// critical path is nx + ny + nz steps plus the handoffs between warps and blocks,
+// against one level per step for the level-set kernels.
+//
+// Blocks are taken from a ticket counter in dependency order (anti-diagonals of the block
+// grid), so a block only waits for blocks of smaller tickets, whose CTAs are running or
+// done; inside a block a warp only waits for warps of smaller index along y or z (all
+// resident), whose faces never wait on their consumers.  Every wait is bounded.
+//
+// A missing neighbour at the grid's boundary has coefficient 0 and value 0, and
+// fma(-0, 0, acc) == acc exactly, so the results are bit-identical to the level-ordered
+// and block-local kernels (src/ilu_solver.cpp:687-696 for L, 719-729 for U).
+#pragma once
+
+#include "common.cuh"
+#include "ilu_kernels.cuh"
+
+namespace gb300 {
+
+constexpr int kLineMaxWarps = 8;  // compute warps per CTA of the line kernels (plus one halo warp)
+
+struct LineGeom {
+    int nx = 0, ny = 0, nz = 0;
+    int wy = 1, wz = 32;  // lanes of a warp along y / z (wy * wz == 32)
+    int by = 1, bz = 1;   // warps of a CTA along y / z
+    int nby = 1, nbz = 1; // blocks along y / z
+    int steps = 0;        // steps of a warp: nx + wy + wz - 2
+    int nblk = 0;         // nby * nbz
+    __host__ __device__ int nw() const { return by * bz; }
+    // Slot of lane `lane` of warp w of block b at step s in the packed operand stream.
+    __host__ __device__ long long slot(int b, int w, int s, int lane) const {
+        return ((static_cast<long long>(b) * nw() + w) * steps + s) * 32 + lane;
+    }
+    __host__ __device__ long long slots() const { return static_cast<long long>(nblk) * nw() * steps * 32; }
+};
+
+template <class T>
+struct LineTri {
+    LineGeom g;
+    const int* order = nullptr;  // [nblk] block (iy + nby iz, sweep coordinates) of each ticket
+    const T* coef = nullptr;     // [slots][4]: c_z, c_y, c_x, d (d: u_ii FP64 / RN(1 / u_ii) FP32; L: unused)
+};
+
+// ---- asynchronous global -> shared copies (cp.async, per thread) ----
+// src_bytes = 0 fills the destination with zeros without reading the source.
+__device__ __forceinline__ void cp_async_16(void* smem, const void* gmem, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_8(void* smem, const void* gmem, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_4(void* smem, const void* gmem, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Stores issued only where `on` holds, as predicated instructions (no branch).
+__device__ __forceinline__ void st_relaxed_if(bool on, double* p, double v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.relaxed.gpu.global.f64 [%1], %2; }" ::"r"(static_cast<unsigned>(on)),
+                 "l"(p), "d"(v));
+}
+__device__ __forceinline__ void st_relaxed_if(bool on, float* p, float v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.relaxed.gpu.global.f32 [%1], %2; }" ::"r"(static_cast<unsigned>(on)),
+                 "l"(p), "f"(v));
+}
+__device__ __forceinline__ void st_global_if(bool on, double* p, double v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.global.f64 [%1], %2; }" ::"r"(static_cast<unsigned>(on)), "l"(p),
+                 "d"(v));
+}
+__device__ __forceinline__ void st_global_if(bool on, float* p, float v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.global.f32 [%1], %2; }" ::"r"(static_cast<unsigned>(on)), "l"(p),
+                 "f"(v));
+}
+__device__ __forceinline__ void st_shared_if(bool on, double* p, double v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.volatile.shared.f64 [%1], %2; }" ::"r"(static_cast<unsigned>(on)),
+                 "r"(static_cast<unsigned>(__cvta_generic_to_shared(p))), "d"(v));
+}
+__device__ __forceinline__ void st_shared_if(bool on, float* p, float v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.volatile.shared.f32 [%1], %2; }" ::"r"(static_cast<unsigned>(on)),
+                 "r"(static_cast<unsigned>(__cvta_generic_to_shared(p))), "f"(v));
+}
+
+// Waits (bounded) until the shared-memory value *p is no longer the sentinel; after many
+// polls it sleeps between polls (a warp waiting for a block far behind).
+template <class T>
+__device__ __noinline__ T line_wait_shared(const T* p, int* status) {
+    T v = ld_volatile_shared(p);
+    WaitBudget wb;
+    int polls = 0;
+    while (Sentinel<T>::is(v)) {
+        if (wb.expired(status)) {
+            atomicExch(status + kStatusTimeout, 1);
+            return T(0);
+        }
+        if (++polls > 4096) __nanosleep(256);  // a long wait (a block far behind)
+        v = ld_volatile_shared(p);
+    }
+    return v;
+}
+
+// Coefficients of one row in the packed stream (c_z, c_y, c_x, d).
+template <class T>
+struct alignas(4 * sizeof(T)) LineCoef {
+    T cz, cy, cx, d;
+};
+
+// Steps of operands in flight per lane (cp.async ring in shared memory).
+template <class T>
+constexpr int kLineRing = sizeof(T) == 4 ? 16 : 8;
+
+// Shared memory of a CTA: faces (consumer-indexed: slot w holds what warp w reads; faceY
+// [nw][nx][wz] when ny > 1, faceZ [nw][nx][wy]), one word holding 0, then the operand
+// rings [R][nw * 32] of coefficients and of right-hand side values.
+__host__ __device__ inline long long line_face_slot_y(const LineGeom& g) {
+    return g.ny > 1 ? static_cast<long long>(g.nx) * g.wz : 0;
+}
+__host__ __device__ inline long long line_face_slot_z(const LineGeom& g) { return static_cast<long long>(g.nx) * g.wy; }
+template <class T>
+__host__ __device__ inline long long line_face_len(const LineGeom& g) {
+    return static_cast<long long>(g.nw()) * (line_face_slot_y(g) + line_face_slot_z(g));
+}
+template <class T>
+__host__ __device__ inline long long line_ring_offset(const LineGeom& g) {
+    return ((line_face_len<T>(g) + 1) * static_cast<long long>(sizeof(T)) + 15) & ~15ll;
+}
+template <class T>
+__host__ __device__ inline long long line_smem_bytes(const LineGeom& g) {
+    return line_ring_offset<T>(g) +
+           static_cast<long long>(kLineRing<T>) * g.nw() * 32 * (static_cast<long long>(sizeof(LineCoef<T>)) + sizeof(T));
+}
+
+// One compute warp's share of block `blk`: wy x wz lines over nx + wy + wz - 2 steps.
+// faceY / faceZ: slot w holds the y / z predecessors of warp w's first lanes along y / z,
+// written by the previous warp of the CTA or by the halo warp (previous block), or zeros
+// at the grid's boundary.
+template <class T, bool UPPER>
+__device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, bool scaled, T sc, T* out, T* faceY,
+                                          T* faceZ, const T* zero_word, LineCoef<T>* cring, T* bring, int* status) {
+    constexpr int R = kLineRing<T>;
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nx = P.g.nx, ny = P.g.ny, nz = P.g.nz;
+    const int wy = P.g.wy, wz = P.g.wz, by = P.g.by, bz = P.g.bz;
+    const int nw = by * bz;
+    const int wyi = w % by, wzi = w / by;
+    const int yy = lane % wy, zz = lane / wy;
+    const int iy = blk % P.g.nby, iz = blk / P.g.nby;
+    const int yq = (iy * by + wyi) * wy + yy;  // sweep coordinates of the lane's line
+    const int zq = (iz * bz + wzi) * wz + zz;
+    const bool line_ok = yq < ny && zq < nz;
+    const int skew = yy + zz;
+    const int steps = P.g.steps;
+    const long long plane = static_cast<long long>(nx) * ny;
+    const long long Y = UPPER ? ny - 1 - yq : yq;
+    const long long Z = UPPER ? nz - 1 - zq : zq;
+    const int sx = UPPER ? -1 : 1;
+    T* const in0 = in + ((UPPER ? nx - 1 : 0) + nx * Y + plane * Z);  // natural row of x' = 0
+    T* const out0 = out + ((UPPER ? nx - 1 : 0) + nx * Y + plane * Z);
+    const bool y_edge = ny > 1 && yy == 0;
+    const bool z_edge = zz == 0;
+    const long long fsy = line_face_slot_y(P.g), fsz = line_face_slot_z(P.g);
+    const T* fy = faceY + w * fsy + zz;  // stride wz per x'
+    const T* fz = faceZ + w * fsz + yy;  // stride wy per x'
+    T* const fy_out = (ny > 1 && yy == wy - 1 && wyi < by - 1) ? faceY + (w + 1) * fsy + zz : nullptr;
+    T* const fz_out = (zz == wz - 1 && wzi < bz - 1) ? faceZ + (w + by) * fsz + yy : nullptr;
+    const LineCoef<T>* const cs = reinterpret_cast<const LineCoef<T>*>(P.coef) + P.g.slot(blk, w, 0, lane);
+    LineCoef<T>* const cr = cring + w * 32 + lane;  // slot k at cr[k * nw * 32]
+    T* const br = bring + w * 32 + lane;
+    const int rs = nw * 32;
+
+    // step t's operands into ring slot t % R (zeros where the lane has no row)
+    const unsigned span = line_ok ? static_cast<unsigned>(nx) : 0u;  // active: (unsigned)(t - skew) < span
+    auto issue = [&](int t) {
+        const int xq = t - skew;
+        const bool act = static_cast<unsigned>(xq) < span;
+        const int k = t & (R - 1);
+        const LineCoef<T>* c = act ? cs + static_cast<long long>(t) * 32 : cs;
+        const T* bp = act ? in0 + static_cast<long long>(sx) * xq : in;
+        if constexpr (sizeof(T) == 4) {
+            cp_async_16(cr + k * rs, c, act ? 16 : 0);
+            cp_async_4(br + k * rs, bp, act ? 4 : 0);
+        } else {
+            cp_async_16(cr + k * rs, c, act ? 16 : 0);
+            cp_async_16(reinterpret_cast<char*>(cr + k * rs) + 16, reinterpret_cast<const char*>(c) + 16, act ? 16 : 0);
+            cp_async_8(br + k * rs, bp, act ? 8 : 0);
+        }
+        cp_async_commit();
+    };
+#pragma unroll 1
+    for (int t = 0; t < R - 1; ++t) issue(t);
+    // face reads: edge lanes at x' (clamped: no read outside the face where the lane has no
+    // row), the other lanes from a word that holds 0
+    const T* const fy_rd = y_edge ? fy : zero_word;
+    const T* const fz_rd = z_edge ? fz : zero_word;
+    const int fy_st = y_edge ? wz : 0, fz_st = z_edge ? wy : 0;
+    T prev = T(0);  // the lane's result of the previous step (0 where it had no row)
+#pragma unroll 2
+    for (int s = 0; s < steps; ++s) {
+        cp_async_wait<R - 2>();  // step s has landed
+        const int k = s & (R - 1);
+        const LineCoef<T> c = cr[k * rs];
+        const T bv = br[k * rs];
+        issue(s + R - 1);  // into the slot read one step ago
+        const int xq = s - skew;
+        const bool act = static_cast<unsigned>(xq) < span;
+        const int xc = act ? xq : 0;
+        const T fyv = ld_volatile_shared(fy_rd + xc * fy_st);
+        const T fzv = ld_volatile_shared(fz_rd + xc * fz_st);
+        const T sh_y = __shfl_up_sync(0xffffffffu, prev, 1);
+        const T sh_z = __shfl_up_sync(0xffffffffu, prev, wy);
+        T vy = y_edge ? fyv : (ny > 1 ? sh_y : T(0));
+        T vz = z_edge ? fzv : sh_z;
+        const bool late = act && (Sentinel<T>::is(vy) || Sentinel<T>::is(vz));
+        if (__any_sync(0xffffffffu, late)) {  // a predecessor is not there yet
+            if (late && Sentinel<T>::is(vy)) vy = line_wait_shared(fy_rd + xc * fy_st, status);
+            if (late && Sentinel<T>::is(vz)) vz = line_wait_shared(fz_rd + xc * fz_st, status);
+        }
+        T acc = scaled ? bv * sc : bv;
+        const T xin = xq > 0 ? prev : T(0);
+        const long long off = static_cast<long long>(sx) * xq;
+        acc = fma(-c.cz, vz, acc);
+        acc = fma(-c.cy, vy, acc);
+        acc = fma(-c.cx, xin, acc);
+        // FP64: the reference's division (lanes without a row divide by 1: no slow path);
+        // FP32 (mixed path): d holds 1 / u_ii
+        if constexpr (UPPER) acc = sizeof(T) == 8 ? acc / (act ? c.d : T(1)) : acc * c.d;
+        const T r = Sentinel<T>::canon(acc);
+        st_relaxed_if(act, out0 + off, r);
+        st_shared_if(act && fy_out != nullptr, fy_out + xc * wz, r);
+        st_shared_if(act && fz_out != nullptr, fz_out + xc * wy, r);
+        prev = act ? r : T(0);
+    }
+    cp_async_wait<0>();
+}
+
+// The halo warp of block `blk`: copies the predecessors that the block's first warps
+// along y and z read from the previous blocks (their last lines, in `out`) into the
+// faces.  Lane e owns entry e of the y-face (the block's z-line e, at most 32) and entry
+// e of the z-face (its y-line e, at most 32) and walks each in x' with its own cursor;
+// each round loads the next kLineHalo positions of both (one L2 round trip) and retires,
+// in order, those that no longer hold the sentinel.
+constexpr int kLineHalo = 16;
+
+template <class T>
+struct HaloCursor {
+    const T* src = nullptr;  // natural row of x' = 0 of the source line (null: no entry)
+    T* dst = nullptr;        // face slot of x' = 0
+    int stride = 0;          // face stride per x'
+    int x = 0;               // next x' to copy
+};
+
+// Loads positions [x, x + kLineHalo) of a cursor (0 past the line's end or without entry).
+template <class T, bool UPPER>
+__device__ __forceinline__ void halo_load(const HaloCursor<T>& h, int nx, T (&v)[kLineHalo]) {
+    constexpr long long sx = UPPER ? -1 : 1;
+#pragma unroll
+    for (int u = 0; u < kLineHalo; ++u)
+        v[u] = (h.src != nullptr && h.x + u < nx) ? ld_relaxed_nb(h.src + sx * (h.x + u)) : T(0);
+}
+
+// Copies, in order, the loaded positions that no longer hold the sentinel; true when
+// the cursor moved.
+template <class T>
+__device__ __forceinline__ bool halo_retire(HaloCursor<T>& h, int nx, const T (&v)[kLineHalo]) {
+    if (h.src == nullptr || h.x >= nx) return false;
+    int adv = 0;
+    bool stop = false;
+#pragma unroll
+    for (int u = 0; u < kLineHalo; ++u) {
+        stop = stop || h.x + u >= nx || Sentinel<T>::is(v[u]);
+        st_shared_if(!stop, h.dst + static_cast<long long>(h.x + u) * h.stride, v[u]);
+        adv += stop ? 0 : 1;
+    }
+    h.x += adv;
+    return adv > 0;
+}
+
+template <class T, bool UPPER>
+__device__ __forceinline__ void line_halo(const LineTri<T>& P, int blk, const T* out, T* faceY, T* faceZ,
+                                          int* status) {
+    const int lane = threadIdx.x & 31;
+    const int nx = P.g.nx, ny = P.g.ny, nz = P.g.nz;
+    const int wy = P.g.wy, wz = P.g.wz, by = P.g.by, bz = P.g.bz;
+    const int iy = blk % P.g.nby, iz = blk / P.g.nby;
+    const long long plane = static_cast<long long>(nx) * ny;
+    auto row0 = [&](int ys, int zs) {
+        const long long Y = UPPER ? ny - 1 - ys : ys;
+        const long long Z = UPPER ? nz - 1 - zs : zs;
+        return (UPPER ? nx - 1 : 0) + nx * Y + plane * Z;
+    };
+    HaloCursor<T> hy, hz;
+    if (ny > 1 && iy > 0 && lane < bz * wz) {  // line (y0 - 1, z) of block (iy - 1, iz)
+        const int wzi = lane / wz, zz = lane % wz;
+        const int zs = (iz * bz + wzi) * wz + zz;
+        if (zs < nz) {
+            hy.src = out + row0(iy * by * wy - 1, zs);
+            hy.dst = faceY + (wzi * by) * line_face_slot_y(P.g) + zz;
+            hy.stride = wz;
+        }
+    }
+    if (iz > 0 && lane < by * wy) {  // line (y, z0 - 1) of block (iy, iz - 1)
+        const int wyi = lane / wy, yy = lane % wy;
+        const int ys = (iy * by + wyi) * wy + yy;
+        if (ys < ny) {
+            hz.src = out + row0(ys, iz * bz * wz - 1);
+            hz.dst = faceZ + wyi * line_face_slot_z(P.g) + yy;
+            hz.stride = wy;
+        }
+    }
+    WaitBudget wb;
+    while ((hy.src != nullptr && hy.x < nx) || (hz.src != nullptr && hz.x < nx)) {
+        // both cursors' loads in flight together: one L2 round trip per round
+        T vy[kLineHalo], vz[kLineHalo];
+        halo_load<T, UPPER>(hy, nx, vy);
+        halo_load<T, UPPER>(hz, nx, vz);
+        const bool a = halo_retire<T>(hy, nx, vy);
+        const bool b = halo_retire<T>(hz, nx, vz);
+        if (!a && !b && wb.expired(status)) {
+            atomicExch(status + kStatusTimeout, 1);
+            // unblock the compute warps: the remaining entries become 0
+            for (; hy.src != nullptr && hy.x < nx; ++hy.x) st_volatile_shared(hy.dst + static_cast<long long>(hy.x) * hy.stride, T(0));
+            for (; hz.src != nullptr && hz.x < nx; ++hz.x) st_volatile_shared(hz.dst + static_cast<long long>(hz.x) * hz.stride, T(0));
+            break;
+        }
+    }
+}
+
+// Forward (UPPER = false): out = L^{-1} (scale * in), in rescaled in place when `scale`
+// is given (block by block, after the block's solve); backward (UPPER = true):
+// out = U^{-1} in.  in / out in natural order; out holds the sentinel at every row on
+// entry.  nw compute warps + 1 halo warp; dynamic shared memory line_smem_bytes.
+template <class T, bool UPPER>
+__global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
+    sptrsv_line_kernel(LineTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
+                       const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    extern __shared__ __align__(16) unsigned char line_smem[];
+    const int nw = P.g.nw();
+    const long long fsy = line_face_slot_y(P.g), fsz = line_face_slot_z(P.g);
+    const long long fy_len = nw * fsy;
+    const long long face_len = line_face_len<T>(P.g);
+    T* faceY = reinterpret_cast<T*>(line_smem);
+    T* faceZ = faceY + fy_len;
+    T* zero_word = faceY + face_len;  // holds 0
+    LineCoef<T>* cring = reinterpret_cast<LineCoef<T>*>(line_smem + line_ring_offset<T>(P.g));
+    T* bring = reinterpret_cast<T*>(cring + static_cast<long long>(kLineRing<T>) * nw * 32);
+    __shared__ int s_ticket;
+    const bool scaled = !UPPER && scale != nullptr;
+    const T sc = scaled ? static_cast<T>(*scale) : T(1);
+    const int w = threadIdx.x >> 5;
+    for (int tk = draw_block_ticket(counter, P.g.nblk, &s_ticket); tk < P.g.nblk;
+         tk = draw_block_ticket(counter, P.g.nblk, &s_ticket)) {
+        const int blk = P.order[tk];
+        const int iy = blk % P.g.nby, iz = blk / P.g.nby;
+        // faces: the sentinel where a value will be written, 0 where the lines lie at the
+        // grid's boundary (slots of the first warps along y / z of the first blocks)
+        for (long long i = threadIdx.x; i < face_len; i += blockDim.x) {
+            const bool zero = i < fy_len ? (iy == 0 && static_cast<int>(i / fsy) % P.g.by == 0)
+                                         : (iz == 0 && static_cast<int>((i - fy_len) / fsz) / P.g.by == 0);
+            faceY[i] = zero ? T(0) : Sentinel<T>::value();
+        }
+        if (threadIdx.x == 0) *zero_word = T(0);
+        // stream the warps' operands into L2 (the right-hand side was written by the
+        // previous kernel and is there already)
+        if (w < nw)
+            prefetch_l2_range(P.coef + P.g.slot(blk, w, 0, 0) * 4,
+                              static_cast<long long>(P.g.steps) * 128 * static_cast<long long>(sizeof(T)),
+                              threadIdx.x & 31);
+        __syncthreads();
+        if (w < nw)
+            line_warp<T, UPPER>(P, blk, in, scaled, sc, out, faceY, faceZ, zero_word, cring, bring, status);
+        else
+            line_halo<T, UPPER>(P, blk, out, faceY, faceZ, status);
+        if (scaled) {
+            // GMRES normalises its new Krylov vector in the forward sweep: the block's rows
+            // of `in` (planes z of its z-lines, rows of its y-lines: contiguous runs) are
+            // rescaled in one coalesced pass once every warp is done reading them (the same
+            // product b * scale the rows used)
+            __syncthreads();
+            const int y0 = iy * P.g.by * P.g.wy, y1 = min(P.g.ny, y0 + P.g.by * P.g.wy);
+            const int z0 = iz * P.g.bz * P.g.wz, z1 = min(P.g.nz, z0 + P.g.bz * P.g.wz);
+            const long long run = static_cast<long long>(P.g.nx) * (y1 - y0);
+            for (int z = z0; z < z1; ++z) {
+                T* p = in + static_cast<long long>(P.g.nx) * (y0 + static_cast<long long>(P.g.ny) * z);
+                for (long long i = threadIdx.x; i < run; i += blockDim.x) p[i] = p[i] * sc;
+            }
+        }
+    }
+}
+
+// Packs the operand stream of a structured factor from its CSR values: one thread per
+// slot.  L: c_z, c_y, c_x are the row's strict-lower entries (columns ascending:
+// r - nx ny, r - nx, r - 1, each present only inside the grid), d = 0.  U: c_z, c_y, c_x
+// are the strict-upper entries r + nx ny, r + nx, r + 1 (columns descending) and d = u_ii
+// (FP64) or RN(1 / u_ii), computed in FP64 and rounded once (FP32, as the other FP32
+// kernels).  Slots without a row hold zeros.
+template <class T, bool UPPER>
+__global__ void line_pack_kernel(LineGeom g, const int* __restrict__ rp, const int* __restrict__ diag,
+                                 const double* __restrict__ lu, T* __restrict__ dst) {
+    const long long total = g.slots();
+    const int nw = g.nw();
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int lane = static_cast<int>(i & 31);
+        long long t = i >> 5;
+        const int s = static_cast<int>(t % g.steps);
+        t /= g.steps;
+        const int w = static_cast<int>(t % nw);
+        const int b = static_cast<int>(t / nw);
+        const int wyi = w % g.by, wzi = w / g.by;
+        const int yy = lane % g.wy, zz = lane / g.wy;
+        const int iy = b % g.nby, iz = b / g.nby;
+        const int yq = (iy * g.by + wyi) * g.wy + yy;
+        const int zq = (iz * g.bz + wzi) * g.wz + zz;
+        const int xq = s - (yy + zz);
+        double cz = 0.0, cy = 0.0, cx = 0.0, d = 0.0;
+        if (yq < g.ny && zq < g.nz && xq >= 0 && xq < g.nx) {
+            const int X = UPPER ? g.nx - 1 - xq : xq;
+            const int Y = UPPER ? g.ny - 1 - yq : yq;
+            const int Z = UPPER ? g.nz - 1 - zq : zq;
+            const long long r = X + static_cast<long long>(g.nx) * (Y + static_cast<long long>(g.ny) * Z);
+            if constexpr (!UPPER) {
+                int p = rp[r];
+                if (Z > 0) cz = lu[p++];
+                if (Y > 0) cy = lu[p++];
+                if (X > 0) cx = lu[p++];
+            } else {
+                int p = diag[r];
+                d = lu[p++];
+                if (X < g.nx - 1) cx = lu[p++];
+                if (Y < g.ny - 1) cy = lu[p++];
+                if (Z < g.nz - 1) cz = lu[p++];
+                if (sizeof(T) == 4) d = 1.0 / d;
+            }
+        }
+        T* o = dst + 4 * i;
+        o[0] = static_cast<T>(cz);
+        o[1] = static_cast<T>(cy);
+        o[2] = static_cast<T>(cx);
+        o[3] = static_cast<T>(d);
+    }
+}
+
+template <class T>
+__global__ void line_fill_kernel(long long n, T* p, T v) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        p[i] = v;
+}
+
+}  // namespace gb300

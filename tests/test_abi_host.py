@@ -240,16 +240,17 @@ def test_ilu_option_values_checked():
     for v in (2, -2, 0.5):
         with pytest.raises(RuntimeError):
             ilu.set_option(api.ILU_OPT_GRID, v)
-    for v in (0, 1, 2, 4):
-        ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, v)
-    for v in (3, 8, -1):
+    for v in (0, 1, 4, 8):
+        ilu.set_option(api.ILU_OPT_GRID_WARP_Y, v)
+    for v in (2, 3, 16, 32, 64, -1):
         with pytest.raises(RuntimeError):
-            ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, v)
-    for opt in (api.ILU_OPT_GRID_TILE_LINES, api.ILU_OPT_GRID_TILE_PLANES):
+            ilu.set_option(api.ILU_OPT_GRID_WARP_Y, v)
+    for opt in (api.ILU_OPT_GRID_CTA_Y, api.ILU_OPT_GRID_CTA_Z):
         ilu.set_option(opt, 0)
         ilu.set_option(opt, 7)
-        with pytest.raises(RuntimeError):
-            ilu.set_option(opt, -3)
+        for v in (-3, 9, 1.5):
+            with pytest.raises(RuntimeError):
+                ilu.set_option(opt, v)
     for v in (0, 1):
         ilu.set_option(api.ILU_OPT_TICKET_ORDER, v)
     with pytest.raises(RuntimeError):

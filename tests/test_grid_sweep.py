@@ -1,13 +1,14 @@
-"""Structured-grid sweeps (LLJBASH_ILU_OPT_GRID = 1): the wavefront-lanes kernels for 7-point
-(3-D) and 5-point (2-D) factors in natural order.
+"""Structured-grid line-pipeline sweeps (LLJBASH_ILU_OPT_GRID): the kernels for 7-point
+(3-D) and 5-point (2-D) factors in natural order, a lane per grid line.
 
-Every row performs the reference's operations in the reference's order, so the grid
+Every row performs the reference's operations in the reference's order, so the line
 schedule must give results bit-identical to the block-local and level-ordered kernels
 (FP64 substitution, and the FP32 path through identical mixed-precision GMRES runs), and
-1e-12 against the CPU oracle.  Covered: grid shapes whose x extent is and is not a
-multiple of 32, 2-D grids (one line per plane), several lane widths (elements per lane)
-and tile shapes (lines and planes per tile, down to one), and matrices the detection
-must reject (27-point stencils, ILU(1) fill, a permuted 7-point matrix)."""
+1e-12 against the CPU oracle.  Covered: grid shapes whose extents are and are not
+multiples of the warp's lanes, 2-D grids, every warp shape (1, 4 or 8 lanes along y),
+CTA shapes from one warp to eight, more blocks than resident CTAs (persistent CTAs taking
+several blocks), and matrices the detection must reject (27-point stencils, ILU(1) fill,
+a permuted 7-point matrix)."""
 import numpy as np
 import pytest
 
@@ -25,12 +26,12 @@ def port():
     return oracle.Port()
 
 
-def solver(f, grid=1, elems=0, lines=0, planes=0, block_rows=0):
+def solver(f, grid=1, wy=0, by=0, bz=0, block_rows=0):
     ilu = api.IluSolver()
     ilu.set_option(api.ILU_OPT_GRID, grid)
-    ilu.set_option(api.ILU_OPT_GRID_LANE_ELEMS, elems)
-    ilu.set_option(api.ILU_OPT_GRID_TILE_LINES, lines)
-    ilu.set_option(api.ILU_OPT_GRID_TILE_PLANES, planes)
+    ilu.set_option(api.ILU_OPT_GRID_WARP_Y, wy)
+    ilu.set_option(api.ILU_OPT_GRID_CTA_Y, by)
+    ilu.set_option(api.ILU_OPT_GRID_CTA_Z, bz)
     ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
     ilu.set_matrix(f)
     assert ilu.setup() == 0, api.last_error()
@@ -55,33 +56,50 @@ def test_grid_sweep_matches_other_schedules_and_oracle(port, name, make):
     f, _ = api.iluk_symbolic(a, 0)
     ilu = solver(f)
     info = ilu.info()
-    assert info.grid_fp64 == 1 and info.grid_fp32 == 1, name
+    assert info.grid_fp64 == 3 and info.grid_fp32 == 3, name  # forward and backward sweeps
     lu_ref, _ = port.factorize(f)
     assert rel_err(ilu.values(), lu_ref, floor=1e-300) <= 1e-12
     _, b = g.random_rhs(a, seed=3)
     x = ilu.substitute(b)
     assert rel_err(x, port.substitute(f, lu_ref, b)) <= 1e-12
-    for kw in ({"grid": -1, "block_rows": -1}, {"grid": 0, "block_rows": 0}):
+    for kw in ({"grid": -1, "block_rows": -1}, {"grid": -1, "block_rows": 0}):
         other = solver(f, **kw)
         assert other.info().grid_fp64 == 0
         assert np.array_equal(other.substitute(b), x), kw
-    assert np.array_equal(ilu.substitute(b), x)  # the layout buffers are back at the sentinel
+    assert np.array_equal(ilu.substitute(b), x)  # repeatable: faces and counters are reset
 
 
-TUNINGS = [dict(elems=1, lines=1, planes=1), dict(elems=1, lines=3, planes=5), dict(elems=2),
-           dict(elems=4, lines=2, planes=3), dict(elems=4), dict(elems=1, lines=8, planes=64)]
+TUNINGS = [dict(wy=1, by=1, bz=1), dict(wy=4, by=3, bz=2), dict(wy=4), dict(wy=8, by=2, bz=4),
+           dict(wy=1, by=8, bz=1), dict(wy=8, by=4, bz=2), dict(wy=8, by=1, bz=1), dict(wy=1, by=2, bz=4)]
 
 
 @pytest.mark.parametrize("kw", TUNINGS, ids=[str(k) for k in TUNINGS])
-@pytest.mark.parametrize("make", [lambda: g.convdiff3d(40, 9, 11), lambda: g.laplace2d(100, 37)],
-                         ids=["convdiff3d_40x9x11", "laplace2d_100x37"])
-def test_grid_tile_shapes_and_lane_widths(make, kw):
+@pytest.mark.parametrize("make", [lambda: g.convdiff3d(40, 9, 11), lambda: g.laplace2d(100, 37),
+                                  lambda: g.convdiff3d(9, 40, 33)],
+                         ids=["convdiff3d_40x9x11", "laplace2d_100x37", "convdiff3d_9x40x33"])
+def test_grid_warp_and_cta_shapes(make, kw):
     a = make()
     f, _ = api.iluk_symbolic(a, 0)
     ref = solver(f, grid=-1, block_rows=-1)
     ilu = solver(f, **kw)
-    assert ilu.info().grid_fp64 == 1
+    info = ilu.info()
+    assert info.grid_fp64 == 3
+    assert info.grid_warp_y * info.grid_warp_z == 32 and info.grid_cta_y * info.grid_cta_z <= 8
     _, b = g.random_rhs(a, seed=5)
+    xr = ref.substitute(b)
+    assert np.array_equal(ilu.substitute(b), xr)
+    assert np.array_equal(ilu.substitute(b), xr)
+
+
+def test_grid_more_blocks_than_resident_ctas():
+    """One-warp CTAs over a grid of 64 x 70 lines: 192 blocks, more than the GPU's SMs, so
+    persistent CTAs take several blocks each."""
+    a = g.convdiff3d(5, 64, 70)
+    f, _ = api.iluk_symbolic(a, 0)
+    ref = solver(f, grid=-1, block_rows=-1)
+    ilu = solver(f, wy=1, by=1, bz=1)
+    assert ilu.info().grid_blocks == 192 and ilu.info().grid_fp64 == 3
+    _, b = g.random_rhs(a, seed=9)
     assert np.array_equal(ilu.substitute(b), ref.substitute(b))
 
 
@@ -95,7 +113,7 @@ def test_grid_gmres_identical_to_block_schedule(make):
     _, b = g.random_rhs(a, seed=7)
     tol = 1e-8 * float(np.linalg.norm(b))
     out = {}
-    for grid in (1, -1):
+    for grid in (1, -1, 0):
         ilu = solver(f, grid=grid)
         for mode in (0, 1):
             gm = api.Gmres(tol, 40, 1000)
@@ -105,8 +123,26 @@ def test_grid_gmres_identical_to_block_schedule(make):
             assert res.ok
             out[(grid, mode)] = (res.iterations, res.x)
     for mode in (0, 1):
-        assert out[(1, mode)][0] == out[(-1, mode)][0]
-        assert np.array_equal(out[(1, mode)][1], out[(-1, mode)][1])
+        for grid in (1, 0):
+            assert out[(grid, mode)][0] == out[(-1, mode)][0]
+            assert np.array_equal(out[(grid, mode)][1], out[(-1, mode)][1])
+
+
+@pytest.mark.parametrize("make", [lambda: g.convdiff3d(64), lambda: g.laplace2d(200)],
+                         ids=["convdiff3d_64", "laplace2d_200"])
+def test_grid_automatic_choice(make):
+    """Automatic mode times each sweep of each precision against the block-local kernel at
+    the first factorisation and keeps the faster: whatever it picks, the substitution is
+    bit-identical to the block-local one, and the choice is reported per sweep."""
+    a = make()
+    f, _ = api.iluk_symbolic(a, 0)
+    ref = solver(f, grid=-1)
+    ilu = solver(f, grid=0)
+    info = ilu.info()
+    assert 0 <= info.grid_fp64 <= 3 and 0 <= info.grid_fp32 <= 3
+    assert info.grid_nx > 0  # the pattern qualified
+    _, b = g.random_rhs(a, seed=13)
+    assert np.array_equal(ilu.substitute(b), ref.substitute(b))
 
 
 def test_grid_detection_rejects_other_patterns():
