@@ -218,7 +218,9 @@ def batched_section(nsys: int, nrhs: int, learned, seed: int = 5, with_cpu: bool
     bs = api.BatchSolver(systems, nrhs=nrhs, restart=30, rtol=RTOL, maxit=MAXIT)
     if learned.get("params") is not None:
         bs.set_shift_model(learned["params"], learned.get("min_shift", 0.0))
-    cps, lf = bs.autotune()
+    bs.autotune()
+    cps, lf, rpc = bs.shape()
+    trials = bs.trials()
     flat = np.concatenate([b.ravel() for b in rhs])
     bs.solve(flat)  # warm-up
     out = bs.solve(flat)
@@ -231,6 +233,7 @@ def batched_section(nsys: int, nrhs: int, learned, seed: int = 5, with_cpu: bool
             fwd = max(fwd, float(np.max(np.abs(xr - xt[k][r]))))
             pos += a.n
     unknowns = int(sum(a.n for a in systems)) * nrhs
+    roof = batched_roofline(systems, nrhs, rpc, out["iterations"], out["ms"])
     cpu = batched_cpu_baseline(systems, rhs, seed) if with_cpu else None
     return {"workload": f"{nsys} variable-coefficient 5-pt systems (sides U[32,224], lognormal sigma 1) x {nrhs} RHS, "
                         "ILU(0) FP32 + GMRES(30), FP64 refinement to rtol 1e-8, one persistent launch",
@@ -238,9 +241,34 @@ def batched_section(nsys: int, nrhs: int, learned, seed: int = 5, with_cpu: bool
             "solves_per_s": round(nsys * nrhs / (out["ms"] * 1e-3), 1),
             "converged_fraction": float(np.mean(out["converged"])), "max_rel_residual": worst,
             "max_forward_error": fwd, "iterations_mean": float(np.mean(out["iterations"])),
-            "iterations_max": int(np.max(out["iterations"])), "autotune": {"ctas_per_sm": cps, "largest_first": lf},
+            "iterations_max": int(np.max(out["iterations"])),
+            "autotune": {"ctas_per_sm": cps, "largest_first": lf, "rhs_per_cta": rpc,
+                         "rows_per_cta_round": 512 // rpc, "trials": trials},
+            "roofline": roof,
             "learned_shift": learned.get("params") is not None, "generation_s": round(gen_s, 2),
             "cpu_baseline": cpu}
+
+
+def batched_roofline(systems, nrhs, rpc, iterations, ms):
+    """Algorithmic bytes of the batched launch over its device time, against the measured
+    HBM copy bandwidth.  Per right-hand side and Krylov step (GMRES(30), step i of a cycle
+    touching i + 1 basis vectors, i = 14.5 on average): the two sweeps (read v, write z,
+    read and write z), the SpMV (read z, write w) and CGS2 (two passes reading i + 1 basis
+    vectors and w, two axpy passes, a norm) on FP32 vectors, 4 n (9 + 4 (i + 1)) bytes;
+    per group of rpc right-hand sides and step, the FP32 factor and matrix values with
+    their column indices once, 16 nnz bytes.  Factorisation and FP64 residuals (once per
+    cycle) are left out: the figure is a lower bound of the traffic."""
+    peak, kind = measured_peaks()
+    it = np.asarray(iterations).reshape(len(systems), nrhs)
+    vec = coef = 0.0
+    for k, a in enumerate(systems):
+        vec += float(np.sum(it[k])) * 4.0 * a.n * (9 + 4 * 15.5)
+        for r0 in range(0, nrhs, rpc):
+            coef += float(np.max(it[k, r0:r0 + rpc])) * 16.0 * a.nnz
+    total = vec + coef
+    achieved = total / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": kind, "alg_bytes": total}
 
 
 BATCH_CPU_SAMPLE = 96

@@ -231,8 +231,20 @@ LLJBASH_BatchHdl LLJBASH_BatchCreateEx(int nsys, const int* n, const int* row_pt
                                        double rtol, int maxit);
 void LLJBASH_BatchDestroy(LLJBASH_BatchHdl hdl);
 int LLJBASH_BatchSetShiftModel(LLJBASH_BatchHdl hdl, const float* params, int nparams, double min_shift);
-/* Picks the launch shape (CTAs per SM, system order) by timing a sample of the batch. */
+/* Picks the launch shape by timing a sample of the batch (up to two systems per SM,
+ * largest first, right-hand sides b = A x for a pseudo-random x, at most 40 iterations
+ * each): right-hand sides per solve item (1, 4 or 16: a CTA of 512 threads handles
+ * 512 / G rows of G right-hand sides per round, loading each coefficient once for the G)
+ * x CTAs per SM (1, 2).  Returns the chosen CTAs per SM and order; right-hand sides and
+ * solutions held from a previous solve are overwritten. */
 int LLJBASH_BatchAutotune(LLJBASH_BatchHdl hdl, int* ctas_per_sm, int* largest_first);
+/* The launch shape in use (after LLJBASH_BatchAutotune or LLJBASH_BatchSetShape). */
+int LLJBASH_BatchGetShape(LLJBASH_BatchHdl hdl, int* ctas_per_sm, int* largest_first, int* rhs_per_cta);
+int LLJBASH_BatchSetShape(LLJBASH_BatchHdl hdl, int ctas_per_sm, int largest_first, int rhs_per_cta);
+/* The autotuner's trials (up to cap of them copied): shape and device time in ms.
+ * Returns the number of trials. */
+int LLJBASH_BatchGetTrials(LLJBASH_BatchHdl hdl, int cap, int* ctas_per_sm, int* largest_first, int* rhs_per_cta,
+                           double* ms);
 /* iters / resid / converged: nsys * nrhs entries (any may be NULL); *ms: device time of
  * the launch. */
 int LLJBASH_BatchSolve(LLJBASH_BatchHdl hdl, const double* rhs, double* x, int* iters, double* resid, int* converged,

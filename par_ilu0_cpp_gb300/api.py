@@ -157,6 +157,9 @@ def load() -> ctypes.CDLL:
         "LLJBASH_BatchDestroy": (None, [ctypes.c_void_p]),
         "LLJBASH_BatchSetShiftModel": (ctypes.c_int, [ctypes.c_void_p, _F, ctypes.c_int, ctypes.c_double]),
         "LLJBASH_BatchAutotune": (ctypes.c_int, [ctypes.c_void_p, _I, _I]),
+        "LLJBASH_BatchGetShape": (ctypes.c_int, [ctypes.c_void_p, _I, _I, _I]),
+        "LLJBASH_BatchSetShape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+        "LLJBASH_BatchGetTrials": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _I, _I, _I, _D]),
         "LLJBASH_BatchSolve": (ctypes.c_int, [ctypes.c_void_p, _D, _D, _I, _D, _I, ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -630,6 +633,28 @@ class BatchSolver:
         if self.lib.LLJBASH_BatchAutotune(self.h, ctypes.byref(c), ctypes.byref(lf)) != 0:
             raise RuntimeError(last_error())
         return int(c.value), bool(lf.value)
+
+    def shape(self):
+        """(CTAs per SM, largest first, right-hand sides per item) in use."""
+        c, lf, g = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        if self.lib.LLJBASH_BatchGetShape(self.h, ctypes.byref(c), ctypes.byref(lf), ctypes.byref(g)) != 0:
+            raise RuntimeError(last_error())
+        return int(c.value), bool(lf.value), int(g.value)
+
+    def set_shape(self, ctas_per_sm: int, largest_first: bool, rhs_per_cta: int):
+        if self.lib.LLJBASH_BatchSetShape(self.h, int(ctas_per_sm), int(bool(largest_first)), int(rhs_per_cta)) != 0:
+            raise RuntimeError(last_error())
+
+    def trials(self):
+        """The autotuner's trials: list of dicts (ctas_per_sm, largest_first, rhs_per_cta, ms)."""
+        k = self.lib.LLJBASH_BatchGetTrials(self.h, 0, None, None, None, None)
+        c = np.zeros(max(k, 1), dtype=np.int32)
+        lf = np.zeros_like(c)
+        g = np.zeros_like(c)
+        ms = np.zeros(max(k, 1))
+        self.lib.LLJBASH_BatchGetTrials(self.h, k, _ip(c), _ip(lf), _ip(g), _dp(ms))
+        return [dict(ctas_per_sm=int(c[i]), largest_first=bool(lf[i]), rhs_per_cta=int(g[i]), ms=float(ms[i]))
+                for i in range(k)]
 
     def solve(self, rhs):
         """rhs: flat array (systems in order, nrhs vectors each).  Returns dict."""

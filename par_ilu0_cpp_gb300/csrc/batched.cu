@@ -136,138 +136,252 @@ __device__ void factor_system(const BatchDesc& D, int s, double* red, float* P) 
     }
 }
 
-// Solve item (system s, right-hand side r).
+// Solve item: system s, right-hand sides r0 .. r0 + G - 1 (those below nrhs), solved in
+// lockstep by one CTA.  Vectors are interleaved [row][G] and thread t works on right-hand
+// side g = t % G of rows t / G, t / G + T / G, ...: each coefficient of L, U and A is
+// loaded once for the G right-hand sides, the G threads reading it touch consecutive
+// vector entries, and the level-synchronous sweeps pay their barriers once for G
+// right-hand sides.  Each right-hand side keeps its own GMRES state (Hessenberg matrix in
+// global workspace, rotations, residual, convergence); one that has converged or run out
+// of iterations idles while the others continue.
 __device__ __forceinline__ float warp_sum_f32(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-// The loops over a system's rows run in FP32 only (coefficients converted once into `cf`,
-// per-thread and per-warp partial sums in FP32, warps combined in FP64): GB300's FP64
-// pipe is far narrower than its FP32 one, and a conversion or FP64 add per element and
-// basis vector set the pace of the Gram-Schmidt passes.
-__device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double* H, double* hc, double* cs,
-                           double* sn, double* rs, float* cf, int* flag) {
-    if (threadIdx.x == 0) *flag = wait_flag(D.ready + s, D.epoch, D.status) ? 1 : 0;
+// Sum over the lanes of a warp that share g = lane % G (lanes g < G hold the sums).
+template <int G, class V>
+__device__ __forceinline__ V warp_sum_g(V v) {
+#pragma unroll
+    for (int o = 16; o >= G; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per-right-hand-side sums over the CTA: every thread adds its value for g = tid % G into
+// acc[g] (shared memory, zeroed by the caller before a barrier); a barrier follows.
+template <int G>
+__device__ __forceinline__ void group_sum(double v, double* acc) {
+    v = warp_sum_g<G>(v);
+    if ((threadIdx.x & 31) < G) atomicAdd(acc + (threadIdx.x & 31), v);
+    __syncthreads();
+}
+
+// Per-item GMRES state of the G right-hand sides, carved from dynamic shared memory
+// (sizes follow the restart length m): reductions acc [m + 1][G], and per right-hand side
+// hc / cs / sn / rs [G][m + 2] (FP64), cf [G][m + 2] (FP32) and scalars.
+struct GroupSmem {
+    double* acc;
+    double *hc, *cs, *sn, *rs;  // row g at g * ld
+    float* cf;
+    double *tol, *stop, *beta, *hnext;
+    int *alive, *cyc, *its, *last, *conv;
+    int* any;
+    int* flag;
+    int ld;
+};
+
+__host__ __device__ inline size_t group_smem_bytes(int m, int G) {
+    const size_t ld = static_cast<size_t>(m) + 2;
+    return sizeof(double) * (static_cast<size_t>(m + 1) * G + 4 * G * ld + 4 * G) + sizeof(float) * G * ld +
+           sizeof(int) * (5 * G + 2) + 16;
+}
+
+__device__ inline GroupSmem group_smem(unsigned char* base, int m, int G) {
+    GroupSmem S;
+    S.ld = m + 2;
+    double* d = reinterpret_cast<double*>(base);
+    S.acc = d;
+    d += (m + 1) * G;
+    S.hc = d;
+    d += G * S.ld;
+    S.cs = d;
+    d += G * S.ld;
+    S.sn = d;
+    d += G * S.ld;
+    S.rs = d;
+    d += G * S.ld;
+    S.tol = d;
+    S.stop = d + G;
+    S.beta = d + 2 * G;
+    S.hnext = d + 3 * G;
+    d += 4 * G;
+    float* f = reinterpret_cast<float*>(d);
+    S.cf = f;
+    f += G * S.ld;
+    int* i = reinterpret_cast<int*>(f);
+    S.alive = i;
+    S.cyc = i + G;
+    S.its = i + 2 * G;
+    S.last = i + 3 * G;
+    S.conv = i + 4 * G;
+    S.any = i + 5 * G;
+    S.flag = i + 5 * G + 1;
+    return S;
+}
+
+template <int G>
+__device__ void solve_group(const BatchDesc& D, int s, int r0, const GroupSmem& S2) {
+    if (threadIdx.x == 0) *S2.flag = wait_flag(D.ready + s, D.epoch, D.status) ? 1 : 0;
     __syncthreads();
     const SysView S = sys_view(D, s);
     const int n = S.n;
     const int m = D.m;
     const long long ws = D.ws;
-    float* V = D.V + static_cast<long long>(blockIdx.x) * (m + 1) * ws;
-    float* Z = D.Z + static_cast<long long>(blockIdx.x) * m * ws;
-    double* x = D.xw + static_cast<long long>(blockIdx.x) * ws;
-    double* rw = D.rw + static_cast<long long>(blockIdx.x) * ws;
-    const long long io = D.rhs_off[s] + static_cast<long long>(r) * n;
-    const double* b = D.rhs + io;
     const int tid = threadIdx.x;
     const int T = blockDim.x;
-    if (!*flag) {  // the factorisation never became ready: report and skip
-        if (tid == 0) {
-            D.iters[s * D.nrhs + r] = 0;
-            D.resid[s * D.nrhs + r] = -1.0;
-            D.converged[s * D.nrhs + r] = 0;
+    const int g = tid % G;   // right-hand side of this thread
+    const int rl = tid / G;  // first row of this thread
+    const int RT = T / G;    // rows per round
+    const int ng = min(G, D.nrhs - r0);
+    float* V = D.V + static_cast<long long>(blockIdx.x) * (m + 1) * ws * G;  // V_k[row][g]
+    float* Z = D.Z + static_cast<long long>(blockIdx.x) * m * ws * G;
+    double* x = D.xw + static_cast<long long>(blockIdx.x) * ws * G;  // x[row][g]
+    double* rw = D.rw + static_cast<long long>(blockIdx.x) * ws * G;
+    const long long io = D.rhs_off[s] + static_cast<long long>(r0 + (g < ng ? g : 0)) * n;
+    const double* b = D.rhs + io;
+    const int out_base = s * D.nrhs + r0;
+    if (!*S2.flag) {  // the factorisation never became ready: report and skip
+        if (tid < ng) {
+            D.iters[out_base + tid] = 0;
+            D.resid[out_base + tid] = -1.0;
+            D.converged[out_base + tid] = 0;
         }
         return;
     }
+    auto vec = [&](float* base, int k, int row) -> float* { return base + (static_cast<long long>(k) * ws + row) * G + g; };
+    if (tid < G) {
+        S2.acc[tid] = 0.0;
+        S2.its[tid] = 0;
+        S2.conv[tid] = 0;
+        S2.alive[tid] = tid < ng ? 1 : 0;
+    }
+    __syncthreads();
     double bb = 0.0;
-    for (int i = tid; i < n; i += T) {
-        x[i] = 0.0;
+    for (int i = rl; i < n; i += RT) {
+        x[static_cast<long long>(i) * G + g] = 0.0;
         bb = fma(b[i], b[i], bb);
     }
-    const double tol = D.rtol * sqrt(block_sum(bb, red));
-    int its = 0;
-    bool conv = false;
-    double beta = 0.0;
+    group_sum<G>(bb, S2.acc);
+    if (tid < G) S2.tol[tid] = D.rtol * sqrt(S2.acc[tid]);
     while (true) {
-        // FP64 residual r = b - A x
+        // FP64 residuals r_g = b_g - A x_g
+        if (tid < G) S2.acc[tid] = 0.0;
+        __syncthreads();
         double ss = 0.0;
-        for (int i = tid; i < n; i += T) {
+        for (int i = rl; i < n; i += RT) {
             double acc = 0.0;
-            for (int p = S.rp[i]; p < S.rp[i + 1]; ++p) acc = fma(S.a64[p], x[S.ci[p]], acc);
+            for (int p = S.rp[i]; p < S.rp[i + 1]; ++p) acc = fma(S.a64[p], x[static_cast<long long>(S.ci[p]) * G + g], acc);
             const double ri = b[i] - acc;
-            rw[i] = ri;
+            rw[static_cast<long long>(i) * G + g] = ri;
             ss = fma(ri, ri, ss);
         }
-        beta = sqrt(block_sum(ss, red));
-        if (beta <= tol) {
-            conv = true;
-            break;
+        group_sum<G>(ss, S2.acc);
+        if (tid < G) {
+            const double beta = sqrt(S2.acc[tid]);
+            S2.beta[tid] = beta;
+            if (S2.alive[tid]) {
+                if (beta <= S2.tol[tid]) {
+                    S2.conv[tid] = 1;
+                    S2.alive[tid] = 0;
+                } else if (S2.its[tid] >= D.maxit || isnan(beta)) {
+                    S2.alive[tid] = 0;
+                }
+            }
+            S2.cyc[tid] = S2.alive[tid];
+            S2.last[tid] = -1;
+            S2.stop[tid] = fmax(S2.tol[tid], D.tau * beta);
+            S2.rs[(tid) * S2.ld + 0] = beta;
         }
-        if (its >= D.maxit || isnan(beta)) break;
-        const double inv = 1.0 / beta;
-        for (int i = tid; i < n; i += T) V[i] = static_cast<float>(rw[i] * inv);
-        const double stop = fmax(tol, D.tau * beta);
-        if (tid == 0) rs[0] = beta;
         __syncthreads();
-        int i = 0;
-        int last = -1;
-        for (; i < m && its < D.maxit; ++i) {
-            ++its;
-            float* vi = V + static_cast<long long>(i) * ws;
-            float* zi = Z + static_cast<long long>(i) * ws;
-            float* w = V + static_cast<long long>(i + 1) * ws;
+        if (tid == 0) {
+            int a = 0;
+            for (int q = 0; q < G; ++q) a |= S2.cyc[q];
+            *S2.any = a;
+        }
+        __syncthreads();
+        if (!*S2.any) break;
+        {
+            const double inv = S2.cyc[g] ? 1.0 / S2.beta[g] : 0.0;
+            for (int i = rl; i < n; i += RT) *vec(V, 0, i) = static_cast<float>(rw[static_cast<long long>(i) * G + g] * inv);
+        }
+        __syncthreads();
+        for (int i = 0; i < m; ++i) {
+            if (tid < G && S2.cyc[tid]) ++S2.its[tid];
             // z = L^{-1} v (ascending entries), level by level
             for (int l = 0; l < S.nlevL; ++l) {
-                for (int q = S.lptrL[l] + tid; q < S.lptrL[l + 1]; q += T) {
+                for (int q = S.lptrL[l] + rl; q < S.lptrL[l + 1]; q += RT) {
                     const int row = S.ordL[q];
-                    float t = vi[row];
-                    for (int p = S.rp[row]; p < S.diag[row]; ++p) t = fmaf(-S.lu32[p], zi[S.ci[p]], t);
-                    zi[row] = t;
+                    float t = *vec(V, i, row);
+                    for (int p = S.rp[row]; p < S.diag[row]; ++p) t = fmaf(-S.lu32[p], *vec(Z, i, S.ci[p]), t);
+                    *vec(Z, i, row) = t;
                 }
                 __syncthreads();
             }
             // z = U^{-1} z (descending entries), in place, level by level
             for (int l = 0; l < S.nlevU; ++l) {
-                for (int q = S.lptrU[l] + tid; q < S.lptrU[l + 1]; q += T) {
+                for (int q = S.lptrU[l] + rl; q < S.lptrU[l + 1]; q += RT) {
                     const int row = S.ordU[q];
-                    float t = zi[row];
-                    for (int p = S.rp[row + 1] - 1; p > S.diag[row]; --p) t = fmaf(-S.lu32[p], zi[S.ci[p]], t);
-                    zi[row] = t * S.dinv[row];
+                    float t = *vec(Z, i, row);
+                    for (int p = S.rp[row + 1] - 1; p > S.diag[row]; --p) t = fmaf(-S.lu32[p], *vec(Z, i, S.ci[p]), t);
+                    *vec(Z, i, row) = t * S.dinv[row];
                 }
                 __syncthreads();
             }
             // w = A z (FP32)
-            for (int k = tid; k < n; k += T) {
+            for (int k = rl; k < n; k += RT) {
                 float acc = 0.f;
-                for (int p = S.rp[k]; p < S.rp[k + 1]; ++p) acc = fmaf(S.a32[p], zi[S.ci[p]], acc);
-                w[k] = acc;
+                for (int p = S.rp[k]; p < S.rp[k + 1]; ++p) acc = fmaf(S.a32[p], *vec(Z, i, S.ci[p]), acc);
+                *vec(V, i + 1, k) = acc;
             }
-            __syncthreads();
-            // CGS2: two projections, dot products accumulated in FP64
+            // CGS2: two projections, per-warp partial sums in FP32, combined in FP64
             for (int pass = 0; pass < 2; ++pass) {
+                for (int q = tid; q < (i + 1) * G; q += T) S2.acc[q] = 0.0;
+                __syncthreads();
                 for (int j = 0; j <= i; ++j) {
-                    const float* vj = V + static_cast<long long>(j) * ws;
                     float part = 0.f;
-                    for (int k = tid; k < n; k += T) part = fmaf(vj[k], w[k], part);
-                    const float wsum = warp_sum_f32(part);
-                    if ((tid & 31) == 0) red[(tid >> 5) * (kBatchMaxM + 1) + j] = static_cast<double>(wsum);
+                    for (int k = rl; k < n; k += RT) part = fmaf(*vec(V, j, k), *vec(V, i + 1, k), part);
+                    part = warp_sum_g<G>(part);
+                    if ((tid & 31) < G) atomicAdd(S2.acc + j * G + (tid & 31), static_cast<double>(part));
                 }
                 __syncthreads();
-                for (int j = tid; j <= i; j += T) {
-                    double t = 0.0;
-                    for (int k = 0; k < kBatchWarps; ++k) t += red[k * (kBatchMaxM + 1) + j];
+                for (int q = tid; q < (i + 1) * G; q += T) {
+                    const int j = q / G, gg = q % G;
+                    const double t = S2.acc[q];
                     if (pass == 0) {
-                        hc[j] = t;
+                        S2.hc[(gg) * S2.ld + j] = t;
                     } else {
-                        hc[j] += t;
+                        S2.hc[(gg) * S2.ld + j] += t;
                     }
-                    cf[j] = static_cast<float>(t);  // this pass's coefficients
+                    S2.cf[(gg) * S2.ld + j] = static_cast<float>(t);  // this pass's coefficients
                 }
                 __syncthreads();
-                for (int k = tid; k < n; k += T) {
-                    float a = w[k];
-                    for (int j = 0; j <= i; ++j) a = fmaf(-cf[j], V[static_cast<long long>(j) * ws + k], a);
-                    w[k] = a;
+                for (int k = rl; k < n; k += RT) {
+                    float a = *vec(V, i + 1, k);
+                    for (int j = 0; j <= i; ++j) a = fmaf(-S2.cf[(g) * S2.ld + j], *vec(V, j, k), a);
+                    *vec(V, i + 1, k) = a;
                 }
                 __syncthreads();
             }
-            float nn = 0.f;
-            for (int k = tid; k < n; k += T) nn = fmaf(w[k], w[k], nn);
-            const double hnext = sqrt(block_sum(static_cast<double>(nn), red));
-            if (tid == 0) {
-                // Givens update of column i (src/gmres.cpp:238-256)
+            if (tid < G) S2.acc[tid] = 0.0;
+            __syncthreads();
+            {
+                float nn = 0.f;
+                for (int k = rl; k < n; k += RT) {
+                    const float wv = *vec(V, i + 1, k);
+                    nn = fmaf(wv, wv, nn);
+                }
+                group_sum<G>(static_cast<double>(nn), S2.acc);
+            }
+            if (tid < G && S2.cyc[tid]) {
+                // Givens update of column i of right-hand side tid (src/gmres.cpp:238-256)
+                const int q = tid;
+                double* H = D.H + (static_cast<long long>(blockIdx.x) * G + q) * (kBatchMaxM + 1) * m;
+                const double hnext = sqrt(S2.acc[q]);
+                double* hc = S2.hc + q * S2.ld;
+                double* cs = S2.cs + q * S2.ld;
+                double* sn = S2.sn + q * S2.ld;
+                double* rs = S2.rs + q * S2.ld;
                 double prev = hc[0];
                 for (int k = 1; k <= i; ++k) {
                     const double cur = hc[k];
@@ -282,71 +396,86 @@ __device__ void solve_item(const BatchDesc& D, int s, int r, double* red, double
                 rs[i + 1] = -sn[i] * rs[i];
                 rs[i] = cs[i] * rs[i];
                 hc[i] = cs[i] * hc[i] + sn[i] * hnext;
-                for (int j = 0; j <= i; ++j) H[i * (kBatchMaxM + 1) + j] = hc[j];
+                for (int j = 0; j <= i; ++j) H[static_cast<long long>(i) * (kBatchMaxM + 1) + j] = hc[j];
                 const double est = fabs(rs[i + 1]);
-                flag[0] = (hnext <= 1e-16 || est <= stop || isnan(est)) ? 1 : 0;
+                S2.last[q] = i;
+                S2.hnext[q] = hnext;
+                if (hnext <= 1e-16 || est <= S2.stop[q] || isnan(est) || S2.its[q] >= D.maxit) S2.cyc[q] = 0;
+            } else if (tid < G) {
+                S2.hnext[tid] = 0.0;
             }
             __syncthreads();
-            const bool done = flag[0] != 0;
-            if (hnext > 1e-16) {
-                const float invn = static_cast<float>(1.0 / hnext);
-                for (int k = tid; k < n; k += T) w[k] *= invn;
+            {
+                const double hn = S2.hnext[g];
+                if (hn > 1e-16) {
+                    const float invn = static_cast<float>(1.0 / hn);
+                    for (int k = rl; k < n; k += RT) *vec(V, i + 1, k) *= invn;
+                }
             }
-            last = i;
+            if (tid == 0) {
+                int a = 0;
+                for (int q = 0; q < G; ++q) a |= S2.cyc[q];
+                *S2.any = a;
+            }
             __syncthreads();
-            if (done) break;
+            if (!*S2.any) break;
         }
-        if (last < 0) break;
-        // least squares: rs[0..last] <- H^{-1} rs, then x += Z y in FP64
-        if (tid == 0) {
-            rs[last] = rs[last] / H[last * (kBatchMaxM + 1) + last];
+        // least squares per right-hand side: rs[0..last] <- H^{-1} rs, then x += Z y (FP64)
+        if (tid < G && S2.last[tid] >= 0) {
+            const int q = tid;
+            const int last = S2.last[q];
+            const double* H = D.H + (static_cast<long long>(blockIdx.x) * G + q) * (kBatchMaxM + 1) * m;
+            double* rs = S2.rs + q * S2.ld;
+            rs[last] = rs[last] / H[static_cast<long long>(last) * (kBatchMaxM + 1) + last];
             for (int ii = last - 1; ii >= 0; --ii) {
                 double t = rs[ii];
-                for (int j = ii + 1; j <= last; ++j) t -= H[j * (kBatchMaxM + 1) + ii] * rs[j];
-                rs[ii] = t / H[ii * (kBatchMaxM + 1) + ii];
+                for (int j = ii + 1; j <= last; ++j) t -= H[static_cast<long long>(j) * (kBatchMaxM + 1) + ii] * rs[j];
+                rs[ii] = t / H[static_cast<long long>(ii) * (kBatchMaxM + 1) + ii];
             }
-            for (int j = 0; j <= last; ++j) cf[j] = static_cast<float>(rs[j]);
+            for (int j = 0; j <= last; ++j) S2.cf[(q) * S2.ld + j] = static_cast<float>(rs[j]);
         }
         __syncthreads();
-        for (int k = tid; k < n; k += T) {
-            float d = 0.f;
-            for (int j = 0; j <= last; ++j) d = fmaf(cf[j], Z[static_cast<long long>(j) * ws + k], d);
-            x[k] += static_cast<double>(d);
+        {
+            const int last = S2.last[g];
+            for (int k = rl; k < n; k += RT) {
+                float d = 0.f;
+                for (int j = 0; j <= last; ++j) d = fmaf(S2.cf[(g) * S2.ld + j], *vec(Z, j, k), d);
+                x[static_cast<long long>(k) * G + g] += static_cast<double>(d);
+            }
         }
         __syncthreads();
     }
-    for (int k = tid; k < n; k += T) D.x[io + k] = x[k];
-    if (tid == 0) {
-        D.iters[s * D.nrhs + r] = its;
-        D.resid[s * D.nrhs + r] = beta;
-        D.converged[s * D.nrhs + r] = conv ? 1 : 0;
+    if (g < ng)
+        for (int k = rl; k < n; k += RT) D.x[io + k] = x[static_cast<long long>(k) * G + g];
+    if (tid < ng) {
+        D.iters[out_base + tid] = S2.its[tid];
+        D.resid[out_base + tid] = S2.beta[tid];
+        D.converged[out_base + tid] = S2.conv[tid];
     }
     __syncthreads();
 }
 
 }  // namespace
 
-// Two CTAs per SM (64 registers per thread): the autotuner's two-CTA shape must really
-// be resident, and the solve items are latency-bound, so two per SM beat one.
+// Two CTAs per SM (64 registers per thread): the autotuner's two-CTA shapes must really
+// be resident, and the solve items are latency-bound, so two per SM beat one.  G: right-
+// hand sides per solve item.
+template <int G>
 __global__ void __launch_bounds__(kBatchThreads, 2) batched_ilu_gmres_kernel(BatchDesc D, int nsys_run) {
-    __shared__ double red[kBatchWarps * (kBatchMaxM + 1)];
-    __shared__ double H[(kBatchMaxM + 1) * kBatchMaxM];
-    __shared__ double hc[kBatchMaxM + 2];
-    __shared__ double cs[2 * kBatchMaxM + 2];
-    __shared__ double sn[kBatchMaxM + 1];
-    __shared__ double rs[kBatchMaxM + 2];
-    __shared__ float cf[kBatchMaxM + 2];
+    __shared__ double red[kBatchWarps];
     __shared__ float P[kMlpParams];
-    __shared__ int flag[2];
     __shared__ int s_ticket;
-    const int njobs = nsys_run + nsys_run * D.nrhs;
+    extern __shared__ __align__(16) unsigned char group_dyn[];
+    const GroupSmem S2 = group_smem(group_dyn, D.m, G);
+    const int groups = (D.nrhs + G - 1) / G;
+    const int njobs = nsys_run + nsys_run * groups;
     for (int job = draw_block_ticket(D.ticket, njobs, &s_ticket); job < njobs;
          job = draw_block_ticket(D.ticket, njobs, &s_ticket)) {
         if (job < nsys_run) {
             factor_system(D, D.sys_of_slot[job], red, P);
         } else {
             const int k = job - nsys_run;
-            solve_item(D, D.sys_of_slot[k / D.nrhs], k % D.nrhs, red, H, hc, cs, sn, rs, cf, flag);
+            solve_group<G>(D, D.sys_of_slot[k / groups], (k % groups) * G, S2);
         }
     }
 }
@@ -504,17 +633,63 @@ void BatchSolver::set_model(const float* params, float min_shift) {
     model_ = true;
 }
 
-void BatchSolver::ensure_workspace(int grid) {
-    const size_t vec = static_cast<size_t>(ws_);
+void BatchSolver::ensure_workspace(int grid, int G) {
+    const size_t vec = static_cast<size_t>(ws_) * G;
     d_V_.reserve(static_cast<size_t>(grid) * (m_ + 1) * vec);
     d_Z_.reserve(static_cast<size_t>(grid) * m_ * vec);
     d_xw_.reserve(static_cast<size_t>(grid) * vec);
     d_rw_.reserve(static_cast<size_t>(grid) * vec);
+    d_H_.reserve(static_cast<size_t>(grid) * G * (kBatchMaxM + 1) * m_);
 }
 
-float BatchSolver::launch(int ctas_per_sm, bool largest_first, int nsys_run) {
+size_t BatchSolver::workspace_bytes(int grid, int G) const {
+    const size_t vec = static_cast<size_t>(ws_) * G;
+    return static_cast<size_t>(grid) * (sizeof(float) * (2 * m_ + 1) * vec + sizeof(double) * 2 * vec +
+                                        sizeof(double) * G * (kBatchMaxM + 1) * m_);
+}
+
+// Right-hand sides for the autotuner's trials, b = A x with x deterministic in [-1, 1)
+// (a hash of system, right-hand side and row), like the callers' b = A x_true: the
+// trials need systems that iterate like real ones, and the caller's right-hand sides
+// arrive only with solve().  One CTA per system.
+__device__ __forceinline__ double trial_x(long long key) {
+    unsigned long long h = static_cast<unsigned long long>(key) * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    return static_cast<double>(h >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+__global__ void batch_trial_rhs_kernel(BatchDesc D, int nsys_run) {
+    for (int q = blockIdx.x; q < nsys_run; q += gridDim.x) {
+        const int s = D.sys_of_slot[q];
+        const int n = D.n[s];
+        const int* rp = D.rp + D.rp_off[s];
+        const int* ci = D.ci + D.nnz_off[s];
+        const double* a = D.a64 + D.nnz_off[s];
+        for (int r = 0; r < D.nrhs; ++r) {
+            double* b = const_cast<double*>(D.rhs) + D.rhs_off[s] + static_cast<long long>(r) * n;
+            const long long key = (static_cast<long long>(s) * D.nrhs + r) << 32;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                double acc = 0.0;
+                for (int p = rp[i]; p < rp[i + 1]; ++p) acc = fma(a[p], trial_x(key + ci[p]), acc);
+                b[i] = acc;
+            }
+        }
+    }
+}
+
+template <int G>
+static void launch_batched(int grid, const BatchDesc& D, int nsys_run, int m, cudaStream_t s) {
+    const size_t smem = group_smem_bytes(m, G);
+    GB_CUDA_CHECK(cudaFuncSetAttribute(batched_ilu_gmres_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem)));
+    batched_ilu_gmres_kernel<G><<<grid, kBatchThreads, smem, s>>>(D, nsys_run);
+}
+
+float BatchSolver::launch(int ctas_per_sm, bool largest_first, int nsys_run, int G) {
     const int grid = std::max(1, ctas_per_sm) * dev_.sms;
-    ensure_workspace(grid);
+    ensure_workspace(grid, G);
     // the first nsys_run systems (input order), processed largest first or in input order
     order_.resize(nsys_run);
     std::iota(order_.begin(), order_.end(), 0);
@@ -567,9 +742,19 @@ float BatchSolver::launch(int ctas_per_sm, bool largest_first, int nsys_run) {
     D.Z = d_Z_.get();
     D.xw = d_xw_.get();
     D.rw = d_rw_.get();
+    D.H = d_H_.get();
     D.ws = ws_;
+    if (trial_) {
+        batch_trial_rhs_kernel<<<2 * dev_.sms, 256, 0, stream_>>>(D, nsys_run);
+        GB_CUDA_CHECK(cudaGetLastError());
+    }
     GB_CUDA_CHECK(cudaEventRecord(ev0_, stream_));
-    batched_ilu_gmres_kernel<<<grid, kBatchThreads, 0, stream_>>>(D, nsys_run);
+    switch (G) {
+        case 1: launch_batched<1>(grid, D, nsys_run, m_, stream_); break;
+        case 4: launch_batched<4>(grid, D, nsys_run, m_, stream_); break;
+        case 16: launch_batched<16>(grid, D, nsys_run, m_, stream_); break;
+        default: throw std::runtime_error("batched: right-hand sides per item must be 1, 4 or 16");
+    }
     GB_CUDA_CHECK(cudaGetLastError());
     GB_CUDA_CHECK(cudaEventRecord(ev1_, stream_));
     GB_CUDA_CHECK(cudaEventSynchronize(ev1_));
@@ -586,27 +771,53 @@ float BatchSolver::launch(int ctas_per_sm, bool largest_first, int nsys_run) {
 }
 
 void BatchSolver::autotune() {
-    // Launch shapes tried on the same sample (the first systems of the batch): CTAs per
-    // SM x system order (largest first / input order).  The fastest wins.
+    // Launch shapes tried on the same sample (the first systems of the batch, largest
+    // first): right-hand sides per CTA (G = 1, 4, 16: rows per CTA round T / G) x CTAs per
+    // SM.  The fastest wins; every trial is kept (trials()).
     const int sample = std::min(nsys_, 2 * dev_.sms);
     float best = 1e30f;
-    for (int cps : {1, 2}) {
-        for (bool lf : {true, false}) {
-            const float ms = launch(cps, lf, sample);
-            tuned_.push_back({cps, lf ? 1 : 0, ms});
+    tuned_.clear();
+    trial_ = true;  // right-hand sides b = A x of its own (below), iterations capped
+    const int maxit = maxit_;
+    maxit_ = std::min(maxit_, kBatchTrialIterations);
+    for (int G : {1, 4, 16}) {
+        if (G > 1 && G / 4 >= nrhs_) continue;  // no wider than the right-hand sides need
+        for (int cps : {1, 2}) {
+            if (workspace_bytes(cps * dev_.sms, G) > kBatchWorkspaceCap) continue;
+            float ms = 0.f;
+            try {
+                ms = launch(cps, true, sample, G);
+            } catch (...) {
+                maxit_ = maxit;
+                trial_ = false;
+                throw;
+            }
+            tuned_.push_back({cps, 1, G, ms});
             if (ms < best) {
                 best = ms;
                 ctas_per_sm_ = cps;
-                largest_first_ = lf;
+                largest_first_ = true;
+                rhs_per_cta_ = G;
             }
         }
     }
+    maxit_ = maxit;
+    trial_ = false;
+}
+
+void BatchSolver::set_shape(int ctas_per_sm, bool largest_first, int rhs_per_cta) {
+    if (ctas_per_sm < 1 || ctas_per_sm > 2) throw std::runtime_error("batched: CTAs per SM must be 1 or 2");
+    if (rhs_per_cta != 1 && rhs_per_cta != 4 && rhs_per_cta != 16)
+        throw std::runtime_error("batched: right-hand sides per item must be 1, 4 or 16");
+    ctas_per_sm_ = ctas_per_sm;
+    largest_first_ = largest_first;
+    rhs_per_cta_ = rhs_per_cta;
 }
 
 float BatchSolver::solve(const double* rhs_host, double* x_host, int* iters, double* resid, int* converged) {
     GB_CUDA_CHECK(cudaMemcpyAsync(d_rhs_.get(), rhs_host, sizeof(double) * static_cast<size_t>(total_rhs_),
                                   cudaMemcpyHostToDevice, stream_));
-    const float ms = launch(ctas_per_sm_, largest_first_, nsys_);
+    const float ms = launch(ctas_per_sm_, largest_first_, nsys_, rhs_per_cta_);
     if (x_host)
         GB_CUDA_CHECK(cudaMemcpyAsync(x_host, d_x_.get(), sizeof(double) * static_cast<size_t>(total_rhs_),
                                       cudaMemcpyDeviceToHost, stream_));

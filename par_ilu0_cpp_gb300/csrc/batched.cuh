@@ -2,7 +2,7 @@
 // each with several right-hand sides, in ONE persistent kernel launch.
 //
 // Work items, drawn from a ticket counter by whole CTAs: first one factorisation item per
-// system, then one solve item per (system, right-hand side).  A solve item waits for its
+// system, then one solve item per (system, group of G right-hand sides).  A solve item waits for its
 // system's ready flag, which the factorising CTA (holding a smaller ticket, hence
 // running) publishes with release semantics; the wait is bounded.
 //
@@ -13,8 +13,10 @@
 //    up-looking order per entry, FP64), then stored as FP32 factors + FP32 1/u_ii;
 //  * solve: GMRES(m) in FP32 cycles with FP64 iterative refinement (every cycle starts
 //    from the FP64 residual b - A x and adds its FP32 correction to the FP64 x; only the
-//    FP64 residual can end the solve), level-synchronous triangular solves within the
-//    CTA, CGS2 with block reductions, Givens and least squares on one thread.
+//    FP64 residual can end the solve) for G right-hand sides in lockstep (vectors
+//    interleaved [row][G], one thread per row and right-hand side), level-synchronous
+//    triangular solves within the CTA, CGS2 with block reductions, Givens and least
+//    squares on one thread per right-hand side.
 #pragma once
 
 #include "common.cuh"
@@ -25,6 +27,7 @@ namespace gb300 {
 constexpr int kBatchThreads = 512;
 constexpr int kBatchWarps = kBatchThreads / kWarp;
 constexpr int kBatchMaxM = 64;
+constexpr int kBatchMaxG = 16;  // right-hand sides per solve item
 
 struct BatchDesc {
     int nsys = 0, nrhs = 0, m = 0, maxit = 0;
@@ -73,6 +76,7 @@ struct BatchDesc {
     float* Z = nullptr;
     double* xw = nullptr;
     double* rw = nullptr;
+    double* H = nullptr;  // per CTA and right-hand side: Hessenberg columns [m][kBatchMaxM + 1]
     long long ws = 0;  // padded vector length
 };
 

@@ -24,8 +24,9 @@ public:
 
     void set_model(const float* params, float min_shift);
     void set_tau(double tau) { tau_ = tau; }
-    // Tries launch shapes (CTAs per SM x system order) on a sample of the batch.
+    // Tries launch shapes (right-hand sides per CTA x CTAs per SM) on a sample of the batch.
     void autotune();
+    void set_shape(int ctas_per_sm, bool largest_first, int rhs_per_cta);
     // rhs_host: for every system, nrhs vectors of n[s] values (system-major); x_host the
     // same layout.  iters / resid / converged: nsys * nrhs entries (optional).
     float solve(const double* rhs_host, double* x_host, int* iters, double* resid, int* converged);
@@ -33,18 +34,26 @@ public:
     struct Trial {
         int ctas_per_sm;
         int largest_first;
+        int rhs_per_cta;
         float ms;
     };
     const std::vector<Trial>& trials() const { return tuned_; }
     int ctas_per_sm() const { return ctas_per_sm_; }
     bool largest_first() const { return largest_first_; }
+    int rhs_per_cta() const { return rhs_per_cta_; }
     float last_ms() const { return last_ms_; }
     long long launches() const { return launches_; }
     long long total_unknowns() const { return total_rhs_; }
 
 private:
-    float launch(int ctas_per_sm, bool largest_first, int nsys_run);
-    void ensure_workspace(int grid);
+    float launch(int ctas_per_sm, bool largest_first, int nsys_run, int rhs_per_cta);
+    void ensure_workspace(int grid, int rhs_per_cta);
+    size_t workspace_bytes(int grid, int rhs_per_cta) const;
+    // largest workspace an autotuner trial may allocate (per-CTA Krylov bases)
+    static constexpr size_t kBatchWorkspaceCap = size_t(48) << 30;
+    // iterations per right-hand side in an autotuner trial
+    static constexpr int kBatchTrialIterations = 40;
+    bool trial_ = false;
 
     int nsys_ = 0, nrhs_ = 0, m_ = 0;
     double rtol_ = 1e-8, tau_ = 1e-6;
@@ -57,6 +66,7 @@ private:
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     int epoch_ = 0;
     int ctas_per_sm_ = 1;
+    int rhs_per_cta_ = 1;
     bool largest_first_ = true;
     bool model_ = false;
     float min_shift_ = 0.f;
@@ -66,7 +76,7 @@ private:
     DeviceBuffer<int> d_n_, d_nlevL_, d_nlevU_, d_order_, d_rp_, d_ci_, d_diag_, d_ordL_, d_ordU_, d_lptrL_, d_lptrU_,
         d_depth_, d_iters_, d_conv_, d_shifted_, d_ready_, d_status_;
     DeviceBuffer<long long> d_rp_off_, d_nnz_off_, d_row_off_, d_lvl_off_, d_rhs_off_;
-    DeviceBuffer<double> d_a64_, d_f64_, d_lu64_, d_rhs_, d_x_, d_resid_, d_xw_, d_rw_;
+    DeviceBuffer<double> d_a64_, d_f64_, d_lu64_, d_rhs_, d_x_, d_resid_, d_xw_, d_rw_, d_H_;
     DeviceBuffer<float> d_a32_, d_lu32_, d_dinv_, d_mlp_, d_V_, d_Z_;
     DeviceBuffer<unsigned> d_ticket_;
 };

@@ -319,6 +319,32 @@ int LLJBASH_BatchAutotune(LLJBASH_BatchHdl hdl, int* ctas_per_sm, int* largest_f
     });
 }
 
+int LLJBASH_BatchGetShape(LLJBASH_BatchHdl hdl, int* ctas_per_sm, int* largest_first, int* rhs_per_cta) {
+    GB_TRY({
+        const auto* b = static_cast<gb300::BatchSolver*>(hdl);
+        if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm();
+        if (largest_first) *largest_first = b->largest_first() ? 1 : 0;
+        if (rhs_per_cta) *rhs_per_cta = b->rhs_per_cta();
+    });
+}
+
+int LLJBASH_BatchSetShape(LLJBASH_BatchHdl hdl, int ctas_per_sm, int largest_first, int rhs_per_cta) {
+    GB_TRY({ static_cast<gb300::BatchSolver*>(hdl)->set_shape(ctas_per_sm, largest_first != 0, rhs_per_cta); });
+}
+
+int LLJBASH_BatchGetTrials(LLJBASH_BatchHdl hdl, int cap, int* ctas_per_sm, int* largest_first, int* rhs_per_cta,
+                           double* ms) {
+    const auto& t = static_cast<gb300::BatchSolver*>(hdl)->trials();
+    const int k = static_cast<int>(t.size());
+    for (int i = 0; i < k && i < cap; ++i) {
+        if (ctas_per_sm) ctas_per_sm[i] = t[i].ctas_per_sm;
+        if (largest_first) largest_first[i] = t[i].largest_first;
+        if (rhs_per_cta) rhs_per_cta[i] = t[i].rhs_per_cta;
+        if (ms) ms[i] = t[i].ms;
+    }
+    return k;
+}
+
 int LLJBASH_BatchSolve(LLJBASH_BatchHdl hdl, const double* rhs, double* x, int* iters, double* resid, int* converged,
                        double* ms) {
     GB_TRY({

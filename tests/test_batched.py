@@ -52,6 +52,13 @@ def test_batched_autotune_and_repeat_are_consistent():
     bsol = api.BatchSolver(systems, nrhs=4, restart=30)
     cps, lf = bsol.autotune()
     assert cps in (1, 2)
+    trials = bsol.trials()
+    assert {t["rhs_per_cta"] for t in trials} == {1, 4}  # 16 is wider than 4 right-hand sides need
+    assert all(t["ms"] > 0 for t in trials)
+    # the trials iterate on right-hand sides of their own (the caller's come with solve())
+    assert all(t["ms"] > 0.05 for t in trials)
+    best = min(trials, key=lambda t: t["ms"])
+    assert bsol.shape() == (best["ctas_per_sm"], best["largest_first"], best["rhs_per_cta"])
     rhs = np.concatenate([b.ravel() for b in bs])
     out1 = bsol.solve(rhs)
     out2 = bsol.solve(rhs)
@@ -80,3 +87,31 @@ def test_batched_matches_single_solver_iterations_roughly():
     out = bsol.solve(b)
     res, _, _ = api.ilu_gmres(a, b, restart=30, mode=1)
     assert abs(int(out["iterations"][0]) - res.iterations) <= 3
+
+
+@pytest.mark.parametrize("rhs_per_cta", [1, 4, 16])
+def test_batched_rhs_groups(rhs_per_cta):
+    """Right-hand sides solved in lockstep groups of 1, 4 or 16 per CTA (7 per system: the
+    last group of a system is partly empty): every answer meets the FP64 tolerance, and
+    each right-hand side takes nearly the iterations it takes alone (the reductions
+    differ in order only)."""
+    sides = [9, 30, 47, 16, 52, 3]
+    systems, xs, bs = _batch(sides, 17, nrhs=7)
+    rhs = np.concatenate([b.ravel() for b in bs])
+    ref = api.BatchSolver(systems, nrhs=7, restart=20)
+    ref.set_shape(1, True, 1)
+    out_ref = ref.solve(rhs)
+    bsol = api.BatchSolver(systems, nrhs=7, restart=20)
+    bsol.set_shape(2, True, rhs_per_cta)
+    assert bsol.shape() == (2, True, rhs_per_cta)
+    out = bsol.solve(rhs)
+    _check(systems, xs, bs, out, 7)
+    assert np.max(np.abs(out["iterations"].astype(int) - out_ref["iterations"].astype(int))) <= 3
+
+
+def test_batched_shape_is_checked():
+    systems, _, _ = _batch([10, 12], 19, nrhs=2)
+    bsol = api.BatchSolver(systems, nrhs=2)
+    for bad in ((3, True, 1), (1, True, 2), (0, False, 4)):
+        with pytest.raises(RuntimeError):
+            bsol.set_shape(*bad)
