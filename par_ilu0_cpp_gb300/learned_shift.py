@@ -2,14 +2,16 @@
 evaluation and the model file.
 
 Labels are found by the method itself: for every training matrix the solver is run
-(ILU(0) with FP32 factors + GMRES(40) in FP32 cycles with FP64 refinement, tol 1e-8)
-for each member of a two-parameter family of per-row shifts
+(ILU(0) with FP32 factors + GMRES(40) in FP32 cycles with FP64 refinement, tol 1e-8,
+at most 400 iterations) for each member of a two-parameter family of per-row shifts
 
     y_i(alpha, beta) = alpha * max(0, 1 - r_i) + beta,      shift_i = sign(a_ii) y_i s_i
 
-(r_i = |a_ii| / s_i the diagonal dominance ratio, s_i = sum_j!=i |a_ij|), and the member
-with the fewest GMRES iterations (ties: the smaller shift, plain ILU first) gives every
-row its target y_i.  The MLP (4 features -> 16 -> 16 -> 1, csrc/mlp.cuh) is then fitted
+(r_i = |a_ii| / s_i the diagonal dominance ratio, s_i = sum_j!=i |a_ij|), and the best
+member gives every row its target y_i: among members that converge, the fewest GMRES
+iterations; if none converges, the smallest final FP64 relative residual (so that the
+matrices on which restarted GMRES stagnates, most of the stress set, still give a
+signal); ties go to the smaller shift, plain ILU first.  The MLP (4 features -> 16 -> 16 -> 1, csrc/mlp.cuh) is then fitted
 to (features, y) by the library's own GPU kernels (forward, backward, Adam).  At run
 time the model's inference runs in the factorisation pre-pass; plain ILU is the
 fallback on a pivot breakdown (inside the library) and when the shifted solve does not
@@ -35,8 +37,8 @@ from . import generators as g
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_MODEL = os.path.join(PKG, "shift_model.json")
-ALPHAS = (0.0, 0.5, 1.0)
-BETAS = (0.0, 0.01, 0.03, 0.1)
+ALPHAS = (0.0, 1.0, 2.0)
+BETAS = (0.0, 0.05, 0.1, 0.3, 1.0)
 RESTART = 40
 LABEL_MAXIT = 400
 
@@ -192,17 +194,23 @@ def build_dataset(specs, log=None, chunk: int = 200):
         bs.close()
         for k, (side, seed) in enumerate(part):
             a = mats[k]
-            its = []
+            its, keys = [], []
+            nb = float(np.linalg.norm(rhs[k * len(cmb)]))
             for j in range(len(cmb)):
                 q = k * len(cmb) + j
-                its.append(int(out["iterations"][q]) if out["converged"][q] else LABEL_MAXIT + 1)
-            best = min(range(len(cmb)), key=lambda j: (its[j], float(np.mean(ys[k][j]))))
+                conv = bool(out["converged"][q])
+                it = int(out["iterations"][q]) if conv else LABEL_MAXIT + 1
+                rel = float(out["residual"][q]) / nb if nb > 0 else 0.0
+                rel = rel if np.isfinite(rel) and rel >= 0 else np.inf
+                its.append(it)
+                keys.append((0, it, 0.0) if conv else (1, 0, rel))
+            best = min(range(len(cmb)), key=lambda j: (keys[j], float(np.mean(ys[k][j]))))
             f, _ = api.iluk_symbolic(a, 0)
             an = api.analyze_pattern(f)
             Xs.append(api.shift_features(f, an["depth_l"], int(an["nlev"][0])))
             Ys.append(ys[k][best].astype(np.float32))
             recs.append(dict(side=side, seed=seed, alpha=cmb[best][0], beta=cmb[best][1], its=its[best],
-                             plain_its=its[0], trials=its))
+                             plain_its=its[0], trials=its, key=keys[best], plain_key=keys[0]))
         if log:
             log(f"labelled {min(c0 + chunk, len(specs))}/{len(specs)} matrices in {time.time() - t0:.1f}s")
     return np.concatenate(Xs), np.concatenate(Ys), recs
@@ -236,6 +244,66 @@ def load_model(path=DEFAULT_MODEL):
     return np.asarray(d["params"], dtype=np.float32), d
 
 
+def evaluate_batched(params, specs, min_shift=0.0, maxit=1000, chunk=200, log=None):
+    """Plain ILU(0) and the learned shift on the matrices of `specs`, each solved by the
+    batched persistent solver (the learned shift inferred in its factorisation pre-pass),
+    GMRES(40), rtol 1e-8, at most `maxit` iterations: iterations, convergence and final
+    FP64 relative residual per matrix."""
+    out = []
+    for c0 in range(0, len(specs), chunk):
+        part = specs[c0:c0 + chunk]
+        mats, rhs = [], []
+        for side, seed in part:
+            a = g.cdr2d(side, seed=seed)
+            _, b = g.random_rhs(a, seed=seed + 1)
+            mats.append(a)
+            rhs.append(b)
+        flat = np.concatenate(rhs)
+        res = {}
+        for label, model in (("plain", None), ("learned", params)):
+            bs = api.BatchSolver(mats, nrhs=1, restart=RESTART, maxit=maxit)
+            if model is not None:
+                bs.set_shift_model(model, min_shift)
+            res[label] = bs.solve(flat)
+            bs.close()
+        for k, (side, seed) in enumerate(part):
+            nb = float(np.linalg.norm(rhs[k]))
+            rec = dict(side=side, seed=seed)
+            for label in ("plain", "learned"):
+                o = res[label]
+                rel = float(o["residual"][k]) / nb
+                rec[label] = int(o["iterations"][k])
+                rec[label + "_converged"] = bool(o["converged"][k])
+                rec[label + "_residual"] = rel if np.isfinite(rel) and rel >= 0 else float("inf")
+            out.append(rec)
+        if log:
+            log(f"evaluated {min(c0 + chunk, len(specs))}/{len(specs)}")
+    return out
+
+
+def summarize(res):
+    """Held-out summary: convergence counts, iterations where both converge, and the
+    final relative residual ratio (learned / plain) where neither converges."""
+    both = [r for r in res if r["plain_converged"] and r["learned_converged"]]
+    neither = [r for r in res if not r["plain_converged"] and not r["learned_converged"]]
+    ratios = [r["learned_residual"] / r["plain_residual"] for r in neither
+              if np.isfinite(r["plain_residual"]) and r["plain_residual"] > 0]
+    broken = [r for r in res if not np.isfinite(r["plain_residual"])]
+    return dict(
+        matrices=len(res),
+        plain_converged=int(sum(bool(r["plain_converged"]) for r in res)),
+        learned_converged=int(sum(bool(r["learned_converged"]) for r in res)),
+        both_converged=len(both),
+        iterations_both=dict(plain=int(sum(r["plain"] for r in both)), learned=int(sum(r["learned"] for r in both)),
+                             learned_fewer=int(sum(r["learned"] < r["plain"] for r in both)),
+                             learned_more=int(sum(r["learned"] > r["plain"] for r in both))),
+        neither_converged=len(neither),
+        residual_ratio_median=float(np.median(ratios)) if ratios else None,
+        residual_lower=int(sum(x < 1.0 for x in ratios)), residual_higher=int(sum(x > 1.0 for x in ratios)),
+        plain_breakdowns=len(broken),
+        breakdowns_repaired=int(sum(bool(np.isfinite(r["learned_residual"])) for r in broken)))
+
+
 def evaluate(params, specs, min_shift=0.0, log=None):
     """Iterations with and without the model on the matrices of `specs`."""
     out = []
@@ -264,6 +332,7 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--out", default=DEFAULT_MODEL)
     ap.add_argument("--log", default=None)
+    ap.add_argument("--eval-out", default=None, help="held-out results (JSON)")
     args = ap.parse_args(argv)
     logf = open(args.log, "w") if args.log else None
 
@@ -279,10 +348,11 @@ def main(argv=None):
         X, Y, recs = build_dataset(specs, log)
         log(f"dataset: {Y.size} rows from {len(specs)} matrices, labels in {time.time() - t0:.1f}s")
         params, hist = train(X, Y, epochs=args.epochs, seed=args.seed, log=log)
-        better = sum(1 for r in recs if r["its"] < r["plain_its"])
+        better = sum(1 for r in recs if tuple(r["key"]) < tuple(r["plain_key"]))
         meta = dict(features=["log(|a_ii|/mean|a_jj|)", "log(||a_i,off||_2/mean|a_jj|)", "min(dominance,4)",
                               "depth/(levels-1)"],
                     family="y = alpha*max(0,1-r) + beta", alphas=list(ALPHAS), betas=list(BETAS),
+                    label_score="fewest iterations among converging members, else smallest final residual",
                     n_train=args.n_train, train_sides=[32, 128], seed=args.seed, rows=int(Y.size), loss=hist,
                     train_better_than_plain=better, min_shift=0.0, train_seconds=time.time() - t0)
         save_model(args.out, params, meta)
@@ -292,11 +362,13 @@ def main(argv=None):
         rng = np.random.default_rng(args.seed + 7)
         sides = rng.integers(args.eval_lo, args.eval_hi + 1, size=args.n_eval)
         seeds = rng.integers(0, 1 << 31, size=args.n_eval)
-        res = evaluate(params, list(zip(map(int, sides), map(int, seeds))), meta.get("min_shift", 0.0), log)
-        wins = sum(1 for r in res if r["learned"] < r["plain"])
-        tot_p = sum(r["plain"] for r in res)
-        tot_l = sum(r["learned"] for r in res)
-        log(f"eval: learned fewer iterations on {wins}/{len(res)}; total {tot_l} vs plain {tot_p}")
+        res = evaluate_batched(params, list(zip(map(int, sides), map(int, seeds))), meta.get("min_shift", 0.0),
+                               log=log)
+        summ = summarize(res)
+        log("eval: " + json.dumps(summ))
+        if args.eval_out:
+            with open(args.eval_out, "w") as fh:
+                json.dump(dict(summary=summ, matrices=res), fh, indent=1)
     if logf:
         logf.close()
 

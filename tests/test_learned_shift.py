@@ -144,3 +144,20 @@ def test_committed_model_against_plain():
         r2 = s.solve_policy(b)  # the decision is reused
         assert r2["iterations"] == r["iterations"]
     print(f"learned shift: {raw_l} iterations vs plain {raw_p} on 3 held-out matrices (before the decision rule)")
+
+
+@pytest.mark.gpu
+def test_committed_model_repairs_breakdowns():
+    """What the trained network gains on the held-out stress set: plain ILU(0) breaks down
+    (non-finite residual) on two unseen 269^2 / 270^2 matrices, and the learned shift
+    turns both into finite, decreasing solves (GMRES(40), 200 iterations)."""
+    from par_ilu0_cpp_gb300 import learned_shift as ls
+
+    path = os.path.join(ROOT, "par_ilu0_cpp_gb300", "shift_model.json")
+    if not os.path.isfile(path):
+        pytest.skip("no trained model committed")
+    params, meta = ls.load_model(path)
+    res = ls.evaluate_batched(params, [(269, 1817867017), (270, 1665652449)], meta.get("min_shift", 0.0), maxit=200)
+    for r in res:
+        assert not np.isfinite(r["plain_residual"]), r
+        assert np.isfinite(r["learned_residual"]) and r["learned_residual"] < 0.1, r
