@@ -112,7 +112,10 @@ enum {
      * for every order): 0 (default) level order (the reference's Levelization); 1 the
      * reference's subtree scheduler (src/subtree.hpp tree_schedule, one worker per SM):
      * the workers' independent subtrees interleaved row by row, then the remaining
-     * (separator) rows in elimination-tree post order.  Next IluSolverSetup. */
+     * (separator) rows in elimination-tree post order; 2 the same partitions, each
+     * factorised by one CTA level by level without waiting on other CTAs, then the
+     * separator rows by tickets (LLJBASH_IluInfo factor_subtree_parts / _rows).  Next
+     * IluSolverSetup. */
     LLJBASH_ILU_OPT_TICKET_ORDER = 11,
     /* factorisation kernel (results are the same for every choice): 0 (default,
      * automatic) and 1: one warp per row; 2: one lane per row when no row has more than
@@ -186,6 +189,8 @@ typedef struct LLJBASH_IluInfo {
     int grid_cta_y;       /* warps of a CTA along y and z */
     int grid_cta_z;
     int grid_blocks;      /* CTA-sized blocks of grid lines */
+    int factor_subtree_parts; /* ticket order 2: subtree partitions (one CTA each) and their rows */
+    int factor_subtree_rows;
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
 

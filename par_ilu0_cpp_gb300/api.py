@@ -55,7 +55,8 @@ class IluInfo(ctypes.Structure):
                 ("grid_nx", ctypes.c_int),
                 ("grid_ny", ctypes.c_int), ("grid_nz", ctypes.c_int), ("grid_warp_y", ctypes.c_int),
                 ("grid_warp_z", ctypes.c_int), ("grid_cta_y", ctypes.c_int), ("grid_cta_z", ctypes.c_int),
-                ("grid_blocks", ctypes.c_int)]
+                ("grid_blocks", ctypes.c_int), ("factor_subtree_parts", ctypes.c_int),
+                ("factor_subtree_rows", ctypes.c_int)]
 
 
 class GmresReport(ctypes.Structure):
@@ -583,6 +584,27 @@ class ShiftTrainer:
         if self.lib.LLJBASH_ShiftTrainerPredict(self.h, _fp(y)) != 0:
             raise RuntimeError(last_error())
         return y
+
+
+def fill_reducing_order(a: Csr, method: str = "nd"):
+    """CsrNdOrder ("nd") or CsrAmdOrder ("amd") of a's pattern: (p, ip), p[k] the row
+    placed k-th and ip its inverse."""
+    lib = load()
+    p = np.zeros(a.n, np.int32)
+    ip = np.zeros(a.n, np.int32)
+    f = lib.LLJBASH_CsrNdOrder if method == "nd" else lib.LLJBASH_CsrAmdOrder
+    rc = f(HostCsrView(a).ref, _ip(p), _ip(ip))
+    if rc != (1 if method == "nd" else 0):
+        raise RuntimeError(last_error())
+    return p, ip
+
+
+def reorder(a: Csr, method: str = "nd") -> Csr:
+    """P A P^T with the fill-reducing order of `method` (rows sorted by column)."""
+    p, _ = fill_reducing_order(a, method)
+    sp = a.to_scipy()[p][:, p].tocsr()
+    sp.sort_indices()
+    return Csr(a.n, sp.indptr.astype(np.int32), sp.indices.astype(np.int32), sp.data.astype(np.float64))
 
 
 class BatchSolver:

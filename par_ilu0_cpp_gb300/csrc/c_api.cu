@@ -164,7 +164,7 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 s->impl()->factor_kernel = static_cast<int>(value);
                 return 0;
             case LLJBASH_ILU_OPT_TICKET_ORDER:
-                if (value != 0 && value != 1) throw std::runtime_error("ticket order must be 0 or 1");
+                if (value != 0 && value != 1 && value != 2) throw std::runtime_error("ticket order must be 0, 1 or 2");
                 s->impl()->ticket_order = static_cast<int>(value);
                 return 0;
             case LLJBASH_ILU_OPT_GRID:
@@ -378,6 +378,8 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
     info->row_lanes_lower = im->level_packs ? im->L.group : 0;
     info->row_lanes_upper = im->level_packs ? im->U.group : 0;
     info->factor_lane = im->fact_lane ? 1 : 0;
+    info->factor_subtree_parts = im->ticket_order == 2 ? im->sub_parts : 0;
+    info->factor_subtree_rows = im->ticket_order == 2 ? im->sub_rows : 0;
     info->grid_fp64 = im->line_use64;
     info->grid_fp32 = im->line_use32;
     if (im->grid64 || im->grid32) {

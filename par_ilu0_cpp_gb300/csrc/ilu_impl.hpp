@@ -153,7 +153,12 @@ struct IluSolver::Impl {
 
     gb300::DeviceBuffer<int> rp, ci, diag, order_l;
     gb300::DeviceBuffer<int> order_fact;  // ticket order of the factorisation (ticket_order = 1)
-    int ticket_order = 0;  // factorisation tickets: 0 level order, 1 the subtree scheduler's order
+    int ticket_order = 0;  // factorisation tickets: 0 level order, 1 the subtree scheduler's order,
+                           // 2 subtree partitions one CTA each, then the separator rows by tickets
+    gb300::DeviceBuffer<int> sub_part_ptr, sub_grp_ptr, sub_rows_d;  // ticket_order 2: partitions
+    int sub_parts = 0, sub_rows = 0, sub_queue = 0;
+    int sub_warps = 0;      // warps per subtree CTA
+    size_t sub_smem = 0;    // its dynamic shared memory
     // lane-per-row factorisation (factor_lane.cuh) for factors with short rows
     int factor_kernel = 0;  // 0 automatic, 1 warp per row, 2 lane per row (when the rows qualify)
     bool fact_lane = false;

@@ -84,6 +84,176 @@ __device__ __forceinline__ bool gate_closed(const int* gate, int step) {
 // are eliminated in global memory.  Row k's values are read at L2 (ld.cg) after an
 // acquire on its ready flag; row j publishes with fence + release.  `shift` (optional) is
 // added to the diagonal before elimination.
+// Per-warp shared-memory staging of ilu_factor_row (dynamic shared memory of the
+// factorisation kernels, `cap` entries and `hcap` table slots per warp).
+struct FactStage {
+    double* sval;
+    double* sukk;
+    int* scol;
+    int* skd;
+    int* ske;
+    int* hkey;
+    int* hpos;
+};
+
+__device__ __forceinline__ FactStage fact_stage(double* fact_smem, int cap, int hcap) {
+    const int w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const size_t wc = static_cast<size_t>(w) * cap, nc_ = static_cast<size_t>(nw) * cap;
+    FactStage st;
+    st.sval = fact_smem + wc;
+    st.sukk = fact_smem + nc_ + wc;
+    int* ibase = reinterpret_cast<int*>(fact_smem + 2 * nc_);
+    st.scol = ibase + wc;
+    st.skd = ibase + nc_ + wc;
+    st.ske = ibase + 2 * nc_ + wc;
+    st.hkey = ibase + 3 * nc_ + static_cast<size_t>(w) * hcap;
+    st.hpos = ibase + 3 * nc_ + static_cast<size_t>(nw) * hcap + static_cast<size_t>(w) * hcap;
+    return st;
+}
+
+// Elimination of row j by one warp, every pivot row already final (see ilu_factor_kernel).
+template <int PRE>
+__device__ __forceinline__ void ilu_factor_row(int j, const int* __restrict__ rp, const int* __restrict__ ci,
+                                               const int* __restrict__ diag, double* lu,
+                                               const double* __restrict__ shift, int* status, int cap,
+                                               const FactStage& st) {
+    const int lane = threadIdx.x & 31;
+    double* sval = st.sval;
+    double* sukk = st.sukk;
+    int* scol = st.scol;
+    int* skd = st.skd;
+    int* ske = st.ske;
+    int* hkey = st.hkey;
+    int* hpos = st.hpos;
+    const int b = rp[j];
+    const int len = rp[j + 1] - b;
+    const int dloc = diag[j] - b;
+    if (len <= cap) {
+        for (int t = lane; t < len; t += kWarp) {
+            const int c = ci[b + t];
+            scol[t] = c;
+            double v = lu[b + t];
+            if (shift != nullptr && t == dloc) v += shift[j];
+            sval[t] = v;
+            if (t < dloc) {
+                const int kd = diag[c];
+                skd[t] = kd;
+                ske[t] = rp[c + 1];
+                sukk[t] = __ldcg(lu + kd);
+            }
+        }
+        // column -> position table of row j (long rows): hsize slots, a power of two
+        // of at least twice the row length, keys -1 where empty
+        const bool hashed = len > kFactHashMin;
+        int hsize = 0, hshift = 0;
+        if (hashed) {
+            hsize = 64;
+            while (hsize < 2 * len) hsize <<= 1;
+            hshift = 32 - (31 - __clz(hsize));
+            for (int h = lane; h < hsize; h += kWarp) hkey[h] = -1;
+        }
+        __syncwarp();
+        if (hashed) {
+            for (int t = lane; t < len; t += kWarp) {
+                const int c = scol[t];
+                unsigned h = (static_cast<unsigned>(c) * 0x9E3779B1u) >> hshift;
+                while (atomicCAS(hkey + h, -1, c) != -1) h = (h + 1) & static_cast<unsigned>(hsize - 1);
+                hpos[h] = t;
+            }
+            __syncwarp();
+        }
+        // position of column c in row j (c lies beyond position t), -1 if absent
+        auto locate = [&](int c, int t) -> int {
+            if (!hashed) return find_sorted(scol, t + 1, len, c);
+            unsigned h = (static_cast<unsigned>(c) * 0x9E3779B1u) >> hshift;
+            for (int probe = 0; probe < hsize; ++probe) {
+                const int k = hkey[h];
+                if (k == c) return hpos[h];
+                if (k < 0) return -1;
+                h = (h + 1) & static_cast<unsigned>(hsize - 1);
+            }
+            return -1;
+        };
+        // strict-upper entries of pivot row t held by this lane: p = kd + 1 + lane + 32 u
+        int nc[PRE];
+        double nv[PRE];
+        auto load_pivot = [&](int t) {
+            const int p0 = skd[t] + 1 + lane;
+            const int pe = ske[t];
+#pragma unroll
+            for (int u = 0; u < PRE; ++u) {
+                const int p = p0 + u * kWarp;
+                nc[u] = p < pe ? ci[p] : -1;
+                nv[u] = p < pe ? __ldcg(lu + p) : 0.0;
+            }
+        };
+        if (dloc > 0) load_pivot(0);
+        for (int t = 0; t < dloc; ++t) {
+            int cc[PRE];
+            double cv[PRE];
+#pragma unroll
+            for (int u = 0; u < PRE; ++u) {
+                cc[u] = nc[u];
+                cv[u] = nv[u];
+            }
+            if (t + 1 < dloc) load_pivot(t + 1);
+            double l = 0.0;
+            if (lane == 0) {
+                l = sval[t] / sukk[t];
+                sval[t] = l;
+            }
+            l = __shfl_sync(0xffffffffu, l, 0);
+#pragma unroll
+            for (int u = 0; u < PRE; ++u) {
+                if (cc[u] >= 0) {
+                    const int pos = locate(cc[u], t);
+                    if (pos >= 0) sval[pos] = fma(-cv[u], l, sval[pos]);
+                }
+            }
+            // strict-upper entries beyond the register window (long pivot rows)
+            for (int p = skd[t] + 1 + lane + PRE * kWarp; p < ske[t]; p += kWarp) {
+                const int pos = locate(ci[p], t);
+                if (pos >= 0) sval[pos] = fma(-__ldcg(lu + p), l, sval[pos]);
+            }
+            __syncwarp();
+        }
+        for (int t = lane; t < len; t += kWarp) lu[b + t] = sval[t];
+        if (lane == 0) {
+            const double u = sval[dloc];
+            if (!(fabs(u) > 0.0) || !isfinite(u)) {
+                atomicAdd(status + kStatusBreakdowns, 1);
+                atomicMin(status + kStatusFirstBreakdown, j);
+            }
+        }
+    } else {
+        const int* col = ci + b;
+        double* val = lu + b;
+        if (shift != nullptr && lane == 0) __stcg(val + dloc, __ldcg(val + dloc) + shift[j]);
+        __syncwarp();
+        for (int t = 0; t < dloc; ++t) {
+            const int k = col[t];
+            const int kd = diag[k];
+            const int ke = rp[k + 1];
+            const double l = __ldcg(val + t) / __ldcg(lu + kd);
+            __syncwarp();
+            if (lane == 0) __stcg(val + t, l);
+            for (int p = kd + 1 + lane; p < ke; p += kWarp) {
+                const int pos = find_sorted(col, t + 1, len, ci[p]);
+                if (pos >= 0) __stcg(val + pos, fma(-__ldcg(lu + p), l, __ldcg(val + pos)));
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            const double u = __ldcg(val + dloc);
+            if (!(fabs(u) > 0.0) || !isfinite(u)) {
+                atomicAdd(status + kStatusBreakdowns, 1);
+                atomicMin(status + kStatusFirstBreakdown, j);
+            }
+        }
+    }
+}
+
 template <int PRE>
 __global__ void __launch_bounds__(kFactWarps * kWarp)
     ilu_factor_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const int* __restrict__ diag,
@@ -91,154 +261,56 @@ __global__ void __launch_bounds__(kFactWarps * kWarp)
                       int stamp, unsigned* counter, int* status, int cap, int hcap) {
     extern __shared__ double fact_smem[];
     const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const int nw = blockDim.x >> 5;
-    const size_t wc = static_cast<size_t>(w) * cap, nc_ = static_cast<size_t>(nw) * cap;
-    double* sval = fact_smem + wc;
-    double* sukk = fact_smem + nc_ + wc;
-    int* ibase = reinterpret_cast<int*>(fact_smem + 2 * nc_);
-    int* scol = ibase + wc;
-    int* skd = ibase + nc_ + wc;
-    int* ske = ibase + 2 * nc_ + wc;
-    int* hkey = ibase + 3 * nc_ + static_cast<size_t>(w) * hcap;
-    int* hpos = ibase + 3 * nc_ + static_cast<size_t>(nw) * hcap + static_cast<size_t>(w) * hcap;
+    const FactStage st = fact_stage(fact_smem, cap, hcap);
     int q = draw_ticket(counter, n, lane);
     while (q < n) {
         const int qn = draw_ticket(counter, n, lane);
         const int j = order[q];
         const int b = rp[j];
-        const int len = rp[j + 1] - b;
         const int dloc = diag[j] - b;
         for (int t = lane; t < dloc; t += kWarp) wait_flag(done + ci[b + t], stamp, status);
         __syncwarp();
-        if (len <= cap) {
-            for (int t = lane; t < len; t += kWarp) {
-                const int c = ci[b + t];
-                scol[t] = c;
-                double v = lu[b + t];
-                if (shift != nullptr && t == dloc) v += shift[j];
-                sval[t] = v;
-                if (t < dloc) {
-                    const int kd = diag[c];
-                    skd[t] = kd;
-                    ske[t] = rp[c + 1];
-                    sukk[t] = __ldcg(lu + kd);
-                }
-            }
-            // column -> position table of row j (long rows): hsize slots, a power of two
-            // of at least twice the row length, keys -1 where empty
-            const bool hashed = len > kFactHashMin;
-            int hsize = 0, hshift = 0;
-            if (hashed) {
-                hsize = 64;
-                while (hsize < 2 * len) hsize <<= 1;
-                hshift = 32 - (31 - __clz(hsize));
-                for (int h = lane; h < hsize; h += kWarp) hkey[h] = -1;
-            }
-            __syncwarp();
-            if (hashed) {
-                for (int t = lane; t < len; t += kWarp) {
-                    const int c = scol[t];
-                    unsigned h = (static_cast<unsigned>(c) * 0x9E3779B1u) >> hshift;
-                    while (atomicCAS(hkey + h, -1, c) != -1) h = (h + 1) & static_cast<unsigned>(hsize - 1);
-                    hpos[h] = t;
-                }
-                __syncwarp();
-            }
-            // position of column c in row j (c lies beyond position t), -1 if absent
-            auto locate = [&](int c, int t) -> int {
-                if (!hashed) return find_sorted(scol, t + 1, len, c);
-                unsigned h = (static_cast<unsigned>(c) * 0x9E3779B1u) >> hshift;
-                for (int probe = 0; probe < hsize; ++probe) {
-                    const int k = hkey[h];
-                    if (k == c) return hpos[h];
-                    if (k < 0) return -1;
-                    h = (h + 1) & static_cast<unsigned>(hsize - 1);
-                }
-                return -1;
-            };
-            // strict-upper entries of pivot row t held by this lane: p = kd + 1 + lane + 32 u
-            int nc[PRE];
-            double nv[PRE];
-            auto load_pivot = [&](int t) {
-                const int p0 = skd[t] + 1 + lane;
-                const int pe = ske[t];
-#pragma unroll
-                for (int u = 0; u < PRE; ++u) {
-                    const int p = p0 + u * kWarp;
-                    nc[u] = p < pe ? ci[p] : -1;
-                    nv[u] = p < pe ? __ldcg(lu + p) : 0.0;
-                }
-            };
-            if (dloc > 0) load_pivot(0);
-            for (int t = 0; t < dloc; ++t) {
-                int cc[PRE];
-                double cv[PRE];
-#pragma unroll
-                for (int u = 0; u < PRE; ++u) {
-                    cc[u] = nc[u];
-                    cv[u] = nv[u];
-                }
-                if (t + 1 < dloc) load_pivot(t + 1);
-                double l = 0.0;
-                if (lane == 0) {
-                    l = sval[t] / sukk[t];
-                    sval[t] = l;
-                }
-                l = __shfl_sync(0xffffffffu, l, 0);
-#pragma unroll
-                for (int u = 0; u < PRE; ++u) {
-                    if (cc[u] >= 0) {
-                        const int pos = locate(cc[u], t);
-                        if (pos >= 0) sval[pos] = fma(-cv[u], l, sval[pos]);
-                    }
-                }
-                // strict-upper entries beyond the register window (long pivot rows)
-                for (int p = skd[t] + 1 + lane + PRE * kWarp; p < ske[t]; p += kWarp) {
-                    const int pos = locate(ci[p], t);
-                    if (pos >= 0) sval[pos] = fma(-__ldcg(lu + p), l, sval[pos]);
-                }
-                __syncwarp();
-            }
-            for (int t = lane; t < len; t += kWarp) lu[b + t] = sval[t];
-            if (lane == 0) {
-                const double u = sval[dloc];
-                if (!(fabs(u) > 0.0) || !isfinite(u)) {
-                    atomicAdd(status + kStatusBreakdowns, 1);
-                    atomicMin(status + kStatusFirstBreakdown, j);
-                }
-            }
-        } else {
-            const int* col = ci + b;
-            double* val = lu + b;
-            if (shift != nullptr && lane == 0) __stcg(val + dloc, __ldcg(val + dloc) + shift[j]);
-            __syncwarp();
-            for (int t = 0; t < dloc; ++t) {
-                const int k = col[t];
-                const int kd = diag[k];
-                const int ke = rp[k + 1];
-                const double l = __ldcg(val + t) / __ldcg(lu + kd);
-                __syncwarp();
-                if (lane == 0) __stcg(val + t, l);
-                for (int p = kd + 1 + lane; p < ke; p += kWarp) {
-                    const int pos = find_sorted(col, t + 1, len, ci[p]);
-                    if (pos >= 0) __stcg(val + pos, fma(-__ldcg(lu + p), l, __ldcg(val + pos)));
-                }
-                __syncwarp();
-            }
-            if (lane == 0) {
-                const double u = __ldcg(val + dloc);
-                if (!(fabs(u) > 0.0) || !isfinite(u)) {
-                    atomicAdd(status + kStatusBreakdowns, 1);
-                    atomicMin(status + kStatusFirstBreakdown, j);
-                }
-            }
-        }
+        ilu_factor_row<PRE>(j, rp, ci, diag, lu, shift, status, cap, st);
         __threadfence();
         __syncwarp();
         if (lane == 0) st_release(done + j, stamp);
         q = qn;
     }
+}
+
+// Subtree partitions of the elimination tree, one CTA each (the reference's subtree
+// scheduler, src/subtree.hpp tree_schedule, run by src/ilu_solver.cpp:394-443): a row's
+// pivots are its descendants in the elimination tree, so a partition made of whole
+// subtrees depends on no other CTA.  The CTA takes its rows level by level (level groups
+// of the partition, rows of a group independent), one warp per row, a barrier between
+// groups: no ready flags are waited for.  Its rows' flags are set at the end for the
+// separator rows, which ilu_factor_kernel then takes by tickets.  part_ptr[p] .. part_ptr[p+1]
+// are partition p's groups in grp_ptr, whose rows are rows[grp_ptr[g] .. grp_ptr[g+1]).
+constexpr int kSubtreeWarps = 32;  // most warps per CTA of the subtree factorisation kernel
+
+template <int PRE>
+__global__ void __launch_bounds__(kSubtreeWarps * kWarp)
+    ilu_factor_subtree_kernel(const int* __restrict__ part_ptr, const int* __restrict__ grp_ptr,
+                              const int* __restrict__ rows, const int* __restrict__ rp, const int* __restrict__ ci,
+                              const int* __restrict__ diag, double* lu, const double* __restrict__ shift, int* done,
+                              int stamp, int* status, int cap, int hcap) {
+    extern __shared__ double fact_smem[];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const FactStage st = fact_stage(fact_smem, cap, hcap);
+    const int p = blockIdx.x;
+    for (int gidx = part_ptr[p]; gidx < part_ptr[p + 1]; ++gidx) {
+        for (int q = grp_ptr[gidx] + w; q < grp_ptr[gidx + 1]; q += nw)
+            ilu_factor_row<PRE>(rows[q], rp, ci, diag, lu, shift, status, cap, st);
+        // the group's rows (global memory, written by this CTA) before the next group reads them
+        __syncthreads();
+    }
+    __threadfence();
+    __syncthreads();
+    const int r0 = grp_ptr[part_ptr[p]], r1 = grp_ptr[part_ptr[p + 1]];
+    for (int q = r0 + threadIdx.x; q < r1; q += blockDim.x) done[rows[q]] = stamp;
+    (void)lane;
 }
 
 // Level-ordered packed triangular factor (default substitution layout).  Rows are taken in the

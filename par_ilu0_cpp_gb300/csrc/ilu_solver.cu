@@ -1101,6 +1101,8 @@ void IluSolver::SetupMatrix() {
     im.diag.upload(im.an.diag.data(), static_cast<size_t>(n), s);
     im.order_l.upload(im.an.order_l.data(), static_cast<size_t>(n), s);
     std::vector<int> tree_order;  // the factorisation's ticket order when ticket_order == 1
+    im.sub_parts = 0;
+    im.sub_rows = 0;
     if (im.ticket_order == 1 && n > 0) {
         // the reference's subtree schedule (one worker per SM): the workers' subtree rows
         // interleaved round-robin (rows of different subtrees are independent), then the
@@ -1248,7 +1250,7 @@ void IluSolver::SetupMatrix() {
     // Factorisation kernel: warp per row (automatic), or lane per row for short rows when
     // requested
     im.fact_lane = false;
-    if (im.factor_kernel == 2 && n > 0)
+    if (im.factor_kernel == 2 && im.ticket_order != 2 && n > 0)
         im.fact_lane = build_lane_factor(n, rp, ci, im.an.diag,
                                          im.ticket_order == 1 ? tree_order : im.an.order_l, im, s);
     // Factorisation launch: rows staged in shared memory up to the longest row where a
@@ -1282,6 +1284,66 @@ void IluSolver::SetupMatrix() {
         int per_sm = 0;
         GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * kWarp, im.fact_smem));
         im.grid_fact = std::max(1, per_sm) * im.dev.sms;
+    }
+    if (im.ticket_order == 2 && n > 0) {
+        // subtree partitions, one CTA each (ilu_factor_subtree_kernel): the reference's
+        // subtree scheduler with one worker per SM (fewer for small matrices: about 256
+        // rows per worker; with more workers than SMs its subtree division leaves the large
+        // matrices measured here without partitions), each run by a CTA of up to
+        // kSubtreeWarps warps; each partition's rows grouped by level depth; the remaining
+        // (separator) rows by tickets in level order (any topological order is
+        // deadlock-free, level order keeps the most rows ready)
+        const int workers = std::max(1, std::min(im.dev.sms, n / 256));
+        const TreeScheduleResult ts =
+            tree_schedule(n, gl, workers, 1, 1.0, RowWeights{rp, im.an.diag.data(), 0, 1});
+        const int np = ts.nproc;
+        std::vector<int> part_ptr(1, 0), grp_ptr(1, 0), rows;
+        rows.reserve(static_cast<size_t>(n));
+        for (int w = 0; w < np; ++w) {
+            const int a0 = ts.part_ptr[static_cast<size_t>(w)], a1 = ts.part_ptr[static_cast<size_t>(w) + 1];
+            if (a1 <= a0) continue;
+            std::vector<int> pr(ts.partitions.begin() + a0, ts.partitions.begin() + a1);
+            std::stable_sort(pr.begin(), pr.end(), [&](int x, int y) { return im.an.depth_l[x] < im.an.depth_l[y]; });
+            for (size_t k = 0; k < pr.size(); ++k) {
+                if (k > 0 && im.an.depth_l[pr[k]] != im.an.depth_l[pr[k - 1]]) grp_ptr.push_back(static_cast<int>(rows.size()));
+                rows.push_back(pr[k]);
+            }
+            grp_ptr.push_back(static_cast<int>(rows.size()));
+            part_ptr.push_back(static_cast<int>(grp_ptr.size()) - 1);
+        }
+        im.sub_parts = static_cast<int>(part_ptr.size()) - 1;
+        im.sub_rows = static_cast<int>(rows.size());
+        {
+            // every pivot of a partition row lies in the same partition (whole subtrees of
+            // the elimination tree): the kernel waits for no other CTA
+            std::vector<int> owner(static_cast<size_t>(n), -1);
+            for (int pp = 0; pp < im.sub_parts; ++pp)
+                for (int q = grp_ptr[static_cast<size_t>(part_ptr[static_cast<size_t>(pp)])];
+                     q < grp_ptr[static_cast<size_t>(part_ptr[static_cast<size_t>(pp) + 1])]; ++q)
+                    owner[static_cast<size_t>(rows[static_cast<size_t>(q)])] = pp;
+            for (int j = 0; j < n; ++j) {
+                if (owner[static_cast<size_t>(j)] < 0) continue;
+                for (int t = rp[j]; t < im.an.diag[static_cast<size_t>(j)]; ++t)
+                    if (owner[static_cast<size_t>(ci[t])] != owner[static_cast<size_t>(j)])
+                        throw std::runtime_error("subtree partition is not closed under the row's pivots");
+            }
+        }
+        std::vector<int> queue(ts.partitions.begin() + ts.part_ptr[static_cast<size_t>(np)], ts.partitions.end());
+        std::stable_sort(queue.begin(), queue.end(), [&](int x, int y) { return im.an.depth_l[x] < im.an.depth_l[y]; });
+        if (im.sub_rows + static_cast<int>(queue.size()) != n)
+            throw std::runtime_error("tree schedule partitions do not cover the rows");
+        im.sub_part_ptr.upload(part_ptr.data(), part_ptr.size(), s);
+        im.sub_grp_ptr.upload(grp_ptr.data(), grp_ptr.size(), s);
+        im.sub_rows_d.upload(rows.data(), std::max<size_t>(rows.size(), 1), s);
+        im.order_fact.upload(queue.data(), std::max<size_t>(queue.size(), 1), s);
+        im.sub_queue = static_cast<int>(queue.size());
+        GB_CUDA_CHECK(cudaStreamSynchronize(s));  // host vectors must outlive the copies
+        auto sk = im.fact_pre == 8 ? ilu_factor_subtree_kernel<8> : ilu_factor_subtree_kernel<2>;
+        const size_t per_warp = im.fact_smem / static_cast<size_t>(im.fact_warps);
+        im.sub_warps = std::max(1, std::min<int>(kSubtreeWarps, static_cast<int>(kFactSmemMax / per_warp)));
+        im.sub_smem = per_warp * static_cast<size_t>(im.sub_warps);
+        GB_CUDA_CHECK(cudaFuncSetAttribute(sk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(im.sub_smem)));
     }
     // Level-ordered kernels: warps draw tasks in level order and spin on the rows they
     // depend on.  Rows of one lane poll in rounds and want many warps ahead (1,216 warps
@@ -1358,12 +1420,30 @@ bool IluSolver::FactorizeFrom(const double* values, bool on_device) {
                 im.launches += 2;
             }
             auto kern = im.fact_pre == 8 ? ilu_factor_kernel<8> : ilu_factor_kernel<2>;
-            if (!im.fact_lane) kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
-                n, im.rp.get(), im.ci.get(), im.diag.get(),
-                im.ticket_order == 1 ? im.order_fact.get() : im.order_l.get(), im.lu.get(), shift, im.done.get(),
-                im.stamp, im.counters.get(), im.status.get(), im.fact_cap, im.fact_hcap);
+            if (!im.fact_lane && im.ticket_order == 2) {
+                // subtree partitions first (one CTA each, no waits), then the separator rows
+                if (im.sub_parts > 0) {
+                    auto sk = im.fact_pre == 8 ? ilu_factor_subtree_kernel<8> : ilu_factor_subtree_kernel<2>;
+                    sk<<<im.sub_parts, im.sub_warps * kWarp, im.sub_smem, s>>>(
+                        im.sub_part_ptr.get(), im.sub_grp_ptr.get(), im.sub_rows_d.get(), im.rp.get(), im.ci.get(),
+                        im.diag.get(), im.lu.get(), shift, im.done.get(), im.stamp, im.status.get(), im.fact_cap,
+                        im.fact_hcap);
+                    im.launches += 1;
+                }
+                if (im.sub_queue > 0) {
+                    kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
+                        im.sub_queue, im.rp.get(), im.ci.get(), im.diag.get(), im.order_fact.get(), im.lu.get(), shift,
+                        im.done.get(), im.stamp, im.counters.get(), im.status.get(), im.fact_cap, im.fact_hcap);
+                    im.launches += 1;
+                }
+            } else if (!im.fact_lane) {
+                kern<<<im.grid_fact, im.fact_warps * kWarp, im.fact_smem, s>>>(
+                    n, im.rp.get(), im.ci.get(), im.diag.get(),
+                    im.ticket_order == 1 ? im.order_fact.get() : im.order_l.get(), im.lu.get(), shift, im.done.get(),
+                    im.stamp, im.counters.get(), im.status.get(), im.fact_cap, im.fact_hcap);
+                im.launches += 1;
+            }
             GB_CUDA_CHECK(cudaGetLastError());
-            if (!im.fact_lane) im.launches += 1;
             if (im.blk64) {
                 gather_block(im.LB64, true, im.lu.get(), s, im.dev.sms);
                 gather_block(im.UB64, false, im.lu.get(), s, im.dev.sms);

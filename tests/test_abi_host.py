@@ -251,9 +251,9 @@ def test_ilu_option_values_checked():
         for v in (-3, 9, 1.5):
             with pytest.raises(RuntimeError):
                 ilu.set_option(opt, v)
-    for v in (0, 1):
+    for v in (0, 1, 2):
         ilu.set_option(api.ILU_OPT_TICKET_ORDER, v)
     with pytest.raises(RuntimeError):
-        ilu.set_option(api.ILU_OPT_TICKET_ORDER, 2)
+        ilu.set_option(api.ILU_OPT_TICKET_ORDER, 3)
     with pytest.raises(RuntimeError):
         ilu.set_option(12345, 1)

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import ragged
+from conftest import ragged, rel_err
 from par_ilu0_cpp_gb300 import api
 from par_ilu0_cpp_gb300 import generators as g
 
@@ -72,7 +72,7 @@ def test_factorisation_in_subtree_schedule_order(name, make):
     factors of the level order bit for bit."""
     f = make()
     out = []
-    for order in (0, 1):
+    for order in (0, 1, 2):
         ilu = api.IluSolver()
         ilu.set_option(api.ILU_OPT_TICKET_ORDER, order)
         ilu.set_matrix(f)
@@ -80,3 +80,42 @@ def test_factorisation_in_subtree_schedule_order(name, make):
         assert ilu.factorize() == 0, api.last_error()
         out.append(ilu.values())
     assert np.array_equal(out[0], out[1])
+    assert np.array_equal(out[0], out[2])
+
+
+SUBTREE_MATS = [
+    ("convdiff3d_32_nd", lambda: api.reorder(g.convdiff3d(32), "nd")),
+    ("laplace2d_96_nd", lambda: api.reorder(g.laplace2d(96), "nd")),
+    ("lognormal27_12_ilu1_nd", lambda: api.iluk_symbolic(api.reorder(g.lognormal27(12, seed=3), "nd"), 1)[0]),
+    ("convdiff3d_24_amd", lambda: api.reorder(g.convdiff3d(24), "amd")),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,make", SUBTREE_MATS, ids=[m[0] for m in SUBTREE_MATS])
+def test_subtree_partitions_one_cta_each(name, make):
+    """Fill-reducing orders give the elimination tree wide independent subtrees: most rows
+    are factorised by subtree CTAs without waiting on any other CTA, and the factors (and
+    the substitution) are those of the level-ordered kernel bit for bit, 1e-12 against the
+    oracle."""
+    import oracle
+
+    f = make()
+    ref = api.IluSolver()
+    ref.set_matrix(f)
+    assert ref.setup() == 0 and ref.factorize() == 0, api.last_error()
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_TICKET_ORDER, 2)
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0, api.last_error()
+    assert ilu.factorize() == 0, api.last_error()
+    info = ilu.info()
+    assert info.factor_subtree_parts > 1 and info.factor_subtree_rows > f.n // 2, (info.factor_subtree_parts,
+                                                                                  info.factor_subtree_rows)
+    assert np.array_equal(ilu.values(), ref.values())
+    oracle.build_port()
+    port = oracle.Port()
+    lu, _ = port.factorize(f)
+    assert rel_err(ilu.values(), lu, floor=1e-300) <= 1e-12
+    b = np.random.default_rng(3).uniform(-1, 1, f.n)
+    assert np.array_equal(ilu.substitute(b), ref.substitute(b))
