@@ -1620,14 +1620,21 @@ void IluSolver::SubstituteDeviceNoAlloc(const double* d_b, double* d_x) {
     fill_sentinel(y, n, s, im.dev.sms);
     fill_sentinel(d_x, n, s, im.dev.sms);
     double* b = const_cast<double*>(d_b);  // read only: no scale is passed to the forward sweep
-    if (im.blk64) {
+    // each sweep on the schedule the solver uses for it (line-pipeline, block-local or
+    // level-ordered; a level-synchronous solver's level packs give the same results)
+    if (im.line_use64 & 1)
+        launch_line<double, false>(im.GP, s, b, nullptr, y, counters + 1, status, nullptr, 0);
+    else if (im.blk64)
         launch_block<double, false>(im.LB64, s, b, nullptr, y, counters + 1, status, nullptr, 0);
-        launch_block<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
-    } else if (im.L.ntask > 0) {
+    else if (im.L.ntask > 0)
         launch_level_lower<double>(im.L, im.grid_solve, im.solve_threads, s, b, nullptr, y, counters + 1, status,
                                    nullptr, 0);
+    if (im.line_use64 & 2)
+        launch_line<double, true>(im.GP, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
+    else if (im.blk64)
+        launch_block<double, true>(im.UB64, s, y, nullptr, d_x, counters + 2, status, nullptr, 0);
+    else if (im.U.ntask > 0)
         launch_level_upper<double>(im.U, im.grid_solve, im.solve_threads, s, y, d_x, counters + 2, status, nullptr, 0);
-    }
     GB_CUDA_CHECK(cudaGetLastError());
     int h[kStatusWords];
     GB_CUDA_CHECK(cudaMemcpyAsync(h, status, sizeof(h), cudaMemcpyDeviceToHost, s));

@@ -220,10 +220,18 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
 #pragma unroll 1
     for (int t = 0; t < R - 1; ++t) issue(t);
     // face reads: edge lanes at x' (clamped: no read outside the face where the lane has no
-    // row), the other lanes from a word that holds 0
+    // row), the other lanes from a word that holds 0; each step's values are loaded one
+    // step ahead, so that the check for a late predecessor is resolved off the chain
     const T* const fy_rd = y_edge ? fy : zero_word;
     const T* const fz_rd = z_edge ? fz : zero_word;
     const int fy_st = y_edge ? wz : 0, fz_st = z_edge ? wy : 0;
+    auto face_at = [&](int t, const T* base, int st) -> const T* {
+        const int xq = t - skew;
+        return base + (static_cast<unsigned>(xq) < span ? xq : 0) * st;
+    };
+    T pfy = ld_volatile_shared(face_at(0, fy_rd, fy_st));
+    T pfz = ld_volatile_shared(face_at(0, fz_rd, fz_st));
+    T* out_p = out0 - static_cast<long long>(sx) * skew;  // row of step s: out_p (advanced by sx per step)
     T prev = T(0);  // the lane's result of the previous step (0 where it had no row)
 #pragma unroll 2
     for (int s = 0; s < steps; ++s) {
@@ -234,29 +242,35 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
         issue(s + R - 1);  // into the slot read one step ago
         const int xq = s - skew;
         const bool act = static_cast<unsigned>(xq) < span;
-        const int xc = act ? xq : 0;
-        const T fyv = ld_volatile_shared(fy_rd + xc * fy_st);
-        const T fzv = ld_volatile_shared(fz_rd + xc * fz_st);
+        T fyv = pfy, fzv = pfz;
+        pfy = ld_volatile_shared(face_at(s + 1, fy_rd, fy_st));
+        pfz = ld_volatile_shared(face_at(s + 1, fz_rd, fz_st));
+        const bool late = act && (Sentinel<T>::is(fyv) || Sentinel<T>::is(fzv));
         const T sh_y = __shfl_up_sync(0xffffffffu, prev, 1);
         const T sh_z = __shfl_up_sync(0xffffffffu, prev, wy);
-        T vy = y_edge ? fyv : (ny > 1 ? sh_y : T(0));
-        T vz = z_edge ? fzv : sh_z;
-        const bool late = act && (Sentinel<T>::is(vy) || Sentinel<T>::is(vz));
-        if (__any_sync(0xffffffffu, late)) {  // a predecessor is not there yet
-            if (late && Sentinel<T>::is(vy)) vy = line_wait_shared(fy_rd + xc * fy_st, status);
-            if (late && Sentinel<T>::is(vz)) vz = line_wait_shared(fz_rd + xc * fz_st, status);
-        }
-        T acc = scaled ? bv * sc : bv;
         const T xin = xq > 0 ? prev : T(0);
-        const long long off = static_cast<long long>(sx) * xq;
-        acc = fma(-c.cz, vz, acc);
-        acc = fma(-c.cy, vy, acc);
-        acc = fma(-c.cx, xin, acc);
-        // FP64: the reference's division (lanes without a row divide by 1: no slow path);
-        // FP32 (mixed path): d holds 1 / u_ii
-        if constexpr (UPPER) acc = sizeof(T) == 8 ? acc / (act ? c.d : T(1)) : acc * c.d;
-        const T r = Sentinel<T>::canon(acc);
-        st_relaxed_if(act, out0 + off, r);
+        const T a0 = scaled ? bv * sc : bv;
+        auto row = [&](T fy_v, T fz_v) -> T {
+            const T vy = y_edge ? fy_v : (ny > 1 ? sh_y : T(0));
+            const T vz = z_edge ? fz_v : sh_z;
+            T acc = fma(-c.cz, vz, a0);
+            acc = fma(-c.cy, vy, acc);
+            acc = fma(-c.cx, xin, acc);
+            // FP64: the reference's division (lanes without a row divide by 1: no slow
+            // path); FP32 (mixed path): d holds 1 / u_ii
+            if constexpr (UPPER) acc = sizeof(T) == 8 ? acc / (act ? c.d : T(1)) : acc * c.d;
+            return Sentinel<T>::canon(acc);
+        };
+        T r = row(fyv, fzv);
+        if (__any_sync(0xffffffffu, late)) {  // a predecessor was not there yet: wait, redo
+            const int xc = act ? xq : 0;
+            if (late && Sentinel<T>::is(fyv)) fyv = line_wait_shared(fy_rd + xc * fy_st, status);
+            if (late && Sentinel<T>::is(fzv)) fzv = line_wait_shared(fz_rd + xc * fz_st, status);
+            r = row(fyv, fzv);
+        }
+        st_relaxed_if(act, out_p, r);
+        out_p += sx;
+        const int xc = act ? xq : 0;
         st_shared_if(act && fy_out != nullptr, fy_out + xc * wz, r);
         st_shared_if(act && fz_out != nullptr, fz_out + xc * wy, r);
         prev = act ? r : T(0);

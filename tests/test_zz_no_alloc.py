@@ -58,10 +58,11 @@ class _DeviceArray:
         self.rt.cudaFree(self.ptr)
 
 
-def _solver(a, block_rows=0, solve_warps=0):
+def _solver(a, block_rows=0, solve_warps=0, grid=0):
     f, _ = api.iluk_symbolic(a, 0)
     ilu = api.IluSolver()
     ilu.set_option(api.ILU_OPT_BLOCK_ROWS, block_rows)
+    ilu.set_option(api.ILU_OPT_GRID, grid)
     if solve_warps:
         ilu.set_option(api.ILU_OPT_SOLVE_WARPS, solve_warps)
     ilu.set_matrix(f)
@@ -83,7 +84,10 @@ CASES = [("laplace2d_64_auto", lambda: g.laplace2d(64), 0),
          ("convdiff3d_20_block", lambda: g.convdiff3d(20), 800),
          ("convdiff3d_20_level", lambda: g.convdiff3d(20), -1),
          ("lognormal27_8_auto", lambda: g.lognormal27(8, seed=2), 0),
-         ("lognormal27_8_level", lambda: g.lognormal27(8, seed=2), -1)]
+         ("lognormal27_8_level", lambda: g.lognormal27(8, seed=2), -1),
+         # line-pipeline sweeps forced for both sweeps (no block-local or level packs)
+         ("laplace2d_64_line", lambda: g.laplace2d(64), "line"),
+         ("convdiff3d_20_line", lambda: g.convdiff3d(20), "line")]
 
 
 @pytest.mark.parametrize("name,make,block_rows", CASES, ids=[c[0] for c in CASES])
@@ -91,11 +95,13 @@ def test_no_alloc_substitution_matches_existing_entry_point(name, make, block_ro
     lib = api.load()
     rt = _cudart()
     a = make()
-    ilu = _solver(a, block_rows)
+    ilu = _solver(a, 0, grid=1) if block_rows == "line" else _solver(a, block_rows)
     info = ilu.info()
+    if block_rows == "line":
+        assert info.grid_fp64 == 3
     if block_rows == -1:
         assert info.block_rows_fp64 == 0  # level-ordered kernel
-    elif block_rows > 0:
+    elif block_rows != "line" and block_rows > 0:
         assert info.block_rows_fp64 == block_rows  # block-local kernel
     rng = np.random.default_rng(11)
     rhs = [rng.uniform(-1, 1, a.n), rng.uniform(-1, 1, a.n)]
