@@ -149,19 +149,24 @@ def algorithmic_bytes(kind, a, nnz_l, nnz_u, tsize, steps_hist):
     return None
 
 
-def measured_traffic(kernel, size, block_rows, cluster):
+def measured_traffic(kernel, size, block_rows, cluster, line=False):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of `kernel`
     for this workload and substitution schedule, from the ncu captures recorded in
-    profiles/dram_traffic.json (entries: kernel, size, block_rows, cluster, bytes,
-    command); None when no capture matches the kernel and schedule that ran."""
+    profiles/dram_traffic.json (entries: kernel, size, schedule "line" or block_rows /
+    cluster of the block-local kernel, bytes, source); None when no capture matches the
+    kernel and schedule that ran."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if not os.path.isfile(path):
         return None
     with open(path) as fh:
         entries = json.load(fh).get("captures", [])
     for e in entries:
-        if (e.get("kernel") == kernel and e.get("size") == size and e.get("block_rows") == block_rows
-                and e.get("cluster") == cluster):
+        if e.get("kernel") != kernel or e.get("size") != size:
+            continue
+        if line and e.get("schedule") == "line":
+            return int(e["bytes"])
+        if not line and e.get("schedule", "block") == "block" and e.get("block_rows") == block_rows \
+                and e.get("cluster") == cluster:
             return int(e["bytes"])
     return None
 
@@ -642,8 +647,13 @@ def run_ours(args):
     achieved = prof[dom]["gbs"]
     info_m = solvers["mixed"][0].info()
     schedule = {"fp64_block_rows": int(info_m.block_rows_fp64), "fp32_block_rows": int(info_m.block_rows_fp32),
-                "fp64_cluster": int(info_m.block_cluster_fp64), "fp32_cluster": int(info_m.block_cluster_fp32)}
-    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"], schedule["fp32_cluster"])
+                "fp64_cluster": int(info_m.block_cluster_fp64), "fp32_cluster": int(info_m.block_cluster_fp32),
+                # line-pipeline sweeps (bit 0 forward, bit 1 backward), chosen by timing at setup
+                "fp64_line": int(info_m.grid_fp64), "fp32_line": int(info_m.grid_fp32),
+                "line_shape": [int(info_m.grid_warp_y), int(info_m.grid_warp_z), int(info_m.grid_cta_y),
+                               int(info_m.grid_cta_z), int(info_m.grid_blocks)]}
+    dom_line = bool(schedule["fp32_line"] & (1 if dom == "sptrsv_lower" else 2 if dom == "sptrsv_upper" else 0))
+    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"], schedule["fp32_cluster"], dom_line)
 
     batched = None
     others = None

@@ -232,7 +232,7 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
     T pfy = ld_volatile_shared(face_at(0, fy_rd, fy_st));
     T pfz = ld_volatile_shared(face_at(0, fz_rd, fz_st));
     T* out_p = out0 - static_cast<long long>(sx) * skew;  // row of step s: out_p (advanced by sx per step)
-    T prev = T(0);  // the lane's result of the previous step (0 where it had no row)
+    T prev = T(0);  // the lane's result of the previous step (used only where it had a row)
 #pragma unroll 2
     for (int s = 0; s < steps; ++s) {
         cp_async_wait<R - 2>();  // step s has landed
@@ -259,7 +259,7 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
             // FP64: the reference's division (lanes without a row divide by 1: no slow
             // path); FP32 (mixed path): d holds 1 / u_ii
             if constexpr (UPPER) acc = sizeof(T) == 8 ? acc / (act ? c.d : T(1)) : acc * c.d;
-            return Sentinel<T>::canon(acc);
+            return acc;
         };
         T r = row(fyv, fzv);
         if (__any_sync(0xffffffffu, late)) {  // a predecessor was not there yet: wait, redo
@@ -268,12 +268,16 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
             if (late && Sentinel<T>::is(fzv)) fzv = line_wait_shared(fz_rd + xc * fz_st, status);
             r = row(fyv, fzv);
         }
-        st_relaxed_if(act, out_p, r);
+        // the next step reads r directly (an active lane's shuffle partners and its own
+        // previous step are active at the same x'); only the stored copies, which other
+        // warps and blocks poll, are kept off the sentinel
+        prev = r;
+        const T rs_ = Sentinel<T>::canon(r);
+        st_relaxed_if(act, out_p, rs_);
         out_p += sx;
         const int xc = act ? xq : 0;
-        st_shared_if(act && fy_out != nullptr, fy_out + xc * wz, r);
-        st_shared_if(act && fz_out != nullptr, fz_out + xc * wy, r);
-        prev = act ? r : T(0);
+        st_shared_if(act && fy_out != nullptr, fy_out + xc * wz, rs_);
+        st_shared_if(act && fz_out != nullptr, fz_out + xc * wy, rs_);
     }
     cp_async_wait<0>();
 }
