@@ -121,7 +121,11 @@ enum {
      * automatic) and 1: one warp per row; 2: one lane per row when no row has more than
      * 16 entries (each finished row publishes u_kk and its upper entries, rows waiting for
      * it poll exactly those values), else one warp per row.  Next IluSolverSetup. */
-    LLJBASH_ILU_OPT_FACTOR_KERNEL = 12
+    LLJBASH_ILU_OPT_FACTOR_KERNEL = 12,
+    /* line-pipeline sweeps in thread-block clusters of 8 CTAs along z, the handoffs inside
+     * a cluster through distributed shared memory: 1 (default) where such clusters can
+     * be scheduled, 0 never.  Results are the same.  Next IluSolverSetup. */
+    LLJBASH_ILU_OPT_GRID_CLUSTER = 13
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 
@@ -189,6 +193,7 @@ typedef struct LLJBASH_IluInfo {
     int grid_cta_y;       /* warps of a CTA along y and z */
     int grid_cta_z;
     int grid_blocks;      /* CTA-sized blocks of grid lines */
+    int grid_cluster;     /* CTAs per thread-block cluster of the line-pipeline sweeps, 0: none */
     int factor_subtree_parts; /* ticket order 2: subtree partitions (one CTA each) and their rows */
     int factor_subtree_rows;
 } LLJBASH_IluInfo;

@@ -55,7 +55,7 @@ class IluInfo(ctypes.Structure):
                 ("grid_nx", ctypes.c_int),
                 ("grid_ny", ctypes.c_int), ("grid_nz", ctypes.c_int), ("grid_warp_y", ctypes.c_int),
                 ("grid_warp_z", ctypes.c_int), ("grid_cta_y", ctypes.c_int), ("grid_cta_z", ctypes.c_int),
-                ("grid_blocks", ctypes.c_int), ("factor_subtree_parts", ctypes.c_int),
+                ("grid_blocks", ctypes.c_int), ("grid_cluster", ctypes.c_int), ("factor_subtree_parts", ctypes.c_int),
                 ("factor_subtree_rows", ctypes.c_int)]
 
 
@@ -74,6 +74,7 @@ ILU_OPT_GRID = 6
 ILU_OPT_GRID_WARP_Y = 7
 ILU_OPT_GRID_CTA_Y = 8
 ILU_OPT_GRID_CTA_Z = 9
+ILU_OPT_GRID_CLUSTER = 13
 ILU_OPT_TICKET_ORDER = 11
 ILU_OPT_FACTOR_KERNEL = 12
 GMRES_OPT_MODE = 1

@@ -183,6 +183,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 (option == LLJBASH_ILU_OPT_GRID_CTA_Y ? s->impl()->grid_by : s->impl()->grid_bz) =
                     static_cast<int>(value);
                 return 0;
+            case LLJBASH_ILU_OPT_GRID_CLUSTER:
+                if (value != 0 && value != 1) throw std::runtime_error("grid clusters must be 0 or 1");
+                s->impl()->grid_cluster = static_cast<int>(value);
+                return 0;
             default:
                 g_last_error = "unknown ILU option";
                 return -1;
@@ -391,6 +395,7 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
         info->grid_cta_y = im->GP.g.by;
         info->grid_cta_z = im->GP.g.bz;
         info->grid_blocks = im->GP.g.nblk;
+        info->grid_cluster = im->GP.g.cl;
     }
     return 0;
 }

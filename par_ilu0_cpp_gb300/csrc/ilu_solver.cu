@@ -855,35 +855,93 @@ static LineGeom line_geometry(int nx, int ny, int nz, int wy_req, int by_req, in
 }
 
 // Tickets of the block grid in dependency order: anti-diagonals iy + iz ascending (the
-// same in the sweep coordinates of L and U).
+// same in the sweep coordinates of L and U); with clusters of cl blocks along z, the
+// tickets are clusters (iy, izc), along the anti-diagonals of the cluster grid.
 static std::vector<int> line_block_order(const LineGeom& g) {
+    const int nz_units = g.cl > 0 ? g.nbzc : g.nbz;
     std::vector<int> o;
-    o.reserve(static_cast<size_t>(g.nblk));
-    for (int d = 0; d < g.nby + g.nbz - 1; ++d)
-        for (int iz = 0; iz < g.nbz; ++iz) {
+    o.reserve(static_cast<size_t>(g.nby) * nz_units);
+    for (int d = 0; d < g.nby + nz_units - 1; ++d)
+        for (int iz = 0; iz < nz_units; ++iz) {
             const int iy = d - iz;
             if (iy >= 0 && iy < g.nby) o.push_back(iy + g.nby * iz);
         }
     return o;
 }
 
+static cudaLaunchConfig_t line_cluster_config(int grid, int threads, size_t smem, int cl, cudaStream_t s,
+                                              cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(grid));
+    cfg.blockDim = dim3(static_cast<unsigned>(threads));
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cl);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
 // Raises the kernels' shared-memory limit, sizes the grid and allocates the packed
-// operands of value type T; false when a CTA cannot be resident.
+// operands of value type T; false when a CTA cannot be resident.  With G.g.cl > 0 the
+// cluster variant is sized (clusters of cl CTAs along z); `try_cluster` (first type
+// configured) decides G.g.cl: clusters of 8 where the grid has at least two blocks along z
+// and such a cluster can be scheduled, else none.
 template <class T>
-static bool configure_line(LinePack& G, const DeviceInfo& dev) {
+static bool configure_line(LinePack& G, const DeviceInfo& dev, bool try_cluster) {
     const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
     if (smem + 1024 > static_cast<size_t>(dev.smem_optin)) return false;
-    int per_sm = 0;
-    for (bool upper : {false, true}) {
-        const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_kernel<T, true>)
-                                 : reinterpret_cast<const void*>(sptrsv_line_kernel<T, false>);
-        GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-        int r = 0;
-        GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, G.threads, smem));
-        if (r < 1) return false;
-        per_sm = per_sm == 0 ? r : std::min(per_sm, r);
+    if (try_cluster) {
+        G.g.cl = 0;
+        G.g.nbzc = 0;
+        if (G.g.nbz >= 2) {
+            const int cl = std::min(8, G.g.nbz);
+            const int nbzc = ceil_div(G.g.nbz, cl);
+            int ok = 1;
+            int nclusters = 1 << 30;
+            for (bool upper : {false, true}) {
+                const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, true>)
+                                         : reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, false>);
+                GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+                cudaLaunchAttribute attr[1];
+                cudaLaunchConfig_t cfg = line_cluster_config(G.g.nby * nbzc * cl, G.threads, smem, cl, nullptr, attr);
+                int nc = 0;
+                if (cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) != cudaSuccess) {
+                    cudaGetLastError();
+                    nc = 0;
+                }
+                if (nc < 1) ok = 0;
+                nclusters = std::min(nclusters, nc);
+            }
+            if (ok) {
+                G.g.cl = cl;
+                G.g.nbzc = nbzc;
+                G.grid = std::min(nclusters, G.g.nby * nbzc) * cl;
+            }
+        }
     }
-    G.grid = std::min(G.g.nblk, per_sm * dev.sms);
+    if (G.g.cl > 0) {
+        for (bool upper : {false, true}) {
+            const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, true>)
+                                     : reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, false>);
+            GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        }
+    } else {
+        int per_sm = 0;
+        for (bool upper : {false, true}) {
+            const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_kernel<T, true>)
+                                     : reinterpret_cast<const void*>(sptrsv_line_kernel<T, false>);
+            GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+            int r = 0;
+            GB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, G.threads, smem));
+            if (r < 1) return false;
+            per_sm = per_sm == 0 ? r : std::min(per_sm, r);
+        }
+        G.grid = std::min(G.g.nblk, per_sm * dev.sms);
+    }
     const size_t len = static_cast<size_t>(G.g.slots()) * 4;
     if constexpr (sizeof(T) == 8) {
         G.l64.reserve(len);
@@ -912,8 +970,15 @@ template <class T, bool UPPER>
 static void launch_line(const LinePack& G, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
                         int* status, const int* gate, int step) {
     const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
-    sptrsv_line_kernel<T, UPPER><<<G.grid, G.threads, smem, s>>>(G.view<T>(UPPER), in, scale, out, counter, status,
-                                                                  gate, step);
+    if (G.g.cl > 0) {
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = line_cluster_config(G.grid, G.threads, smem, G.g.cl, s, attr);
+        GB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, sptrsv_line_cluster_kernel<T, UPPER>, G.view<T>(UPPER), in, scale, out,
+                                         counter, status, gate, step));
+    } else {
+        sptrsv_line_kernel<T, UPPER><<<G.grid, G.threads, smem, s>>>(G.view<T>(UPPER), in, scale, out, counter,
+                                                                      status, gate, step);
+    }
     GB_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -1155,13 +1220,13 @@ void IluSolver::SetupMatrix() {
             for (int attempt = 0; attempt < 8; ++attempt) {
                 im.GP.g = line_geometry(gx, gy, gz, im.grid_wy, by, bz);
                 im.GP.threads = (im.GP.g.nw() + 1) * kWarp;  // compute warps + the halo warp
-                im.grid64 = configure_line<double>(im.GP, im.dev);
+                im.grid64 = configure_line<double>(im.GP, im.dev, im.grid_cluster != 0);
                 if (im.grid64 || im.GP.g.nw() == 1) break;
                 by = im.GP.g.by;
                 bz = im.GP.g.bz;
                 (bz >= by ? bz : by) = std::max(1, (bz >= by ? bz : by) / 2);
             }
-            im.grid32 = configure_line<float>(im.GP, im.dev);
+            im.grid32 = configure_line<float>(im.GP, im.dev, false);
             const std::vector<int> order = line_block_order(im.GP.g);
             im.GP.order.upload(order.data(), order.size(), s);
             GB_CUDA_CHECK(cudaStreamSynchronize(s));  // `order` must outlive the copy

@@ -50,6 +50,8 @@ struct LineGeom {
     int nby = 1, nbz = 1; // blocks along y / z
     int steps = 0;        // steps of a warp: nx + wy + wz - 2
     int nblk = 0;         // nby * nbz
+    int cl = 0;           // CTAs per thread-block cluster (consecutive blocks along z), 0: none
+    int nbzc = 0;         // clusters along z: ceil(nbz / cl)
     __host__ __device__ int nw() const { return by * bz; }
     // Slot of lane `lane` of warp w of block b at step s in the packed operand stream.
     __host__ __device__ long long slot(int b, int w, int s, int lane) const {
@@ -61,7 +63,8 @@ struct LineGeom {
 template <class T>
 struct LineTri {
     LineGeom g;
-    const int* order = nullptr;  // [nblk] block (iy + nby iz, sweep coordinates) of each ticket
+    const int* order = nullptr;  // [nblk] block (iy + nby iz, sweep coordinates) of each ticket;
+                                 // with clusters [nby nbzc]: cluster (iy + nby izc) of each ticket
     const T* coef = nullptr;     // [slots][4]: c_z, c_y, c_x, d (d: u_ii FP64 / RN(1 / u_ii) FP32; L: unused)
 };
 
@@ -109,6 +112,17 @@ __device__ __forceinline__ void st_shared_if(bool on, double* p, double v) {
 __device__ __forceinline__ void st_shared_if(bool on, float* p, float v) {
     asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.volatile.shared.f32 [%1], %2; }" ::"r"(static_cast<unsigned>(on)),
                  "r"(static_cast<unsigned>(__cvta_generic_to_shared(p))), "f"(v));
+}
+
+__device__ __forceinline__ void st_cluster_if(bool on, unsigned addr, double v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.relaxed.cluster.shared::cluster.f64 [%1], %2; }" ::"r"(
+                     static_cast<unsigned>(on)),
+                 "r"(addr), "d"(v));
+}
+__device__ __forceinline__ void st_cluster_if(bool on, unsigned addr, float v) {
+    asm volatile("{ .reg .pred q; setp.ne.u32 q, %0, 0; @q st.relaxed.cluster.shared::cluster.f32 [%1], %2; }" ::"r"(
+                     static_cast<unsigned>(on)),
+                 "r"(addr), "f"(v));
 }
 
 // Waits (bounded) until the shared-memory value *p is no longer the sentinel; after many
@@ -166,7 +180,8 @@ __host__ __device__ inline long long line_smem_bytes(const LineGeom& g) {
 // at the grid's boundary.
 template <class T, bool UPPER>
 __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, bool scaled, T sc, T* out, T* faceY,
-                                          T* faceZ, const T* zero_word, LineCoef<T>* cring, T* bring, int* status) {
+                                          T* faceZ, const T* zero_word, LineCoef<T>* cring, T* bring,
+                                          unsigned fz_remote, int* status) {
     constexpr int R = kLineRing<T>;
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
@@ -194,6 +209,11 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
     const T* fz = faceZ + w * fsz + yy;  // stride wy per x'
     T* const fy_out = (ny > 1 && yy == wy - 1 && wyi < by - 1) ? faceY + (w + 1) * fsy + zz : nullptr;
     T* const fz_out = (zz == wz - 1 && wzi < bz - 1) ? faceZ + (w + by) * fsz + yy : nullptr;
+    // cluster variant: the last warps along z push into the next CTA of the cluster (its
+    // warp (wyi, 0) slot), fz_remote being that CTA's faceZ in the cluster's shared window
+    const unsigned fz_push = (fz_remote != 0u && zz == wz - 1 && wzi == bz - 1)
+                                 ? fz_remote + static_cast<unsigned>((wyi * fsz + yy) * static_cast<long long>(sizeof(T)))
+                                 : 0u;
     const LineCoef<T>* const cs = reinterpret_cast<const LineCoef<T>*>(P.coef) + P.g.slot(blk, w, 0, lane);
     LineCoef<T>* const cr = cring + w * 32 + lane;  // slot k at cr[k * nw * 32]
     T* const br = bring + w * 32 + lane;
@@ -278,6 +298,7 @@ __device__ __forceinline__ void line_warp(const LineTri<T>& P, int blk, T* in, b
         const int xc = act ? xq : 0;
         st_shared_if(act && fy_out != nullptr, fy_out + xc * wz, rs_);
         st_shared_if(act && fz_out != nullptr, fz_out + xc * wy, rs_);
+        st_cluster_if(act && fz_push != 0u, fz_push + static_cast<unsigned>(xc * wy * static_cast<int>(sizeof(T))), rs_);
     }
     cp_async_wait<0>();
 }
@@ -326,7 +347,7 @@ __device__ __forceinline__ bool halo_retire(HaloCursor<T>& h, int nx, const T (&
 
 template <class T, bool UPPER>
 __device__ __forceinline__ void line_halo(const LineTri<T>& P, int blk, const T* out, T* faceY, T* faceZ,
-                                          int* status) {
+                                          bool z_from_l2, int* status) {
     const int lane = threadIdx.x & 31;
     const int nx = P.g.nx, ny = P.g.ny, nz = P.g.nz;
     const int wy = P.g.wy, wz = P.g.wz, by = P.g.by, bz = P.g.bz;
@@ -347,7 +368,7 @@ __device__ __forceinline__ void line_halo(const LineTri<T>& P, int blk, const T*
             hy.stride = wz;
         }
     }
-    if (iz > 0 && lane < by * wy) {  // line (y, z0 - 1) of block (iy, iz - 1)
+    if (z_from_l2 && iz > 0 && lane < by * wy) {  // line (y, z0 - 1) of block (iy, iz - 1)
         const int wyi = lane / wy, yy = lane % wy;
         const int ys = (iy * by + wyi) * wy + yy;
         if (ys < ny) {
@@ -371,6 +392,36 @@ __device__ __forceinline__ void line_halo(const LineTri<T>& P, int blk, const T*
             for (; hz.src != nullptr && hz.x < nx; ++hz.x) st_volatile_shared(hz.dst + static_cast<long long>(hz.x) * hz.stride, T(0));
             break;
         }
+    }
+}
+
+// Resets a block's faces: the sentinel where a value will be written, 0 where the lines
+// lie at the grid's boundary (slots of the first warps along y / z of the first blocks).
+template <class T>
+__device__ __forceinline__ void line_reset_faces(const LineGeom& g, int iy, int iz, T* faceY, T* zero_word) {
+    const long long fsy = line_face_slot_y(g), fsz = line_face_slot_z(g);
+    const long long fy_len = g.nw() * fsy;
+    const long long face_len = line_face_len<T>(g);
+    for (long long i = threadIdx.x; i < face_len; i += blockDim.x) {
+        const bool zero = i < fy_len ? (iy == 0 && static_cast<int>(i / fsy) % g.by == 0)
+                                     : (iz == 0 && static_cast<int>((i - fy_len) / fsz) / g.by == 0);
+        faceY[i] = zero ? T(0) : Sentinel<T>::value();
+    }
+    if (threadIdx.x == 0) *zero_word = T(0);
+}
+
+// GMRES normalises its new Krylov vector in the forward sweep: the block's rows of `in`
+// (planes z of its z-lines, rows of its y-lines: contiguous runs) are rescaled in one
+// coalesced pass once every warp is done reading them (the same product b * scale the
+// rows used).  Called after a barrier.
+template <class T>
+__device__ __forceinline__ void line_rescale_block(const LineGeom& g, int iy, int iz, T* in, T sc) {
+    const int y0 = iy * g.by * g.wy, y1 = min(g.ny, y0 + g.by * g.wy);
+    const int z0 = iz * g.bz * g.wz, z1 = min(g.nz, z0 + g.bz * g.wz);
+    const long long run = static_cast<long long>(g.nx) * (y1 - y0);
+    for (int z = z0; z < z1; ++z) {
+        T* p = in + static_cast<long long>(g.nx) * (y0 + static_cast<long long>(g.ny) * z);
+        for (long long i = threadIdx.x; i < run; i += blockDim.x) p[i] = p[i] * sc;
     }
 }
 
@@ -401,14 +452,7 @@ __global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
          tk = draw_block_ticket(counter, P.g.nblk, &s_ticket)) {
         const int blk = P.order[tk];
         const int iy = blk % P.g.nby, iz = blk / P.g.nby;
-        // faces: the sentinel where a value will be written, 0 where the lines lie at the
-        // grid's boundary (slots of the first warps along y / z of the first blocks)
-        for (long long i = threadIdx.x; i < face_len; i += blockDim.x) {
-            const bool zero = i < fy_len ? (iy == 0 && static_cast<int>(i / fsy) % P.g.by == 0)
-                                         : (iz == 0 && static_cast<int>((i - fy_len) / fsz) / P.g.by == 0);
-            faceY[i] = zero ? T(0) : Sentinel<T>::value();
-        }
-        if (threadIdx.x == 0) *zero_word = T(0);
+        line_reset_faces<T>(P.g, iy, iz, faceY, zero_word);
         // stream the warps' operands into L2 (the right-hand side was written by the
         // previous kernel and is there already)
         if (w < nw)
@@ -417,23 +461,84 @@ __global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
                               threadIdx.x & 31);
         __syncthreads();
         if (w < nw)
-            line_warp<T, UPPER>(P, blk, in, scaled, sc, out, faceY, faceZ, zero_word, cring, bring, status);
+            line_warp<T, UPPER>(P, blk, in, scaled, sc, out, faceY, faceZ, zero_word, cring, bring, 0u, status);
         else
-            line_halo<T, UPPER>(P, blk, out, faceY, faceZ, status);
+            line_halo<T, UPPER>(P, blk, out, faceY, faceZ, true, status);
         if (scaled) {
-            // GMRES normalises its new Krylov vector in the forward sweep: the block's rows
-            // of `in` (planes z of its z-lines, rows of its y-lines: contiguous runs) are
-            // rescaled in one coalesced pass once every warp is done reading them (the same
-            // product b * scale the rows used)
             __syncthreads();
-            const int y0 = iy * P.g.by * P.g.wy, y1 = min(P.g.ny, y0 + P.g.by * P.g.wy);
-            const int z0 = iz * P.g.bz * P.g.wz, z1 = min(P.g.nz, z0 + P.g.bz * P.g.wz);
-            const long long run = static_cast<long long>(P.g.nx) * (y1 - y0);
-            for (int z = z0; z < z1; ++z) {
-                T* p = in + static_cast<long long>(P.g.nx) * (y0 + static_cast<long long>(P.g.ny) * z);
-                for (long long i = threadIdx.x; i < run; i += blockDim.x) p[i] = p[i] * sc;
+            line_rescale_block<T>(P.g, iy, iz, in, sc);
+        }
+    }
+}
+
+// Cluster variant: launched with clusters of g.cl CTAs; the cluster of ticket q takes the
+// blocks (iy, izc cl + rank) of cluster q (tickets along anti-diagonals of the cluster
+// grid: a cluster only waits for clusters of smaller tickets, whose CTAs are running or
+// done; the CTAs of one cluster are co-scheduled).  A CTA's last warps along z push
+// their results into the next CTA's face in distributed shared memory, so only the first
+// CTA of a cluster and the y-direction take their predecessors from L2 (halo warp).
+template <class T, bool UPPER>
+__global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
+    sptrsv_line_cluster_kernel(LineTri<T> P, T* in, const double* scale, T* out, unsigned* counter, int* status,
+                               const int* gate, int step) {
+    if (gate_closed(gate, step)) return;
+    extern __shared__ __align__(16) unsigned char line_smem[];
+    const int nw = P.g.nw();
+    const long long fy_len = static_cast<long long>(nw) * line_face_slot_y(P.g);
+    const long long face_len = line_face_len<T>(P.g);
+    T* faceY = reinterpret_cast<T*>(line_smem);
+    T* faceZ = faceY + fy_len;
+    T* zero_word = faceY + face_len;
+    LineCoef<T>* cring = reinterpret_cast<LineCoef<T>*>(line_smem + line_ring_offset<T>(P.g));
+    T* bring = reinterpret_cast<T*>(cring + static_cast<long long>(kLineRing<T>) * nw * 32);
+    __shared__ int s_ticket;
+    const bool scaled = !UPPER && scale != nullptr;
+    const T sc = scaled ? static_cast<T>(*scale) : T(1);
+    const int w = threadIdx.x >> 5;
+    const unsigned rank = cluster_rank_u32();
+    const unsigned CL = cluster_size_u32();
+    const int nq = P.g.nby * P.g.nbzc;
+    const int nclusters = static_cast<int>(gridDim.x / CL);
+    for (;;) {
+        // the previous round is complete in every CTA of the cluster (no push in flight)
+        // before the ticket and the faces are reset
+        cluster_sync_all();
+        if (rank == 0 && threadIdx.x == 0) {
+            const int q = static_cast<int>(atomicAdd(counter, 1u));
+            if (q == nq + nclusters - 1) atomicExch(counter, 0u);
+            for (unsigned r = 0; r < CL; ++r) st_cluster(map_shared_rank(&s_ticket, r), q);
+        }
+        cluster_sync_all();
+        const int q = *reinterpret_cast<volatile int*>(&s_ticket);
+        if (q >= nq) break;
+        const int cb = P.order[q];
+        const int iy = cb % P.g.nby;
+        const int iz = (cb / P.g.nby) * static_cast<int>(CL) + static_cast<int>(rank);
+        const bool active = iz < P.g.nbz;
+        const int blk = iy + P.g.nby * iz;
+        if (active) {
+            line_reset_faces<T>(P.g, iy, iz, faceY, zero_word);
+            if (w < nw)
+                prefetch_l2_range(P.coef + P.g.slot(blk, w, 0, 0) * 4,
+                                  static_cast<long long>(P.g.steps) * 128 * static_cast<long long>(sizeof(T)),
+                                  threadIdx.x & 31);
+        }
+        __syncthreads();
+        // every face of the cluster is reset before any CTA pushes into it
+        cluster_sync_all();
+        if (active) {
+            const bool push = rank + 1 < CL && iz + 1 < P.g.nbz;
+            const unsigned remote = push ? map_shared_rank(faceZ, rank + 1) : 0u;
+            if (w < nw)
+                line_warp<T, UPPER>(P, blk, in, scaled, sc, out, faceY, faceZ, zero_word, cring, bring, remote, status);
+            else
+                line_halo<T, UPPER>(P, blk, out, faceY, faceZ, rank == 0, status);
+            if (scaled) {
+                __syncthreads();
+                line_rescale_block<T>(P.g, iy, iz, in, sc);
             }
         }
+        __syncthreads();
     }
 }
 

@@ -26,9 +26,10 @@ def port():
     return oracle.Port()
 
 
-def solver(f, grid=1, wy=0, by=0, bz=0, block_rows=0):
+def solver(f, grid=1, wy=0, by=0, bz=0, block_rows=0, cluster=1):
     ilu = api.IluSolver()
     ilu.set_option(api.ILU_OPT_GRID, grid)
+    ilu.set_option(api.ILU_OPT_GRID_CLUSTER, cluster)
     ilu.set_option(api.ILU_OPT_GRID_WARP_Y, wy)
     ilu.set_option(api.ILU_OPT_GRID_CTA_Y, by)
     ilu.set_option(api.ILU_OPT_GRID_CTA_Z, bz)
@@ -71,6 +72,9 @@ def test_grid_sweep_matches_other_schedules_and_oracle(port, name, make):
 
 TUNINGS = [dict(wy=1, by=1, bz=1), dict(wy=4, by=3, bz=2), dict(wy=4), dict(wy=8, by=2, bz=4),
            dict(wy=1, by=8, bz=1), dict(wy=8, by=4, bz=2), dict(wy=8, by=1, bz=1), dict(wy=1, by=2, bz=4)]
+
+
+TUNINGS = TUNINGS + [dict(k, cluster=0) for k in TUNINGS[:4]]
 
 
 @pytest.mark.parametrize("kw", TUNINGS, ids=[str(k) for k in TUNINGS])
@@ -159,3 +163,23 @@ def test_grid_detection_rejects_other_patterns():
     for name, f in cases.items():
         ilu = solver(f)
         assert ilu.info().grid_fp64 == 0, name
+
+
+@pytest.mark.parametrize("make", [lambda: g.convdiff3d(40, 24, 70), lambda: g.laplace2d(90, 300)],
+                         ids=["convdiff3d_40x24x70", "laplace2d_90x300"])
+def test_grid_clusters_match_plain_line_kernel(make):
+    """Thread-block clusters along z (handoffs in distributed shared memory, the cluster's
+    first CTA and the y-direction through L2) give the results of the plain line kernel and
+    of the block-local kernel, including a last cluster that is only partly filled."""
+    a = make()
+    f, _ = api.iluk_symbolic(a, 0)
+    ref = solver(f, grid=-1)
+    plain = solver(f, cluster=0)
+    clus = solver(f, cluster=1, bz=1)
+    assert plain.info().grid_cluster == 0 and clus.info().grid_cluster > 1
+    assert clus.info().grid_blocks % clus.info().grid_cluster != 0 or clus.info().grid_blocks > clus.info().grid_cluster
+    _, b = g.random_rhs(a, seed=21)
+    x = ref.substitute(b)
+    assert np.array_equal(plain.substitute(b), x)
+    assert np.array_equal(clus.substitute(b), x)
+    assert np.array_equal(clus.substitute(b), x)
