@@ -552,6 +552,8 @@ def run_ours(args):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
         rc = ilu.factorize_device(dev["fv"].data_ptr())
+        if rc != 0:
+            raise RuntimeError(f"{name} factorisation failed: rc={rc} {api.last_error()}")
         ok, its = gm.solve_device(a.n, dev["rp"].data_ptr(), dev["ci"].data_ptr(), dev["av"].data_ptr(),
                                   dev["b"].data_ptr(), dev["x"].data_ptr())
         e1.record()

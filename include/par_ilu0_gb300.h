@@ -123,8 +123,9 @@ enum {
      * it poll exactly those values), else one warp per row.  Next IluSolverSetup. */
     LLJBASH_ILU_OPT_FACTOR_KERNEL = 12,
     /* line-pipeline sweeps in thread-block clusters of 8 CTAs along z, the handoffs inside
-     * a cluster through distributed shared memory: 1 (default) where such clusters can
-     * be scheduled, 0 never.  Results are the same.  Next IluSolverSetup. */
+     * a cluster through distributed shared memory: 1 (default) clusters of 16 CTAs, else
+     * of 8, where such clusters can be scheduled; 2 .. 16 clusters of at most that many
+     * CTAs; 0 never.  Results are the same.  Next IluSolverSetup. */
     LLJBASH_ILU_OPT_GRID_CLUSTER = 13
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);

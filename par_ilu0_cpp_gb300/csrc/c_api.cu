@@ -184,7 +184,8 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                     static_cast<int>(value);
                 return 0;
             case LLJBASH_ILU_OPT_GRID_CLUSTER:
-                if (value != 0 && value != 1) throw std::runtime_error("grid clusters must be 0 or 1");
+                if (value < 0 || value > 16 || value != static_cast<int>(value))
+                    throw std::runtime_error("grid clusters must be 0 (none), 1 (automatic) or 2 .. 16 CTAs");
                 s->impl()->grid_cluster = static_cast<int>(value);
                 return 0;
             default:

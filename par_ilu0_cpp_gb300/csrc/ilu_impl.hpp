@@ -189,7 +189,7 @@ struct IluSolver::Impl {
     int grid_wy = 0;    // requested lanes of a warp along y (0 automatic)
     int grid_by = 0;    // requested warps of a CTA along y (0 automatic)
     int grid_bz = 0;    // requested warps of a CTA along z (0 automatic)
-    int grid_cluster = 1;  // 1: thread-block clusters along z where they can be scheduled, 0: none
+    int grid_cluster = 1;  // 1: clusters along z of 16, else 8 CTAs; 2 .. 16: at most that many; 0: none
     // line-pipeline sweeps in use per value type (bit 0: forward, bit 1: backward); in
     // automatic mode chosen at the first Factorize after SetupMatrix by timing each sweep
     // against the block-local / level-ordered kernel

@@ -888,17 +888,21 @@ static cudaLaunchConfig_t line_cluster_config(int grid, int threads, size_t smem
 // Raises the kernels' shared-memory limit, sizes the grid and allocates the packed
 // operands of value type T; false when a CTA cannot be resident.  With G.g.cl > 0 the
 // cluster variant is sized (clusters of cl CTAs along z); `try_cluster` (first type
-// configured) decides G.g.cl: clusters of 8 where the grid has at least two blocks along z
-// and such a cluster can be scheduled, else none.
+// configured) decides G.g.cl: with `max_cluster` 1, clusters of 16, else 8, where the grid
+// has at least two blocks along z and such a cluster can be scheduled; with 2 .. 16,
+// clusters of at most that many CTAs; with 0, none.
 template <class T>
-static bool configure_line(LinePack& G, const DeviceInfo& dev, bool try_cluster) {
+static bool configure_line(LinePack& G, const DeviceInfo& dev, bool try_cluster, int max_cluster) {
     const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
     if (smem + 1024 > static_cast<size_t>(dev.smem_optin)) return false;
     if (try_cluster) {
         G.g.cl = 0;
         G.g.nbzc = 0;
-        if (G.g.nbz >= 2) {
-            const int cl = std::min(8, G.g.nbz);
+        // clusters of 16 (non-portable) where they can be scheduled, else of 8
+        const int wants[2] = {max_cluster == 1 ? 16 : max_cluster, max_cluster == 1 ? 8 : 0};
+        for (int want : wants) {
+            if (want < 2 || G.g.nbz < 2 || G.g.cl > 0) break;
+            const int cl = std::min(want, G.g.nbz);
             const int nbzc = ceil_div(G.g.nbz, cl);
             int ok = 1;
             int nclusters = 1 << 30;
@@ -906,6 +910,7 @@ static bool configure_line(LinePack& G, const DeviceInfo& dev, bool try_cluster)
                 const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, true>)
                                          : reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, false>);
                 GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+                if (cl > 8) GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
                 cudaLaunchAttribute attr[1];
                 cudaLaunchConfig_t cfg = line_cluster_config(G.g.nby * nbzc * cl, G.threads, smem, cl, nullptr, attr);
                 int nc = 0;
@@ -928,6 +933,7 @@ static bool configure_line(LinePack& G, const DeviceInfo& dev, bool try_cluster)
             const void* kern = upper ? reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, true>)
                                      : reinterpret_cast<const void*>(sptrsv_line_cluster_kernel<T, false>);
             GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+            if (G.g.cl > 8) GB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         }
     } else {
         int per_sm = 0;
@@ -1220,13 +1226,13 @@ void IluSolver::SetupMatrix() {
             for (int attempt = 0; attempt < 8; ++attempt) {
                 im.GP.g = line_geometry(gx, gy, gz, im.grid_wy, by, bz);
                 im.GP.threads = (im.GP.g.nw() + 1) * kWarp;  // compute warps + the halo warp
-                im.grid64 = configure_line<double>(im.GP, im.dev, im.grid_cluster != 0);
+                im.grid64 = configure_line<double>(im.GP, im.dev, true, im.grid_cluster);
                 if (im.grid64 || im.GP.g.nw() == 1) break;
                 by = im.GP.g.by;
                 bz = im.GP.g.bz;
                 (bz >= by ? bz : by) = std::max(1, (bz >= by ? bz : by) / 2);
             }
-            im.grid32 = configure_line<float>(im.GP, im.dev, false);
+            im.grid32 = configure_line<float>(im.GP, im.dev, false, 0);
             const std::vector<int> order = line_block_order(im.GP.g);
             im.GP.order.upload(order.data(), order.size(), s);
             GB_CUDA_CHECK(cudaStreamSynchronize(s));  // `order` must outlive the copy

@@ -251,10 +251,11 @@ def test_ilu_option_values_checked():
         for v in (-3, 9, 1.5):
             with pytest.raises(RuntimeError):
                 ilu.set_option(opt, v)
-    for v in (0, 1):
+    for v in (0, 1, 2, 8, 16):
         ilu.set_option(api.ILU_OPT_GRID_CLUSTER, v)
-    with pytest.raises(RuntimeError):
-        ilu.set_option(api.ILU_OPT_GRID_CLUSTER, 2)
+    for v in (-1, 17, 2.5):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_GRID_CLUSTER, v)
     for v in (0, 1, 2):
         ilu.set_option(api.ILU_OPT_TICKET_ORDER, v)
     with pytest.raises(RuntimeError):

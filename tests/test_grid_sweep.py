@@ -167,7 +167,8 @@ def test_grid_detection_rejects_other_patterns():
 
 @pytest.mark.parametrize("make", [lambda: g.convdiff3d(40, 24, 70), lambda: g.laplace2d(90, 300)],
                          ids=["convdiff3d_40x24x70", "laplace2d_90x300"])
-def test_grid_clusters_match_plain_line_kernel(make):
+@pytest.mark.parametrize("cluster", [1, 3, 8])
+def test_grid_clusters_match_plain_line_kernel(make, cluster):
     """Thread-block clusters along z (handoffs in distributed shared memory, the cluster's
     first CTA and the y-direction through L2) give the results of the plain line kernel and
     of the block-local kernel, including a last cluster that is only partly filled."""
@@ -175,9 +176,11 @@ def test_grid_clusters_match_plain_line_kernel(make):
     f, _ = api.iluk_symbolic(a, 0)
     ref = solver(f, grid=-1)
     plain = solver(f, cluster=0)
-    clus = solver(f, cluster=1, bz=1)
+    clus = solver(f, cluster=cluster, bz=1)
     assert plain.info().grid_cluster == 0 and clus.info().grid_cluster > 1
-    assert clus.info().grid_blocks % clus.info().grid_cluster != 0 or clus.info().grid_blocks > clus.info().grid_cluster
+    if cluster > 1:
+        assert clus.info().grid_cluster <= cluster
+        assert clus.info().grid_blocks > clus.info().grid_cluster
     _, b = g.random_rhs(a, seed=21)
     x = ref.substitute(b)
     assert np.array_equal(plain.substitute(b), x)
