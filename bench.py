@@ -152,9 +152,10 @@ def algorithmic_bytes(kind, a, nnz_l, nnz_u, tsize, steps_hist):
 def measured_traffic(kernel, size, block_rows, cluster, line=False):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of `kernel`
     for this workload and substitution schedule, from the ncu captures recorded in
-    profiles/dram_traffic.json (entries: kernel, size, schedule "line" or block_rows /
-    cluster of the block-local kernel, bytes, source); None when no capture matches the
-    kernel and schedule that ran."""
+    profiles/dram_traffic.json (entries: kernel, size, schedule "line" with the CTAs per
+    cluster of the line-pipeline kernel (0: none), or block_rows / cluster of the
+    block-local kernel, bytes, source); None when no capture matches the kernel and
+    schedule that ran."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if not os.path.isfile(path):
         return None
@@ -163,7 +164,7 @@ def measured_traffic(kernel, size, block_rows, cluster, line=False):
     for e in entries:
         if e.get("kernel") != kernel or e.get("size") != size:
             continue
-        if line and e.get("schedule") == "line":
+        if line and e.get("schedule") == "line" and e.get("cluster", 0) == cluster:
             return int(e["bytes"])
         if not line and e.get("schedule", "block") == "block" and e.get("block_rows") == block_rows \
                 and e.get("cluster") == cluster:
@@ -520,6 +521,7 @@ def run_ours(args):
 
     def make(mode):
         ilu = api.IluSolver()
+        ilu.set_option(api.ILU_OPT_GRID_CLUSTER, args.line_cluster)
         ilu.set_matrix(f)
         assert ilu.setup() == 0, api.last_error()
         ilu.set_option(api.ILU_OPT_COPY_BACK, 0)
@@ -613,6 +615,7 @@ def run_ours(args):
     # live in the solver's own (page-locked) GetMatrix() storage.
     e2e_ms = []
     ilu_h = api.IluSolver()
+    ilu_h.set_option(api.ILU_OPT_GRID_CLUSTER, args.line_cluster)
     ilu_h.set_matrix(f)
     assert ilu_h.setup() == 0
     gm_h = api.Gmres(tol, RESTART, MAXIT)
@@ -653,9 +656,11 @@ def run_ours(args):
                 # line-pipeline sweeps (bit 0 forward, bit 1 backward), chosen by timing at setup
                 "fp64_line": int(info_m.grid_fp64), "fp32_line": int(info_m.grid_fp32),
                 "line_shape": [int(info_m.grid_warp_y), int(info_m.grid_warp_z), int(info_m.grid_cta_y),
-                               int(info_m.grid_cta_z), int(info_m.grid_blocks)]}
+                               int(info_m.grid_cta_z), int(info_m.grid_blocks)],
+                "line_cluster": int(info_m.grid_cluster)}
     dom_line = bool(schedule["fp32_line"] & (1 if dom == "sptrsv_lower" else 2 if dom == "sptrsv_upper" else 0))
-    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"], schedule["fp32_cluster"], dom_line)
+    traffic = measured_traffic(dom, args.size, schedule["fp32_block_rows"],
+                               schedule["line_cluster"] if dom_line else schedule["fp32_cluster"], dom_line)
 
     batched = None
     others = None
@@ -712,6 +717,9 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the batched and secondary configurations")
     ap.add_argument("--batch-systems", type=int, default=512)
     ap.add_argument("--batch-rhs", type=int, default=16)
+    ap.add_argument("--line-cluster", type=int, default=1,
+                    help="CTAs per thread-block cluster of the line-pipeline sweeps: 1 automatic (16, else 8), "
+                         "2-16 at most that many, 0 none")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
