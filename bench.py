@@ -522,6 +522,8 @@ def run_ours(args):
     def make(mode):
         ilu = api.IluSolver()
         ilu.set_option(api.ILU_OPT_GRID_CLUSTER, args.line_cluster)
+        ilu.set_option(api.ILU_OPT_GRID_CTA_Y, args.line_cta[0])
+        ilu.set_option(api.ILU_OPT_GRID_CTA_Z, args.line_cta[1])
         ilu.set_matrix(f)
         assert ilu.setup() == 0, api.last_error()
         ilu.set_option(api.ILU_OPT_COPY_BACK, 0)
@@ -616,6 +618,8 @@ def run_ours(args):
     e2e_ms = []
     ilu_h = api.IluSolver()
     ilu_h.set_option(api.ILU_OPT_GRID_CLUSTER, args.line_cluster)
+    ilu_h.set_option(api.ILU_OPT_GRID_CTA_Y, args.line_cta[0])
+    ilu_h.set_option(api.ILU_OPT_GRID_CTA_Z, args.line_cta[1])
     ilu_h.set_matrix(f)
     assert ilu_h.setup() == 0
     gm_h = api.Gmres(tol, RESTART, MAXIT)
@@ -720,6 +724,8 @@ def main():
     ap.add_argument("--line-cluster", type=int, default=1,
                     help="CTAs per thread-block cluster of the line-pipeline sweeps: 1 automatic (16, else 8), "
                          "2-16 at most that many, 0 none")
+    ap.add_argument("--line-cta", type=lambda v: [int(t) for t in v.split(",")], default=[0, 0],
+                    help="warps of a line-pipeline CTA along y,z (0,0: automatic)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -126,7 +126,10 @@ enum {
      * a cluster through distributed shared memory: 1 (default) clusters of 16 CTAs, else
      * of 8, where such clusters can be scheduled; 2 .. 16 clusters of at most that many
      * CTAs; 0 never.  Results are the same.  Next IluSolverSetup. */
-    LLJBASH_ILU_OPT_GRID_CLUSTER = 13
+    LLJBASH_ILU_OPT_GRID_CLUSTER = 13,
+    /* 1: record a per-block timeline of every line-pipeline sweep (read with
+     * LLJBASH_IluSolverGetSweepTimeline); 0 (default) off.  Next IluSolverSetup. */
+    LLJBASH_ILU_OPT_SWEEP_TIMELINE = 14
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 
@@ -199,6 +202,15 @@ typedef struct LLJBASH_IluInfo {
     int factor_subtree_rows;
 } LLJBASH_IluInfo;
 int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info);
+
+/* Per-block timeline of the last line-pipeline sweep of one kind (upper: 0 forward /
+ * 1 backward; fp32: 0 FP64 / 1 FP32), recorded with LLJBASH_ILU_OPT_SWEEP_TIMELINE on:
+ * 12 values per block (sweep coordinates, block iy + nby iz): [0] compute start
+ * (%globaltimer ns), [1] SM id, [2 + w] end of compute warp w, [2 + warps] end of the
+ * block's halo warp, the rest 0.  Waits for the device, copies nblocks * 12 values into
+ * `out` (capacity `cap`; NULL only queries) and returns nblocks; -1 when no timeline
+ * was recorded.  A diagnostic: no counterpart in the reference. */
+int LLJBASH_IluSolverGetSweepTimeline(IluSolverHdl hdl, int upper, int fp32, unsigned long long* out, int cap);
 
 /* Integer results of SetupMatrix's analysis (each array of length n, any may be NULL):
  * diagonal positions, Liu elimination-tree parents of the lower DAG and of the

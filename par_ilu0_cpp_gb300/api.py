@@ -75,6 +75,8 @@ ILU_OPT_GRID_WARP_Y = 7
 ILU_OPT_GRID_CTA_Y = 8
 ILU_OPT_GRID_CTA_Z = 9
 ILU_OPT_GRID_CLUSTER = 13
+ILU_OPT_SWEEP_TIMELINE = 14
+LINE_TIMELINE_WORDS = 12  # values per block of a sweep timeline
 ILU_OPT_TICKET_ORDER = 11
 ILU_OPT_FACTOR_KERNEL = 12
 GMRES_OPT_MODE = 1
@@ -132,6 +134,8 @@ def load() -> ctypes.CDLL:
         "LLJBASH_IluSolverSetShift": (ctypes.c_int, [ctypes.c_void_p, _D]),
         "LLJBASH_IluSolverGetInfo": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(IluInfo)]),
         "LLJBASH_IluSolverGetAnalysis": (ctypes.c_int, [ctypes.c_void_p, _I, _I, _I, _I, _I]),
+        "LLJBASH_IluSolverGetSweepTimeline": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                             ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
         "LLJBASH_Gb300AnalyzePattern": (ctypes.c_int, [ctypes.c_int, _I, _I, _I, _I, _I, _I, _I, _I]),
         "LLJBASH_Gb300TreeSchedule": (ctypes.c_int, [ctypes.c_int, _I, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                      ctypes.c_double, _I, _I, _I, _I, _I, _I]),
@@ -401,6 +405,20 @@ class IluSolver:
         if rc != 0:
             raise RuntimeError(last_error())
         return outs
+
+    def sweep_timeline(self, upper: bool, fp32: bool) -> np.ndarray:
+        """Per-block timeline [nblocks, 12] (uint64) of the last line-pipeline sweep of
+        this kind: compute start (ns), SM id, end of each compute warp, end of the halo
+        warp (LLJBASH_IluSolverGetSweepTimeline)."""
+        nblk = self.lib.LLJBASH_IluSolverGetSweepTimeline(self.h, int(upper), int(fp32), None, 0)
+        if nblk < 0:
+            raise RuntimeError(last_error())
+        out = np.zeros((nblk, LINE_TIMELINE_WORDS), dtype=np.uint64)
+        rc = self.lib.LLJBASH_IluSolverGetSweepTimeline(
+            self.h, int(upper), int(fp32), out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), out.size)
+        if rc < 0:
+            raise RuntimeError(last_error())
+        return out
 
 
 @dataclass

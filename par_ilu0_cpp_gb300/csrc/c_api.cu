@@ -183,6 +183,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 (option == LLJBASH_ILU_OPT_GRID_CTA_Y ? s->impl()->grid_by : s->impl()->grid_bz) =
                     static_cast<int>(value);
                 return 0;
+            case LLJBASH_ILU_OPT_SWEEP_TIMELINE:
+                if (value != 0 && value != 1) throw std::runtime_error("sweep timeline must be 0 or 1");
+                s->impl()->sweep_timeline = value != 0;
+                return 0;
             case LLJBASH_ILU_OPT_GRID_CLUSTER:
                 if (value < 0 || value > 16 || value != static_cast<int>(value))
                     throw std::runtime_error("grid clusters must be 0 (none), 1 (automatic) or 2 .. 16 CTAs");
@@ -399,6 +403,32 @@ int LLJBASH_IluSolverGetInfo(IluSolverHdl hdl, LLJBASH_IluInfo* info) {
         info->grid_cluster = im->GP.g.cl;
     }
     return 0;
+}
+
+int LLJBASH_IluSolverGetSweepTimeline(IluSolverHdl hdl, int upper, int fp32, unsigned long long* out, int cap) {
+    try {
+        const auto* im = ilu(hdl)->impl();
+        if (!im) throw std::runtime_error("SetupMatrix() has not been called");
+        const auto& buf = im->GP.tl[fp32 ? 1 : 0][upper ? 1 : 0];
+        if (buf.get() == nullptr)
+            throw std::runtime_error(
+                "no sweep timeline: set LLJBASH_ILU_OPT_SWEEP_TIMELINE before IluSolverSetup (line-pipeline sweeps of "
+                "structured factors only)");
+        const int nblk = im->GP.g.nblk;
+        const size_t len = static_cast<size_t>(nblk) * gb300::kLineTimeline;
+        if (out != nullptr) {
+            if (cap < 0 || static_cast<size_t>(cap) < len) throw std::runtime_error("timeline buffer too small");
+            int prev = 0;
+            GB_CUDA_CHECK(cudaGetDevice(&prev));
+            GB_CUDA_CHECK(cudaSetDevice(im->dev.device));
+            GB_CUDA_CHECK(cudaDeviceSynchronize());
+            GB_CUDA_CHECK(cudaMemcpy(out, buf.get(), len * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+            GB_CUDA_CHECK(cudaSetDevice(prev));
+        }
+        return nblk;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
 }
 
 int LLJBASH_Gb300TreeSchedule(int n, const int* row_ptr, const int* col_idx, int upper, int nproc, int granularity,

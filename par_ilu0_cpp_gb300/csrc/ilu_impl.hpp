@@ -114,12 +114,16 @@ struct LinePack {
     DeviceBuffer<int> order;        // [nblk] block of each ticket
     DeviceBuffer<double> l64, u64;  // [4 slots]
     DeviceBuffer<float> l32, u32;
+    // per-block timelines [fp32][upper] of the last sweep of each kind (allocated only
+    // with the timeline option on)
+    DeviceBuffer<unsigned long long> tl[2][2];
 
     template <class T>
     LineTri<T> view(bool upper) const {
         LineTri<T> p;
         p.g = g;
         p.order = order.get();
+        p.tl = tl[sizeof(T) == 4 ? 1 : 0][upper ? 1 : 0].get();
         if constexpr (sizeof(T) == 8) {
             p.coef = upper ? u64.get() : l64.get();
         } else {
@@ -190,6 +194,7 @@ struct IluSolver::Impl {
     int grid_by = 0;    // requested warps of a CTA along y (0 automatic)
     int grid_bz = 0;    // requested warps of a CTA along z (0 automatic)
     int grid_cluster = 1;  // 1: clusters along z of 16, else 8 CTAs; 2 .. 16: at most that many; 0: none
+    bool sweep_timeline = false;  // record per-block timelines of the line-pipeline sweeps
     // line-pipeline sweeps in use per value type (bit 0: forward, bit 1: backward); in
     // automatic mode chosen at the first Factorize after SetupMatrix by timing each sweep
     // against the block-local / level-ordered kernel

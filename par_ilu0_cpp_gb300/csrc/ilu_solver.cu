@@ -1233,6 +1233,16 @@ void IluSolver::SetupMatrix() {
                 (bz >= by ? bz : by) = std::max(1, (bz >= by ? bz : by) / 2);
             }
             im.grid32 = configure_line<float>(im.GP, im.dev, false, 0);
+            for (int f = 0; f < 2; ++f)
+                for (int u = 0; u < 2; ++u) {
+                    auto& buf = im.GP.tl[f][u];
+                    buf.release();
+                    if (im.sweep_timeline && (f == 0 ? im.grid64 : im.grid32)) {
+                        const size_t len = static_cast<size_t>(im.GP.g.nblk) * kLineTimeline;
+                        buf.reserve(len);
+                        GB_CUDA_CHECK(cudaMemsetAsync(buf.get(), 0, len * sizeof(unsigned long long), s));
+                    }
+                }
             const std::vector<int> order = line_block_order(im.GP.g);
             im.GP.order.upload(order.data(), order.size(), s);
             GB_CUDA_CHECK(cudaStreamSynchronize(s));  // `order` must outlive the copy

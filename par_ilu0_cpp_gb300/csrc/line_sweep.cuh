@@ -66,7 +66,32 @@ struct LineTri {
     const int* order = nullptr;  // [nblk] block (iy + nby iz, sweep coordinates) of each ticket;
                                  // with clusters [nby nbzc]: cluster (iy + nby izc) of each ticket
     const T* coef = nullptr;     // [slots][4]: c_z, c_y, c_x, d (d: u_ii FP64 / RN(1 / u_ii) FP32; L: unused)
+    unsigned long long* tl = nullptr;  // per-block timeline [nblk][kLineTimeline] (null: off)
 };
+
+// Timeline record of one block (nanoseconds of %globaltimer): [0] compute start (faces
+// reset, after the CTA barrier), [1] SM id, [2 + w] end of compute warp w (w < nw), [2 +
+// nw] end of the halo warp; unused entries 0.
+constexpr int kLineTimeline = 12;
+
+__device__ __forceinline__ unsigned sm_id() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+    return r;
+}
+template <class T>
+__device__ __forceinline__ void line_stamp_start(const LineTri<T>& P, int blk) {
+    if (P.tl != nullptr && threadIdx.x == 0) {
+        unsigned long long* r = P.tl + static_cast<long long>(blk) * kLineTimeline;
+        r[0] = global_ns();
+        r[1] = sm_id();
+    }
+}
+template <class T>
+__device__ __forceinline__ void line_stamp_end(const LineTri<T>& P, int blk) {
+    if (P.tl != nullptr && (threadIdx.x & 31) == 0)
+        P.tl[static_cast<long long>(blk) * kLineTimeline + 2 + (threadIdx.x >> 5)] = global_ns();
+}
 
 // ---- asynchronous global -> shared copies (cp.async, per thread) ----
 // src_bytes = 0 fills the destination with zeros without reading the source.
@@ -460,10 +485,12 @@ __global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
                               static_cast<long long>(P.g.steps) * 128 * static_cast<long long>(sizeof(T)),
                               threadIdx.x & 31);
         __syncthreads();
+        line_stamp_start(P, blk);
         if (w < nw)
             line_warp<T, UPPER>(P, blk, in, scaled, sc, out, faceY, faceZ, zero_word, cring, bring, 0u, status);
         else
             line_halo<T, UPPER>(P, blk, out, faceY, faceZ, true, status);
+        line_stamp_end(P, blk);
         if (scaled) {
             __syncthreads();
             line_rescale_block<T>(P.g, iy, iz, in, sc);
@@ -529,10 +556,12 @@ __global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
         if (active) {
             const bool push = rank + 1 < CL && iz + 1 < P.g.nbz;
             const unsigned remote = push ? map_shared_rank(faceZ, rank + 1) : 0u;
+            line_stamp_start(P, blk);
             if (w < nw)
                 line_warp<T, UPPER>(P, blk, in, scaled, sc, out, faceY, faceZ, zero_word, cring, bring, remote, status);
             else
                 line_halo<T, UPPER>(P, blk, out, faceY, faceZ, rank == 0, status);
+            line_stamp_end(P, blk);
             if (scaled) {
                 __syncthreads();
                 line_rescale_block<T>(P.g, iy, iz, in, sc);

@@ -256,6 +256,13 @@ def test_ilu_option_values_checked():
     for v in (-1, 17, 2.5):
         with pytest.raises(RuntimeError):
             ilu.set_option(api.ILU_OPT_GRID_CLUSTER, v)
+    for v in (0, 1):
+        ilu.set_option(api.ILU_OPT_SWEEP_TIMELINE, v)
+    for v in (2, -1):
+        with pytest.raises(RuntimeError):
+            ilu.set_option(api.ILU_OPT_SWEEP_TIMELINE, v)
+    with pytest.raises(RuntimeError):  # nothing recorded before SetupMatrix
+        ilu.sweep_timeline(False, False)
     for v in (0, 1, 2):
         ilu.set_option(api.ILU_OPT_TICKET_ORDER, v)
     with pytest.raises(RuntimeError):

@@ -16,6 +16,7 @@ import oracle
 from conftest import rel_err
 from par_ilu0_cpp_gb300 import api
 from par_ilu0_cpp_gb300 import generators as g
+from par_ilu0_cpp_gb300 import sweep_timeline
 
 pytestmark = pytest.mark.gpu
 
@@ -186,3 +187,32 @@ def test_grid_clusters_match_plain_line_kernel(make, cluster):
     assert np.array_equal(plain.substitute(b), x)
     assert np.array_equal(clus.substitute(b), x)
     assert np.array_equal(clus.substitute(b), x)
+
+
+def test_sweep_timeline_records_every_block_without_changing_results():
+    """LLJBASH_ILU_OPT_SWEEP_TIMELINE: every block of the last sweep of each kind has its
+    start, SM and warp end stamps, in order, and the results stay bit-identical."""
+    a = g.convdiff3d(40, 24, 70)
+    f, _ = api.iluk_symbolic(a, 0)
+    plain = solver(f)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_GRID, 1)
+    ilu.set_option(api.ILU_OPT_SWEEP_TIMELINE, 1)
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0 and ilu.factorize() == 0, api.last_error()
+    _, b = g.random_rhs(a, seed=5)
+    assert np.array_equal(ilu.substitute(b), plain.substitute(b))
+    info = ilu.info()
+    nw = info.grid_cta_y * info.grid_cta_z
+    for upper in (False, True):
+        tl = ilu.sweep_timeline(upper, False).astype(np.int64)
+        assert tl.shape == (info.grid_blocks, api.LINE_TIMELINE_WORDS)
+        start, ends = tl[:, 0], tl[:, 2:3 + nw]
+        assert (start > 0).all() and (ends >= start[:, None]).all()
+        assert (tl[:, 3 + nw:] == 0).all()
+        assert (tl[:, 1] < 1024).all()
+        s = sweep_timeline.summarize(tl.astype(np.uint64), info)
+        assert s["blocks"] == info.grid_blocks and s["span_us"] > 0
+    # timelines off: nothing to read
+    with pytest.raises(RuntimeError):
+        plain.sweep_timeline(False, False)
