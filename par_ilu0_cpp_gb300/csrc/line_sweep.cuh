@@ -435,23 +435,58 @@ __device__ __forceinline__ void line_reset_faces(const LineGeom& g, int iy, int 
     if (threadIdx.x == 0) *zero_word = T(0);
 }
 
-// GMRES normalises its new Krylov vector in the forward sweep: the block's rows of `in`
-// (planes z of its z-lines, rows of its y-lines: contiguous runs) are rescaled in one
-// coalesced pass once every warp is done reading them (the same product b * scale the
-// rows used).  Called after a barrier.
+// GMRES normalises its new Krylov vector in the forward sweep: once a compute warp is
+// done with its lines (its own lanes are the only readers of their rows of `in`, and
+// all their copies have landed), it rescales them in place, the same product b * scale
+// its rows used.  Its y-lines of one plane z are one contiguous run of rows, walked by
+// the whole warp, 16 bytes per access where the runs allow it (eight accesses in flight
+// per lane).
 template <class T>
-__device__ __forceinline__ void line_rescale_block(const LineGeom& g, int iy, int iz, T* in, T sc) {
-    const int y0 = iy * g.by * g.wy, y1 = min(g.ny, y0 + g.by * g.wy);
-    const int z0 = iz * g.bz * g.wz, z1 = min(g.nz, z0 + g.bz * g.wz);
+__device__ __forceinline__ void line_rescale_warp(const LineGeom& g, int blk, T* in, T sc) {
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int wyi = w % g.by, wzi = w / g.by;
+    const int iy = blk % g.nby, iz = blk / g.nby;
+    const int y0 = (iy * g.by + wyi) * g.wy, y1 = min(g.ny, y0 + g.wy);
+    const int z0 = (iz * g.bz + wzi) * g.wz, z1 = min(g.nz, z0 + g.wz);
+    if (y0 >= y1 || z0 >= z1) return;
     const long long run = static_cast<long long>(g.nx) * (y1 - y0);
-    for (int z = z0; z < z1; ++z) {
-        T* p = in + static_cast<long long>(g.nx) * (y0 + static_cast<long long>(g.ny) * z);
-        for (long long i = threadIdx.x; i < run; i += blockDim.x) p[i] = p[i] * sc;
+    const long long plane = static_cast<long long>(g.nx) * g.ny;
+    T* const base = in + static_cast<long long>(g.nx) * y0 + plane * z0;
+    constexpr int V = 16 / sizeof(T);  // rows per 16-byte access
+    const bool vec = run % V == 0 && plane % V == 0 && (reinterpret_cast<unsigned long long>(base) & 15ull) == 0;
+    if (vec) {
+        const int rv = static_cast<int>(run / V);
+        for (int zi = 0; zi < z1 - z0; ++zi) {
+#pragma unroll 8
+            for (int e = lane; e < rv; e += 32) {
+                T* p = base + zi * plane + static_cast<long long>(e) * V;
+                if constexpr (sizeof(T) == 4) {
+                    float4 v = *reinterpret_cast<const float4*>(p);
+                    v.x *= sc;
+                    v.y *= sc;
+                    v.z *= sc;
+                    v.w *= sc;
+                    *reinterpret_cast<float4*>(p) = v;
+                } else {
+                    double2 v = *reinterpret_cast<const double2*>(p);
+                    v.x *= sc;
+                    v.y *= sc;
+                    *reinterpret_cast<double2*>(p) = v;
+                }
+            }
+        }
+    } else {
+        for (int zi = 0; zi < z1 - z0; ++zi) {
+            T* const q = base + zi * plane;
+#pragma unroll 8
+            for (long long e = lane; e < run; e += 32) q[e] = q[e] * sc;
+        }
     }
 }
 
 // Forward (UPPER = false): out = L^{-1} (scale * in), in rescaled in place when `scale`
-// is given (block by block, after the block's solve); backward (UPPER = true):
+// is given (each compute warp's lines once that warp has solved them); backward (UPPER = true):
 // out = U^{-1} in.  in / out in natural order; out holds the sentinel at every row on
 // entry.  nw compute warps + 1 halo warp; dynamic shared memory line_smem_bytes.
 template <class T, bool UPPER>
@@ -491,10 +526,7 @@ __global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
         else
             line_halo<T, UPPER>(P, blk, out, faceY, faceZ, true, status);
         line_stamp_end(P, blk);
-        if (scaled) {
-            __syncthreads();
-            line_rescale_block<T>(P.g, iy, iz, in, sc);
-        }
+        if (scaled && w < nw) line_rescale_warp<T>(P.g, blk, in, sc);
     }
 }
 
@@ -562,10 +594,7 @@ __global__ void __launch_bounds__((kLineMaxWarps + 1) * kWarp, 1)
             else
                 line_halo<T, UPPER>(P, blk, out, faceY, faceZ, rank == 0, status);
             line_stamp_end(P, blk);
-            if (scaled) {
-                __syncthreads();
-                line_rescale_block<T>(P.g, iy, iz, in, sc);
-            }
+            if (scaled && w < nw) line_rescale_warp<T>(P.g, blk, in, sc);
         }
         __syncthreads();
     }
