@@ -418,12 +418,18 @@ int LLJBASH_IluSolverGetSweepTimeline(IluSolverHdl hdl, int upper, int fp32, uns
         const size_t len = static_cast<size_t>(nblk) * gb300::kLineTimeline;
         if (out != nullptr) {
             if (cap < 0 || static_cast<size_t>(cap) < len) throw std::runtime_error("timeline buffer too small");
-            int prev = 0;
-            GB_CUDA_CHECK(cudaGetDevice(&prev));
-            GB_CUDA_CHECK(cudaSetDevice(im->dev.device));
+            // the solver's device for the wait and the copy, the caller's current device
+            // back afterwards (also when either fails)
+            struct CurrentDevice {
+                int prev = 0;
+                explicit CurrentDevice(int d) {
+                    GB_CUDA_CHECK(cudaGetDevice(&prev));
+                    GB_CUDA_CHECK(cudaSetDevice(d));
+                }
+                ~CurrentDevice() { cudaSetDevice(prev); }
+            } current(im->dev.device);
             GB_CUDA_CHECK(cudaDeviceSynchronize());
             GB_CUDA_CHECK(cudaMemcpy(out, buf.get(), len * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-            GB_CUDA_CHECK(cudaSetDevice(prev));
         }
         return nblk;
     } catch (const std::exception& e) {
