@@ -129,7 +129,11 @@ enum {
     LLJBASH_ILU_OPT_GRID_CLUSTER = 13,
     /* 1: record a per-block timeline of every line-pipeline sweep (read with
      * LLJBASH_IluSolverGetSweepTimeline); 0 (default) off.  Next IluSolverSetup. */
-    LLJBASH_ILU_OPT_SWEEP_TIMELINE = 14
+    LLJBASH_ILU_OPT_SWEEP_TIMELINE = 14,
+    /* 1: line-pipeline CTAs request more than half of an SM's shared memory, so that no
+     * two share an SM; 0 (default) their own size.  Results are the same.  Next
+     * IluSolverSetup. */
+    LLJBASH_ILU_OPT_GRID_ONE_CTA_PER_SM = 15
 };
 int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value);
 

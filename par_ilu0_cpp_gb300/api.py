@@ -76,6 +76,7 @@ ILU_OPT_GRID_CTA_Y = 8
 ILU_OPT_GRID_CTA_Z = 9
 ILU_OPT_GRID_CLUSTER = 13
 ILU_OPT_SWEEP_TIMELINE = 14
+ILU_OPT_GRID_ONE_CTA_PER_SM = 15
 LINE_TIMELINE_WORDS = 12  # values per block of a sweep timeline
 ILU_OPT_TICKET_ORDER = 11
 ILU_OPT_FACTOR_KERNEL = 12

@@ -183,6 +183,10 @@ int LLJBASH_IluSolverSetOption(IluSolverHdl hdl, int option, double value) {
                 (option == LLJBASH_ILU_OPT_GRID_CTA_Y ? s->impl()->grid_by : s->impl()->grid_bz) =
                     static_cast<int>(value);
                 return 0;
+            case LLJBASH_ILU_OPT_GRID_ONE_CTA_PER_SM:
+                if (value != 0 && value != 1) throw std::runtime_error("one CTA per SM must be 0 or 1");
+                s->impl()->grid_one_cta_per_sm = value != 0;
+                return 0;
             case LLJBASH_ILU_OPT_SWEEP_TIMELINE:
                 if (value != 0 && value != 1) throw std::runtime_error("sweep timeline must be 0 or 1");
                 s->impl()->sweep_timeline = value != 0;

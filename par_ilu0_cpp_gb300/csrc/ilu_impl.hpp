@@ -111,6 +111,7 @@ struct LinePack {
     LineGeom g;
     int threads = 0;  // CTA size: nw warps
     int grid = 0;     // CTAs launched
+    int smem_floor = 0;  // dynamic shared memory requested at least (bytes; one CTA per SM)
     DeviceBuffer<int> order;        // [nblk] block of each ticket
     DeviceBuffer<double> l64, u64;  // [4 slots]
     DeviceBuffer<float> l32, u32;
@@ -195,6 +196,7 @@ struct IluSolver::Impl {
     int grid_bz = 0;    // requested warps of a CTA along z (0 automatic)
     int grid_cluster = 1;  // 1: clusters along z of 16, else 8 CTAs; 2 .. 16: at most that many; 0: none
     bool sweep_timeline = false;  // record per-block timelines of the line-pipeline sweeps
+    bool grid_one_cta_per_sm = false;  // line-pipeline CTAs request enough shared memory to be alone on an SM
     // line-pipeline sweeps in use per value type (bit 0: forward, bit 1: backward); in
     // automatic mode chosen at the first Factorize after SetupMatrix by timing each sweep
     // against the block-local / level-ordered kernel

@@ -893,7 +893,7 @@ static cudaLaunchConfig_t line_cluster_config(int grid, int threads, size_t smem
 // clusters of at most that many CTAs; with 0, none.
 template <class T>
 static bool configure_line(LinePack& G, const DeviceInfo& dev, bool try_cluster, int max_cluster) {
-    const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
+    const size_t smem = std::max(static_cast<size_t>(line_smem_bytes<T>(G.g)), static_cast<size_t>(G.smem_floor));
     if (smem + 1024 > static_cast<size_t>(dev.smem_optin)) return false;
     if (try_cluster) {
         G.g.cl = 0;
@@ -975,7 +975,7 @@ static void pack_line(LinePack& G, const int* rp, const int* diag, const double*
 template <class T, bool UPPER>
 static void launch_line(const LinePack& G, cudaStream_t s, T* in, const double* scale, T* out, unsigned* counter,
                         int* status, const int* gate, int step) {
-    const size_t smem = static_cast<size_t>(line_smem_bytes<T>(G.g));
+    const size_t smem = std::max(static_cast<size_t>(line_smem_bytes<T>(G.g)), static_cast<size_t>(G.smem_floor));
     if (G.g.cl > 0) {
         cudaLaunchAttribute attr[1];
         cudaLaunchConfig_t cfg = line_cluster_config(G.grid, G.threads, smem, G.g.cl, s, attr);
@@ -1226,6 +1226,10 @@ void IluSolver::SetupMatrix() {
             for (int attempt = 0; attempt < 8; ++attempt) {
                 im.GP.g = line_geometry(gx, gy, gz, im.grid_wy, by, bz);
                 im.GP.threads = (im.GP.g.nw() + 1) * kWarp;  // compute warps + the halo warp
+                // one CTA per SM on request: more than half of an SM's shared memory
+                im.GP.smem_floor = im.grid_one_cta_per_sm
+                                       ? std::min(im.dev.smem_per_sm / 2 + 1024, im.dev.smem_optin - 1024)
+                                       : 0;
                 im.grid64 = configure_line<double>(im.GP, im.dev, true, im.grid_cluster);
                 if (im.grid64 || im.GP.g.nw() == 1) break;
                 by = im.GP.g.by;

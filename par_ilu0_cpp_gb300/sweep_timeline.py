@@ -77,7 +77,7 @@ def summarize(tl: np.ndarray, info: api.IluInfo) -> dict:
     }
 
 
-def run(size: int, cta=(0, 0), cluster: int = 1) -> dict:
+def run(size: int, cta=(0, 0), cluster: int = 1, one_cta_per_sm: bool = False) -> dict:
     a = gen.convdiff3d(size)
     f, _ = api.iluk_symbolic(a, 0)
     _, b = gen.random_rhs(a, seed=1)
@@ -86,6 +86,7 @@ def run(size: int, cta=(0, 0), cluster: int = 1) -> dict:
     ilu.set_option(api.ILU_OPT_GRID_CTA_Y, cta[0])
     ilu.set_option(api.ILU_OPT_GRID_CTA_Z, cta[1])
     ilu.set_option(api.ILU_OPT_GRID_CLUSTER, cluster)
+    ilu.set_option(api.ILU_OPT_GRID_ONE_CTA_PER_SM, int(one_cta_per_sm))
     ilu.set_matrix(f)
     if ilu.setup() != 0 or ilu.factorize() != 0:
         raise RuntimeError(api.last_error())
@@ -96,7 +97,8 @@ def run(size: int, cta=(0, 0), cluster: int = 1) -> dict:
     info = ilu.info()
     out = {"workload": f"convdiff3d {size}^3 ILU(0), mixed GMRES(50)", "iterations": int(res.iterations),
            "line_shape": [info.grid_warp_y, info.grid_warp_z, info.grid_cta_y, info.grid_cta_z, info.grid_blocks],
-           "cluster": int(info.grid_cluster), "fp64_line": int(info.grid_fp64), "fp32_line": int(info.grid_fp32),
+           "cluster": int(info.grid_cluster), "one_cta_per_sm": bool(one_cta_per_sm),
+           "fp64_line": int(info.grid_fp64), "fp32_line": int(info.grid_fp32),
            "sweeps": {}}
     for fp32 in (True, False):
         for upper in (False, True):
@@ -118,8 +120,9 @@ def main() -> None:
     ap.add_argument("--cta", type=lambda v: [int(t) for t in v.split(",")], default=[0, 0],
                     help="warps of a CTA along y,z (0,0: automatic)")
     ap.add_argument("--cluster", type=int, default=1, help="LLJBASH_ILU_OPT_GRID_CLUSTER")
+    ap.add_argument("--one-cta-per-sm", action="store_true", help="LLJBASH_ILU_OPT_GRID_ONE_CTA_PER_SM")
     args = ap.parse_args()
-    r = run(args.size, args.cta, args.cluster)
+    r = run(args.size, args.cta, args.cluster, args.one_cta_per_sm)
     text = json.dumps(r, indent=1)
     print(text)
     if args.out:

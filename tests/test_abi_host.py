@@ -258,6 +258,9 @@ def test_ilu_option_values_checked():
             ilu.set_option(api.ILU_OPT_GRID_CLUSTER, v)
     for v in (0, 1):
         ilu.set_option(api.ILU_OPT_SWEEP_TIMELINE, v)
+        ilu.set_option(api.ILU_OPT_GRID_ONE_CTA_PER_SM, v)
+    with pytest.raises(RuntimeError):
+        ilu.set_option(api.ILU_OPT_GRID_ONE_CTA_PER_SM, 2)
     for v in (2, -1):
         with pytest.raises(RuntimeError):
             ilu.set_option(api.ILU_OPT_SWEEP_TIMELINE, v)

@@ -216,3 +216,27 @@ def test_sweep_timeline_records_every_block_without_changing_results():
     # timelines off: nothing to read
     with pytest.raises(RuntimeError):
         plain.sweep_timeline(False, False)
+
+
+def test_one_cta_per_sm_gives_the_same_results():
+    """LLJBASH_ILU_OPT_GRID_ONE_CTA_PER_SM pads the line kernels' shared memory so that
+    no two CTAs share an SM (fewer clusters resident at once): same results."""
+    a = g.convdiff3d(40, 24, 70)
+    f, _ = api.iluk_symbolic(a, 0)
+    base = solver(f)
+    ilu = api.IluSolver()
+    ilu.set_option(api.ILU_OPT_GRID, 1)
+    ilu.set_option(api.ILU_OPT_GRID_ONE_CTA_PER_SM, 1)
+    ilu.set_matrix(f)
+    assert ilu.setup() == 0 and ilu.factorize() == 0, api.last_error()
+    assert ilu.info().grid_fp64 == 3
+    _, b = g.random_rhs(a, seed=8)
+    assert np.array_equal(ilu.substitute(b), base.substitute(b))
+    x1 = api.Gmres(1e-8, 30, 500)
+    x1.set_preconditioner(ilu)
+    x1.set_option(api.GMRES_OPT_MODE, 1)
+    x2 = api.Gmres(1e-8, 30, 500)
+    x2.set_preconditioner(base)
+    x2.set_option(api.GMRES_OPT_MODE, 1)
+    r1, r2 = x1.solve(a, b), x2.solve(a, b)
+    assert r1.iterations == r2.iterations and np.array_equal(r1.x, r2.x)
