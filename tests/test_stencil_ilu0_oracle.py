@@ -1,7 +1,8 @@
 """The diagonal recurrence of ILU(0) on full 7-point / 5-point stencils (oracle, CPU)
-against the port of the reference's row elimination: the same factor values, entry by
-entry, so a line-pipeline factorisation of such matrices (the sweep's dependency
-structure, one division per step) computes the reference's factors."""
+against the port of the reference's row elimination and against the reference's own
+code (its build without contraction or fast-math, where it loads): the same factor
+values, entry by entry, so a line-pipeline factorisation of such matrices (the sweep's
+dependency structure, one division per step) computes the reference's factors."""
 import platform
 
 import numpy as np
@@ -16,6 +17,14 @@ from par_ilu0_cpp_gb300 import generators as g
 def port():
     oracle.build_port()
     return oracle.Port()
+
+
+@pytest.fixture(scope="module")
+def ref():
+    try:
+        return oracle.Ref(oracle.REF_STRICT_SO)
+    except OSError as e:
+        pytest.skip(f"reference build not loadable here: {e}")
 
 
 CASES = [
@@ -41,6 +50,13 @@ def test_diagonal_recurrence_matches_row_elimination(port, name, make, dims):
     rows = np.repeat(np.arange(a.n), np.diff(rp))
     upper = ci > rows
     assert np.array_equal(lu[upper], a.values[upper])
+
+
+@pytest.mark.parametrize("name,make,dims", CASES, ids=[c[0] for c in CASES])
+def test_diagonal_recurrence_matches_the_reference_build(ref, name, make, dims):
+    a = make()
+    lu_ref, _ = ref.factorize(a)
+    assert np.array_equal(stencil_ilu0(a, *dims), lu_ref), name
 
 
 def test_recurrence_rejects_other_shapes():
